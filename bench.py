@@ -1,0 +1,328 @@
+"""Benchmark of the GB300 clustering hot path.
+
+Workload (one "step" = one full ParallelModularityClusterer::Cluster on the
+graph): RMAT scale 22, edge factor 16, a/b/c/d = 0.57/0.19/0.19/0.05,
+symmetrised, deduplicated, self-loops removed (~60M undirected edges), unit
+weights; modularity resolution 1.0, refine, NBHR_MOVE, synchronous moves.
+Synthetic data from a seeded generator (no dataset download).
+
+Metric: best-move edge visits per second -- an edge visit is one adjacency
+entry scanned by a best-move evaluation; the count is summed over every
+round, level and refinement pass, identically to the oracle.
+
+  value   edge visits / device time of Cluster() with the graph resident in
+          HBM (CUDA events on the library's stream, summed over the steps)
+  e2e     the same metric through pcc_cluster_host_csr on pinned host
+          buffers: upload + cluster + label download every step
+  --impl reference   the oracle (the CPU restatement of the reference
+          clusterer) on the host cores, same config, bounded sample
+
+Multi-GPU: the path does not shard (a Louvain round needs the whole graph's
+cluster state), so N GPUs run N independent replicas ("replicas only").
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "parallel-correlation-clustering_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "best-move edge-visits/s"
+UNIT = "edge-visits/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=int, default=22)
+    ap.add_argument("--async", dest="async_", action="store_true")
+    ap.add_argument("--cpu-scale", type=int, default=20,
+                    help="RMAT scale of the bounded CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def config_dict(args, n, m):
+    return {
+        "workload": f"rmat{args.scale}_ef16_modularity_refine_nbhr_{'async' if args.async_ else 'sync'}",
+        "graph": f"RMAT scale {args.scale}, edge factor 16, a/b/c/d=0.57/0.19/0.19/0.05, symmetrised, "
+                 "deduplicated, self-loops removed, unit weights",
+        "n": n, "m_entries": m, "undirected_edges": m // 2,
+        "clusterer": "ParallelModularityClusterer", "resolution": 1.0, "refine": True,
+        "move_method": "NBHR_MOVE", "async": bool(args.async_),
+        "louvain_num_iterations": 10, "louvain_num_inner_iterations": 10,
+        "l2": "inputs larger than L2 (CSR > 129 MB), no flush",
+        "parallelism": "replicas",
+    }
+
+
+def make_cfg(P, args):
+    return P.make_config(resolution=1.0, refine=True, move_method=P.NBHR_MOVE, async_=args.async_,
+                         random_seed=1)
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.idx = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(args, P, G):
+    """The oracle on the host cores, bounded sample: the same config on an
+    RMAT graph of scale --cpu-scale (edge visits/s is size-normalised)."""
+    import oracle as O
+    O.set_threads(0)
+    threads = O.get_threads()
+    g = G.rmat(args.cpu_scale, 16, seed=1)
+    og = O.OracleGraph(g)
+    cfg = make_cfg(P, args)
+    t = time.perf_counter()
+    _, st = O.modularity_cluster(og, cfg)
+    dt = time.perf_counter() - t
+    return {
+        "value": st["edge_visits"] / dt, "unit": UNIT, "cores": threads, "kind": "port",
+        "sample": f"one full clustering of RMAT scale {args.cpu_scale} (n={g.n}, m={g.m}) with the same "
+                  f"config; {st['edge_visits']} edge visits in {dt:.2f} s",
+        "modularity": st["modularity"],
+    }
+
+
+def run_reference(args):
+    """--impl reference: the oracle port on all host threads; rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import pcc_gb300 as P
+    import pcc_graphs as G
+    import oracle as O
+    import build_native
+    build_native.build_host()
+    O.build()
+    O.set_threads(0)
+    threads = O.get_threads()
+    g = G.rmat(args.cpu_scale, 16, seed=1)
+    og = O.OracleGraph(g)
+    cfg = make_cfg(P, args)
+    for _ in range(args.warmup):
+        O.modularity_cluster(og, cfg)
+    total_ev = 0
+    total_t = 0.0
+    mod = None
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        _, st = O.modularity_cluster(og, cfg)
+        total_t += time.perf_counter() - t
+        total_ev += st["edge_visits"]
+        mod = st["modularity"]
+    value = total_ev / total_t
+    sample = (f"each step one full clustering of RMAT scale {args.cpu_scale} (n={g.n}, m={g.m}), "
+              f"same config as the GPU arm (scale {args.scale})")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded RMAT generator)", "config": config_dict(args, g.n, g.m),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "quality": {"modularity": mod},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+    import pcc_gb300 as P
+    import pcc_graphs as G
+    import build_native
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    build_native.build_all()
+
+    g = G.rmat(args.scale, 16, seed=1)
+    ctx = P.Context(local)
+    dg = ctx.upload(g)
+    cfg = make_cfg(P, args)
+
+    def barrier():
+        torch.cuda.synchronize(local)
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(max(args.warmup, 0)):
+        P.modularity_cluster(dg, cfg)
+
+    # Timed region: K full clusterings on the resident graph.
+    sampler = ClockSampler(local)
+    barrier()
+    sampler.start()
+    wall0 = time.perf_counter()
+    ev = 0
+    vv = 0
+    dev_ms = 0.0
+    bm_ms = 0.0
+    comp_ms = 0.0
+    algo_bytes = 0
+    launches = 0
+    quality = {}
+    for _ in range(args.steps):
+        labels, st = P.modularity_cluster(dg, cfg)
+        ev += st["edge_visits"]
+        vv += st["vertex_visits"]
+        dev_ms += st["ms_total"]
+        bm_ms += st["ms_best_moves"]
+        comp_ms += st["ms_compress"]
+        launches += st["kernel_launches"]
+        algo_bytes += st["algo_bytes_best_moves"]
+        quality = {"modularity": st["modularity"], "objective": st["objective"],
+                   "num_clusters": st["num_clusters"], "levels": st["levels"], "rounds": st["rounds"]}
+    barrier()
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+
+    # End to end through the public C ABI from pinned host memory.
+    off_h = torch.from_numpy(g.offsets.view(np.int64)).pin_memory()
+    nbr_h = torch.from_numpy(g.neighbors.view(np.int32)).pin_memory()
+    g_pinned = P.CsrGraph(off_h.numpy().view(np.uint64), nbr_h.numpy().view(np.uint32), None)
+    P.cluster_host_csr(ctx, g_pinned, cfg, objective=1)
+    barrier()
+    e2e_t = 0.0
+    e2e_ev = 0
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        lab, st = P.cluster_host_csr(ctx, g_pinned, cfg, objective=1)
+        e2e_t += time.perf_counter() - t
+        e2e_ev += st["edge_visits"]
+    barrier()
+
+    # Max time over ranks; edge visits summed over ranks.
+    dev_s = dev_ms / 1000.0
+    if dist is not None:
+        t = torch.tensor([dev_s, e2e_t], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        s = torch.tensor([ev, e2e_ev], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(s, op=dist.ReduceOp.SUM)
+        dev_s, e2e_t = float(t[0]), float(t[1])
+        ev_all, e2e_ev_all = float(s[0]), float(s[1])
+    else:
+        ev_all, e2e_ev_all = float(ev), float(e2e_ev)
+
+    if rank == 0:
+        peak, peak_kind = measured_peak()
+        achieved = (algo_bytes / (bm_ms / 1000.0)) / 1e9 if bm_ms > 0 else None
+        cpu = None
+        if not args.no_cpu_baseline:
+            try:
+                cpu = cpu_baseline(args, P, G)
+            except Exception as e:  # the baseline is reported, never required
+                cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {e}"}
+        line = {
+            "metric": METRIC, "value": ev_all / dev_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded RMAT generator)",
+            "config": config_dict(args, g.n, g.m),
+            "e2e": {"value": e2e_ev_all / e2e_t, "unit": UNIT,
+                    "h2d_bytes_per_step": int(g.offsets.nbytes + g.neighbors.nbytes),
+                    "d2h_bytes_per_step": int(4 * g.n)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": None,
+                         "kernel": "best-move kernels (degree bins), algorithmic bytes "
+                                   "8 or 12 B per edge visit + 40 B per vertex visit",
+                         "peak_kind": f"{peak_kind} hbm_gbs"},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": launches,
+            "phases_ms_per_step": {"total": dev_ms / args.steps, "best_moves": bm_ms / args.steps,
+                                   "compress": comp_ms / args.steps},
+            "wall_s": wall,
+            "quality": quality,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,240 @@
+/*
+ * pcc_gb300.h -- C ABI of the GB300 (sm_103a) correlation / modularity
+ * clustering library (libpcc_gb300.so).
+ *
+ * This is the drop-in boundary for the Louvain-style hot path of the
+ * reference's ParallelCorrelationClusterer / ParallelModularityClusterer:
+ * best-move rounds, graph compression and multilevel refinement.  Every
+ * signature uses plain pointers and sizes; no C++ or torch types cross it.
+ * The C++ InMemoryClusterer mirror (pcc_clusterer.h) and the Python
+ * binding are the callers.
+ *
+ * Graph layout (host and device): symmetric CSR.
+ *   offsets   uint64[n+1]   row i = entries [offsets[i], offsets[i+1])
+ *   neighbors uint32[m]     neighbour vertex id of each entry
+ *   weights   float[m]      edge weight of each entry, or NULL for unit weights
+ * Each undirected edge appears in both rows, as in the reference's GBBS
+ * symmetric_ptr_graph<symmetric_vertex, float> (clustering/gbbs-graph.h:39-56).
+ *
+ * Status codes are numerically identical to absl::StatusCode, the error
+ * type of the reference (clustering/status_macros.h:26-60).
+ */
+#ifndef PCC_GB300_H_
+#define PCC_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pcc_status {
+  PCC_OK = 0,
+  PCC_CANCELLED = 1,
+  PCC_UNKNOWN = 2,
+  PCC_INVALID_ARGUMENT = 3,
+  PCC_DEADLINE_EXCEEDED = 4,
+  PCC_NOT_FOUND = 5,
+  PCC_ALREADY_EXISTS = 6,
+  PCC_PERMISSION_DENIED = 7,
+  PCC_RESOURCE_EXHAUSTED = 8,
+  PCC_FAILED_PRECONDITION = 9,
+  PCC_ABORTED = 10,
+  PCC_OUT_OF_RANGE = 11,
+  PCC_UNIMPLEMENTED = 12,
+  PCC_INTERNAL = 13,
+  PCC_UNAVAILABLE = 14,
+  PCC_DATA_LOSS = 15
+} pcc_status;
+
+/* CorrelationClustererConfig.ClusteringMovesMethod (clustering/config.proto:122-130) */
+enum { PCC_DEFAULT_CLUSTER_MOVES = 0, PCC_LOUVAIN = 1 };
+/* CorrelationClustererConfig.SubclusteringMethod (config.proto:132-137) */
+enum {
+  PCC_NONE_SUBCLUSTERING = 0,
+  PCC_TRIANGLE_SUBCLUSTERING = 1,
+  PCC_CONNECTIVITY_SUBCLUSTERING = 2,
+  PCC_SLOW_CONNECTIVITY_SUBCLUSTERING = 3
+};
+/* CorrelationClustererConfig.MoveMethod (config.proto:155-160) */
+enum { PCC_NBHR_CLUSTER_MOVE = 0, PCC_ALL_MOVE = 1, PCC_NBHR_MOVE = 2 };
+
+/*
+ * Plain-C mirror of research_graph.in_memory.CorrelationClustererConfig
+ * (clustering/config.proto:94-165) plus LouvainConfig (config.proto:176-183).
+ * pcc_config_default() gives the proto defaults: every number 0, LOUVAIN,
+ * NONE_SUBCLUSTERING, NBHR_CLUSTER_MOVE, all flags false.
+ */
+typedef struct pcc_config {
+  double resolution;                   /* tag 1 */
+  double edge_weight_offset;           /* tag 2 */
+  int64_t num_iterations;              /* tag 4 (DEFAULT_CLUSTER_MOVES rounds) */
+  int64_t louvain_num_iterations;      /* louvain_config.num_iterations */
+  int64_t louvain_num_inner_iterations;/* louvain_config.num_inner_iterations */
+  int32_t clustering_moves_method;     /* tag 9 */
+  int32_t subclustering_method;        /* tag 10 */
+  int32_t preclustering_method;        /* tag 11, parsed and ignored as in the reference */
+  int32_t move_method;                 /* tag 16 */
+  int32_t refine;                      /* tag 13 */
+  int32_t async;                       /* tag 14 */
+  int32_t permute;                     /* tag 18 */
+  int32_t all_iter;                    /* tag 17, sequential clusterers only */
+  uint64_t random_seed;                /* tag 3; also seeds permute / async order */
+} pcc_config;
+
+/* Per-call counters and phase times, filled by the clustering entry points. */
+typedef struct pcc_stats {
+  uint64_t edge_visits;      /* sum of deg(v) over every best-move evaluation */
+  uint64_t vertex_visits;    /* number of best-move evaluations */
+  uint64_t moves;            /* vertices that changed cluster */
+  int32_t levels;            /* compression levels whose best moves ran */
+  int32_t rounds;            /* best-move rounds, all levels and refinement */
+  int32_t refine_passes;     /* refinement levels run */
+  int32_t num_clusters;      /* clusters in the returned clustering */
+  double objective;          /* ComputeObjective of the result on the input graph */
+  double modularity;         /* modularity runs: ComputeModularity, else 0 */
+  double ms_total;           /* device time of the whole call (CUDA events) */
+  double ms_best_moves;      /* device time spent in best-move kernels */
+  double ms_compress;        /* device time spent in graph compression */
+  uint64_t kernel_launches;  /* CUDA kernels this call launched */
+  uint64_t algo_bytes_best_moves; /* algorithmic bytes of the best-move kernels:
+                                     (8 or 12) per edge visit + 40 per vertex
+                                     visit (8 when the graph has no weights) */
+} pcc_stats;
+
+void pcc_config_default(pcc_config* config);
+
+/* ------------------------------------------------------------------------
+ * Context: one GPU, one CUDA stream, one stream-ordered memory pool.
+ * Replaces the reference's implicit global GBBS scheduler; one context per
+ * host thread.  hbm_budget_bytes = 0 means "no budget" (device capacity).
+ * ---------------------------------------------------------------------- */
+typedef struct pcc_context pcc_context;
+typedef struct pcc_graph pcc_graph;
+
+pcc_status pcc_create(pcc_context** out, int device, uint64_t hbm_budget_bytes);
+void pcc_destroy(pcc_context* ctx);
+/* Message of the last failed call on this context ("" if none). */
+const char* pcc_last_error(const pcc_context* ctx);
+/* Library version string. */
+const char* pcc_version(void);
+/* Bytes of device memory currently held by the context. */
+uint64_t pcc_device_bytes_in_use(const pcc_context* ctx);
+
+/*
+ * Graph upload.  Copies a host CSR graph into HBM.  Replaces
+ * GbbsGraph::Import/FinishImport (clustering/gbbs-graph.cc:32-76) and the
+ * CLI's CopyGraph injection (clustering/cluster-in-memory_main.cc:231-306).
+ * weights == NULL stores a unit-weight graph with no weight array.
+ */
+pcc_status pcc_graph_upload(pcc_context* ctx, uint32_t n, uint64_t m,
+                            const uint64_t* offsets, const uint32_t* neighbors,
+                            const float* weights, pcc_graph** out);
+/* Same, from device pointers (device-to-device copy on the context stream). */
+pcc_status pcc_graph_upload_device(pcc_context* ctx, uint32_t n, uint64_t m,
+                                   const uint64_t* d_offsets,
+                                   const uint32_t* d_neighbors,
+                                   const float* d_weights, pcc_graph** out);
+void pcc_graph_free(pcc_context* ctx, pcc_graph* graph);
+pcc_status pcc_graph_info(const pcc_graph* graph, uint32_t* n, uint64_t* m,
+                          int32_t* has_weights);
+/* Copies the graph back to host buffers (weights may be NULL to skip). */
+pcc_status pcc_graph_download(pcc_context* ctx, const pcc_graph* graph,
+                              uint64_t* offsets, uint32_t* neighbors,
+                              float* weights);
+
+/*
+ * ParallelCorrelationClusterer::RefineClusters / Cluster
+ * (clustering/clusterers/parallel-correlation-clusterer.cc:392-653).
+ *   node_weights    host double[n] or NULL (all 1, parallel-correlation-
+ *                   clusterer-internal.h:47)
+ *   initial_labels  host uint32[n] or NULL.  NULL = all singletons (Cluster).
+ *                   Otherwise vertex i starts in cluster initial_labels[i]
+ *                   (< n), like RefineClusters(config, &clustering) with
+ *                   clustering[c] = { i : initial_labels[i] == c }.
+ *   out_labels      host uint32[n]: index of the vertex's cluster in the
+ *                   returned InMemoryClusterer::Clustering (clusters ordered
+ *                   by internal id, members ascending -- OutputIndicesById,
+ *                   parallel/parallel-sequence-ops.h:183-209).
+ */
+pcc_status pcc_correlation_cluster(pcc_context* ctx, const pcc_graph* graph,
+                                   const pcc_config* config,
+                                   const double* node_weights,
+                                   const uint32_t* initial_labels,
+                                   uint32_t* out_labels, pcc_stats* stats);
+
+/*
+ * ParallelModularityClusterer::RefineClusters / Cluster
+ * (clustering/clusterers/parallel-modularity-clusterer.cc:68-111):
+ * node weight = degree, resolution' = resolution / sum(degree), offset 0,
+ * then the correlation path; stats->modularity = ComputeModularity with the
+ * original resolution (parallel-modularity-clusterer.cc:36-66).
+ */
+pcc_status pcc_modularity_cluster(pcc_context* ctx, const pcc_graph* graph,
+                                  const pcc_config* config,
+                                  const uint32_t* initial_labels,
+                                  uint32_t* out_labels, pcc_stats* stats);
+
+/*
+ * End-to-end convenience call on host CSR buffers: upload, cluster (objective
+ * 0 = correlation, 1 = modularity), download labels, free.  The call a user
+ * without a persistent graph handle makes.
+ */
+pcc_status pcc_cluster_host_csr(pcc_context* ctx, uint32_t n, uint64_t m,
+                                const uint64_t* offsets,
+                                const uint32_t* neighbors, const float* weights,
+                                const pcc_config* config, int32_t objective,
+                                const double* node_weights,
+                                uint32_t* out_labels, pcc_stats* stats);
+
+/*
+ * ClusteringHelper::ComputeObjective on host labels
+ * (parallel-correlation-clusterer-internal.cc:118-149).  Labels < n.
+ */
+pcc_status pcc_objective(pcc_context* ctx, const pcc_graph* graph,
+                         const pcc_config* config, const double* node_weights,
+                         const uint32_t* labels, double* out_objective);
+
+/* ComputeModularity (parallel-modularity-clusterer.cc:36-66). */
+pcc_status pcc_modularity(pcc_context* ctx, const pcc_graph* graph,
+                          double resolution, const uint32_t* labels,
+                          double* out_modularity);
+
+/*
+ * One synchronous best-move pass over ALL vertices from a given state:
+ * ClusteringHelper::EfficientBestMove plus the sync decision of
+ * BestMovesForVertexSubset (parallel-correlation-clusterer-internal.cc:
+ * 448-583, parallel-correlation-clusterer.cc:139-157).  Host arrays of n.
+ *   out_targets[v]  cluster id (n = new cluster) chosen by EfficientBestMove
+ *   out_values[v]   its objective change (before the singleton rule)
+ *   out_moves[v]    decided move after the singleton rule and value > 0,
+ *                   or 0xFFFFFFFF for "no move"; may be NULL.
+ */
+pcc_status pcc_best_moves(pcc_context* ctx, const pcc_graph* graph,
+                          const pcc_config* config,
+                          const uint32_t* cluster_ids,
+                          const uint32_t* cluster_sizes,
+                          const double* node_weights,
+                          const double* cluster_weights, uint32_t* out_targets,
+                          double* out_values, uint32_t* out_moves);
+
+/*
+ * CompressGraph (parallel-correlation-clusterer-internal.cc:709-782 with
+ * ComputeInterClusterEdgesSort, parallel/parallel-graph-utils.cc:156-231):
+ * contracts `graph` by cluster_ids (host uint32[n]) into a new graph over
+ * 1 + max(cluster_ids) vertices.  node_weights host double[n] or NULL (1).
+ * The new graph's node weights are downloaded with pcc_graph_node_weights.
+ */
+pcc_status pcc_compress(pcc_context* ctx, const pcc_graph* graph,
+                        const uint32_t* cluster_ids, const double* node_weights,
+                        pcc_graph** out);
+/* Node weights attached to a compressed graph (host double[n]). */
+pcc_status pcc_graph_node_weights(pcc_context* ctx, const pcc_graph* graph,
+                                  double* out);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif  /* PCC_GB300_H_ */

@@ -1,0 +1,256 @@
+// common.cuh -- shared host/device infrastructure of libpcc_gb300.so:
+// status plumbing, the per-call device context, stream-ordered device
+// buffers and small warp utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "pcc_gb300.h"
+
+namespace pcc {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+
+// Status carried through host code; converts 1:1 to pcc_status / absl codes.
+struct Status {
+  pcc_status code = PCC_OK;
+  std::string msg;
+  bool ok() const { return code == PCC_OK; }
+  static Status Ok() { return {}; }
+};
+
+inline Status MakeError(pcc_status code, std::string msg) {
+  Status s;
+  s.code = code;
+  s.msg = std::move(msg);
+  return s;
+}
+
+#define PCC_RETURN_IF_ERROR(expr)            \
+  do {                                       \
+    ::pcc::Status _st = (expr);              \
+    if (!_st.ok()) return _st;               \
+  } while (0)
+
+#define PCC_CUDA(expr)                                                          \
+  do {                                                                          \
+    cudaError_t _e = (expr);                                                    \
+    if (_e != cudaSuccess)                                                      \
+      return ::pcc::MakeError(PCC_INTERNAL, std::string(#expr) + ": " +         \
+                                                cudaGetErrorString(_e));        \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Context: one device, one stream, one stream-ordered pool with an optional
+// HBM budget.  All kernels of a call run on `stream`.
+// ---------------------------------------------------------------------------
+struct Context {
+  int device = 0;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t budget = 0;             // 0 = device capacity
+  std::atomic<uint64_t> in_use{0};
+  std::mutex mu;
+  std::unordered_map<void*, uint64_t> sizes;
+  std::string last_error;
+
+  Status Alloc(void** p, uint64_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return Status::Ok();
+    bytes = (bytes + 255) & ~uint64_t(255);
+    if (budget && in_use.load() + bytes > budget)
+      return MakeError(PCC_RESOURCE_EXHAUSTED,
+                       "HBM budget exceeded: need " + std::to_string(bytes) +
+                           " more bytes, " + std::to_string(in_use.load()) +
+                           " of " + std::to_string(budget) + " in use");
+    cudaError_t e = cudaMallocAsync(p, bytes, stream);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return MakeError(PCC_RESOURCE_EXHAUSTED,
+                       std::string("device allocation of ") +
+                           std::to_string(bytes) + " bytes failed: " +
+                           cudaGetErrorString(e));
+    }
+    in_use += bytes;
+    std::lock_guard<std::mutex> lk(mu);
+    sizes[*p] = bytes;
+    return Status::Ok();
+  }
+  void Free(void* p) {
+    if (!p) return;
+    cudaFreeAsync(p, stream);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = sizes.find(p);
+    if (it != sizes.end()) {
+      in_use -= it->second;
+      sizes.erase(it);
+    }
+  }
+};
+
+// Stream-ordered device array owned by a context.
+template <class T>
+struct DBuf {
+  Context* ctx = nullptr;
+  T* p = nullptr;
+  uint64_t count = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept { *this = std::move(o); }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) {
+      Release();
+      ctx = o.ctx;
+      p = o.p;
+      count = o.count;
+      o.p = nullptr;
+      o.count = 0;
+    }
+    return *this;
+  }
+  ~DBuf() { Release(); }
+  Status Alloc(Context* c, uint64_t n) {
+    Release();
+    ctx = c;
+    count = n;
+    void* q = nullptr;
+    PCC_RETURN_IF_ERROR(c->Alloc(&q, n * sizeof(T)));
+    p = static_cast<T*>(q);
+    return Status::Ok();
+  }
+  // Grows to at least n elements (contents not preserved).
+  Status Reserve(Context* c, uint64_t n) {
+    if (p && count >= n) return Status::Ok();
+    return Alloc(c, n);
+  }
+  void Release() {
+    if (p && ctx) ctx->Free(p);
+    p = nullptr;
+    count = 0;
+  }
+  Status Zero() {
+    if (count) PCC_CUDA(cudaMemsetAsync(p, 0, count * sizeof(T), ctx->stream));
+    return Status::Ok();
+  }
+  Status Fill(int byte) {
+    if (count) PCC_CUDA(cudaMemsetAsync(p, byte, count * sizeof(T), ctx->stream));
+    return Status::Ok();
+  }
+  Status FromHost(const T* h, uint64_t n) {
+    if (n) PCC_CUDA(cudaMemcpyAsync(p, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    return Status::Ok();
+  }
+  Status ToHost(T* h, uint64_t n) const {
+    if (n) PCC_CUDA(cudaMemcpyAsync(h, p, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+    return Status::Ok();
+  }
+};
+
+inline Status Sync(Context* c) {
+  PCC_CUDA(cudaStreamSynchronize(c->stream));
+  PCC_CUDA(cudaGetLastError());
+  return Status::Ok();
+}
+
+inline Status LaunchCheck() {
+  PCC_CUDA(cudaGetLastError());
+  return Status::Ok();
+}
+
+// Process-wide count of kernel launches issued by this library; a call
+// reports the difference across its own duration.
+inline std::atomic<uint64_t>& LaunchCounter() {
+  static std::atomic<uint64_t> c{0};
+  return c;
+}
+#define PCC_COUNT(k) (::pcc::LaunchCounter() += (k))
+
+// CUDA-event spans of named phases on the context stream; totals are read
+// after the stream has been synchronised.
+struct PhaseTimer {
+  cudaStream_t stream = nullptr;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> spans[4];
+  cudaEvent_t open[4] = {nullptr, nullptr, nullptr, nullptr};
+  explicit PhaseTimer(cudaStream_t s) : stream(s) {}
+  PhaseTimer(const PhaseTimer&) = delete;
+  PhaseTimer& operator=(const PhaseTimer&) = delete;
+  void Begin(int k) {
+    cudaEventCreate(&open[k]);
+    cudaEventRecord(open[k], stream);
+  }
+  void End(int k) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, stream);
+    spans[k].emplace_back(open[k], e);
+    open[k] = nullptr;
+  }
+  double TotalMs(int k) const {
+    double t = 0;
+    for (const auto& sp : spans[k]) {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, sp.first, sp.second) == cudaSuccess) t += ms;
+    }
+    return t;
+  }
+  ~PhaseTimer() {
+    for (auto& v : spans)
+      for (auto& sp : v) {
+        cudaEventDestroy(sp.first);
+        cudaEventDestroy(sp.second);
+      }
+    for (auto e : open)
+      if (e) cudaEventDestroy(e);
+  }
+};
+constexpr int kPhaseBestMoves = 0;
+constexpr int kPhaseCompress = 1;
+
+inline unsigned Blocks(uint64_t items, unsigned per_block, unsigned cap) {
+  uint64_t b = (items + per_block - 1) / per_block;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return static_cast<unsigned>(b);
+}
+
+// ---------------------------------------------------------------------------
+// Device helpers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned LaneId() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%laneid;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned LaneMaskLt() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+  return r;
+}
+
+// IEEE double arithmetic without contraction into FMA: the reference's
+// values are computed with separate roundings (built with the oracle's
+// -ffp-contract=off), so every step here rounds separately too.
+__device__ __forceinline__ double Dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double Dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double Dsub(double a, double b) { return __dsub_rn(a, b); }
+
+}  // namespace pcc
+
+// The opaque C-ABI types.
+struct pcc_context {
+  pcc::Context c;
+};

@@ -1,0 +1,149 @@
+// engine.cuh -- device data layout of the clustering engine and the
+// launchers shared between translation units.
+//
+// HBM layout (SoA, one set per compression level):
+//   graph   off u64[n+1], nbr u32[m], w f32[m] (absent for unit weights)
+//   state   C u32[n] (cluster_ids_), s u32[n] (cluster_sizes_),
+//           k f64[n] (node_weights_), K f64[n] (cluster_weights_)
+// mirroring ClusteringHelper (parallel-correlation-clusterer-internal.h:
+// 36-165).  Per-round scratch (sized by the level-0 vertex count) holds the
+// degree-binned frontier, the decided moves and round-stamped flags, so no
+// per-round clearing pass is needed.
+#pragma once
+
+#include "primitives.cuh"
+
+namespace pcc {
+
+// ---------------------------------------------------------------------------
+// Graph resident in HBM.
+// ---------------------------------------------------------------------------
+struct DevGraph {
+  uint32_t n = 0;
+  uint64_t m = 0;
+  DBuf<uint64_t> off;
+  DBuf<uint32_t> nbr;
+  DBuf<float> w;          // empty => unit weights
+  DBuf<double> node_w;    // node weights attached by compression
+  uint32_t max_deg = 0;
+  bool integral = true;   // every weight is an integer value
+  double max_abs_w = 1.0; // max |w| (1 for unit weights)
+  const float* wp() const { return w.p; }
+};
+
+// Computes max degree / weight properties on the device (one sync).
+Status ComputeGraphProperties(Context* ctx, DevGraph* g);
+
+// ---------------------------------------------------------------------------
+// Degree bins.  Each bin is served by one best-move kernel shape:
+//   d <= 4, 8, 16, 32    lane groups of 4/8/16/32 lanes, one chunk
+//   d <= 128/256/512     one warp, shared-memory hash of 256/512/1024 slots
+//   d <= 1000            one warp, shared-memory hash of 2048 slots
+//                        (the reference's sequential path ends at 1000)
+//   d <= 4096            one CTA, shared-memory hash of 8192 slots
+//   d >  4096            one CTA, hash in global scratch
+// ---------------------------------------------------------------------------
+enum Bin : int {
+  kBinG4 = 0, kBinG8, kBinG16, kBinG32,
+  kBinW128, kBinW256, kBinW512, kBinW1000,
+  kBinCta, kBinGlobal,
+  kNumBins
+};
+constexpr uint32_t kBinMaxDeg[kNumBins] = {4, 8, 16, 32, 128, 256, 512, 1000, 4096, 0xFFFFFFFFu};
+constexpr uint32_t kCtaHashSlots = 8192;
+
+__host__ __device__ inline int BinOf(uint64_t d) {
+  if (d <= 4) return kBinG4;
+  if (d <= 8) return kBinG8;
+  if (d <= 16) return kBinG16;
+  if (d <= 32) return kBinG32;
+  if (d <= 128) return kBinW128;
+  if (d <= 256) return kBinW256;
+  if (d <= 512) return kBinW512;
+  if (d <= 1000) return kBinW1000;
+  if (d <= 4096) return kBinCta;
+  return kBinGlobal;
+}
+
+// Device counters of one call (all in one allocation).
+struct DevCounters {
+  uint32_t bin_count[kNumBins];
+  uint32_t bin_start[kNumBins + 1];
+  uint32_t frontier;        // vertices in the frontier being built
+  uint32_t movers;          // real movers of this round
+  uint32_t new_movers;      // movers to a new cluster
+  uint32_t marked;          // vertices marked for the next frontier
+  uint32_t level_moved;     // OR over rounds of "next frontier non-empty"
+  uint32_t rounds;          // best-move rounds executed
+  uint32_t present;         // generic count used by compaction steps
+  uint32_t max_u32;         // generic max used by reductions
+  unsigned long long pend_edges;     // sum deg of the frontier being built
+  unsigned long long edge_visits;    // sum deg over executed rounds
+  unsigned long long vertex_visits;  // sum |F| over executed rounds
+  unsigned long long moves;          // real moves (sync) / moves (async)
+  int error;                // nonzero: a bounded wait gave up (see kErr*)
+  int pad;
+};
+
+constexpr int kErrProbeLimit = 1;   // async new-cluster probe exceeded its bound
+constexpr int kErrHashFull = 2;     // a best-move hash table filled up
+
+// Degree-binned vertex list: bins are contiguous segments of `list`.
+struct BinSet {
+  DBuf<uint32_t> list;       // n entries
+  DBuf<uint32_t> counts;     // [kNumBins] counts, then [kNumBins+1] starts
+  uint64_t edges = 0;        // sum of degrees (host copy, static bins only)
+  uint32_t size = 0;         // vertices (host copy, static bins only)
+  uint32_t host_counts[kNumBins] = {0};
+};
+
+// Best-move kernel arguments.
+struct BMArgs {
+  uint32_t n;
+  const uint64_t* off;
+  const uint32_t* nbr;
+  const float* w;
+  const uint32_t* C;
+  const uint32_t* s;
+  const double* k;
+  const double* K;
+  double res;
+  double offset;
+  int32_t ioffset;          // integer offset (INT mode)
+  uint32_t stamp;
+  // sync outputs
+  uint32_t* moves;          // decided target per vertex (read for movers)
+  uint32_t* moved_stamp;    // moved_vertex: = stamp when value > 0
+  uint32_t* movers;         // list of real movers (target != current)
+  DevCounters* ctr;
+  // replay outputs (nullable)
+  uint32_t* out_target;
+  double* out_value;
+  uint32_t* out_moves;
+  // global-hash scratch for the hub bin
+  uint32_t* g_keys;
+  unsigned long long* g_vals;
+  uint32_t g_cap;           // slots per CTA
+  // async mode: apply moves immediately with atomics
+  int async;
+  uint32_t* s_mut;
+  double* K_mut;
+  uint32_t* C_mut;
+  uint32_t* moved_cluster_stamp;
+};
+
+// Launches every best-move kernel over `bins` (counts read on the device).
+// int_mode selects exact integer accumulation (all weights and the offset
+// integral and small) over FP64 accumulation in adjacency order.
+Status LaunchBestMoves(Context* ctx, const BMArgs& a, const uint32_t* list, const uint32_t* bin_counts,
+                       const uint32_t* bin_starts, const uint32_t* host_counts, bool int_mode,
+                       uint32_t max_deg);
+
+// Bytes of global scratch the hub bin needs for a graph of this max degree.
+uint64_t GlobalHashSlots(Context* ctx, uint32_t max_deg);
+
+}  // namespace pcc
+
+struct pcc_graph {
+  pcc::DevGraph g;
+};

@@ -1,0 +1,252 @@
+// graph.cu -- context lifetime, graph upload / download and graph
+// properties (C ABI).  A graph upload replaces GbbsGraph::Import /
+// FinishImport (clustering/gbbs-graph.cc:32-76) and the CLI's CopyGraph
+// (clustering/cluster-in-memory_main.cc:231-306): the CSR arrays are copied
+// once into HBM and stay there for every clustering call.
+#include <cmath>
+
+#include "engine.cuh"
+
+namespace pcc {
+
+namespace {
+
+struct DegreeInput {
+  const uint64_t* off;
+  __device__ uint32_t operator()(uint64_t i) const { return static_cast<uint32_t>(off[i + 1] - off[i]); }
+};
+
+// Non-integral weight count and max |w| (as float bits of the magnitude).
+struct WeightStats {
+  unsigned long long nonint;
+  float maxabs;
+};
+struct WeightInput {
+  const float* w;
+  __device__ WeightStats operator()(uint64_t i) const {
+    const float x = w[i];
+    WeightStats r;
+    r.nonint = (x != truncf(x) || isnan(x) || isinf(x)) ? 1ull : 0ull;
+    r.maxabs = fabsf(x);
+    return r;
+  }
+};
+struct WeightOp {
+  __device__ WeightStats operator()(WeightStats a, WeightStats b) const {
+    WeightStats r;
+    r.nonint = a.nonint + b.nonint;
+    r.maxabs = fmaxf(a.maxabs, b.maxabs);
+    return r;
+  }
+};
+
+__global__ void CheckCsrKernel(uint32_t n, uint64_t m, const uint64_t* __restrict__ off,
+                               const uint32_t* __restrict__ nbr, int* bad) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i <= n; i += uint64_t(gridDim.x) * blockDim.x) {
+    if (i == 0 && off[0] != 0) atomicExch(bad, 1);
+    if (i == n && off[n] != m) atomicExch(bad, 2);
+    if (i < n && off[i] > off[i + 1]) atomicExch(bad, 3);
+  }
+  for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < m; j += uint64_t(gridDim.x) * blockDim.x)
+    if (nbr[j] >= n) atomicExch(bad, 4);
+}
+
+}  // namespace
+
+Status ComputeGraphProperties(Context* ctx, DevGraph* g) {
+  DBuf<uint32_t> part, out;
+  PCC_RETURN_IF_ERROR(out.Alloc(ctx, 1));
+  uint32_t maxd = 0;
+  if (g->n) {
+    PCC_RETURN_IF_ERROR(Reduce<uint32_t>(ctx, g->n, DegreeInput{g->off.p}, OpMax{}, 0u, out.p, part));
+    PCC_RETURN_IF_ERROR(out.ToHost(&maxd, 1));
+  }
+  WeightStats ws{0, 1.0f};
+  if (g->w.p && g->m) {
+    DBuf<WeightStats> wpart, wout;
+    PCC_RETURN_IF_ERROR(wout.Alloc(ctx, 1));
+    PCC_RETURN_IF_ERROR(Reduce<WeightStats>(ctx, g->m, WeightInput{g->w.p}, WeightOp{}, WeightStats{0, 0.0f},
+                                            wout.p, wpart));
+    PCC_RETURN_IF_ERROR(wout.ToHost(&ws, 1));
+    PCC_RETURN_IF_ERROR(Sync(ctx));
+  }
+  PCC_RETURN_IF_ERROR(Sync(ctx));
+  g->max_deg = maxd;
+  g->integral = ws.nonint == 0;
+  g->max_abs_w = ws.maxabs;
+  return Status::Ok();
+}
+
+namespace {
+
+Status Upload(pcc_context* pctx, uint32_t n, uint64_t m, const uint64_t* off, const uint32_t* nbr, const float* w,
+              bool device_src, pcc_graph** out) {
+  if (!pctx || !out) return MakeError(PCC_INVALID_ARGUMENT, "null context or output");
+  if (!off || (m && !nbr)) return MakeError(PCC_INVALID_ARGUMENT, "null offsets or neighbors");
+  if (m >= 0xFFFFFFFFull) return MakeError(PCC_INVALID_ARGUMENT, "graphs with 2^32 or more entries are not supported");
+  if (n == 0xFFFFFFFFu) return MakeError(PCC_INVALID_ARGUMENT, "n must be below 2^32 - 1");
+  Context* ctx = &pctx->c;
+  if (!device_src) {
+    if (off[0] != 0 || off[n] != m)
+      return MakeError(PCC_INVALID_ARGUMENT, "offsets must start at 0 and end at m");
+  }
+  auto h = std::make_unique<pcc_graph>();
+  DevGraph& g = h->g;
+  g.n = n;
+  g.m = m;
+  const cudaMemcpyKind kind = device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  PCC_RETURN_IF_ERROR(g.off.Alloc(ctx, uint64_t(n) + 1));
+  PCC_RETURN_IF_ERROR(g.nbr.Alloc(ctx, m ? m : 1));
+  PCC_CUDA(cudaMemcpyAsync(g.off.p, off, sizeof(uint64_t) * (uint64_t(n) + 1), kind, ctx->stream));
+  if (m) PCC_CUDA(cudaMemcpyAsync(g.nbr.p, nbr, sizeof(uint32_t) * m, kind, ctx->stream));
+  if (w) {
+    PCC_RETURN_IF_ERROR(g.w.Alloc(ctx, m ? m : 1));
+    if (m) PCC_CUDA(cudaMemcpyAsync(g.w.p, w, sizeof(float) * m, kind, ctx->stream));
+  }
+  DBuf<int> bad;
+  PCC_RETURN_IF_ERROR(bad.Alloc(ctx, 1));
+  PCC_RETURN_IF_ERROR(bad.Zero());
+  CheckCsrKernel<<<Blocks(std::max<uint64_t>(m, n + 1), 256, unsigned(ctx->num_sms) * 8), 256, 0, ctx->stream>>>(
+      n, m, g.off.p, g.nbr.p, bad.p); PCC_COUNT(1);
+  int hbad = 0;
+  PCC_RETURN_IF_ERROR(bad.ToHost(&hbad, 1));
+  PCC_RETURN_IF_ERROR(Sync(ctx));
+  if (hbad)
+    return MakeError(PCC_INVALID_ARGUMENT,
+                     hbad == 4 ? "neighbor id out of range" : "offsets are not a valid CSR row index");
+  PCC_RETURN_IF_ERROR(ComputeGraphProperties(ctx, &g));
+  *out = h.release();
+  return Status::Ok();
+}
+
+pcc_status Done(pcc_context* ctx, const Status& st) {
+  if (ctx) ctx->c.last_error = st.ok() ? std::string() : st.msg;
+  return st.code;
+}
+
+}  // namespace
+}  // namespace pcc
+
+using namespace pcc;
+
+extern "C" {
+
+void pcc_config_default(pcc_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->clustering_moves_method = PCC_LOUVAIN;
+  c->subclustering_method = PCC_NONE_SUBCLUSTERING;
+  c->move_method = PCC_NBHR_CLUSTER_MOVE;
+}
+
+const char* pcc_version(void) { return "pcc_gb300 0.1.0 (sm_103a)"; }
+
+pcc_status pcc_create(pcc_context** out, int device, uint64_t hbm_budget_bytes) {
+  if (!out) return PCC_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return PCC_UNAVAILABLE;
+  }
+  if (device < 0 || device >= count) return PCC_INVALID_ARGUMENT;
+  if (cudaSetDevice(device) != cudaSuccess) return PCC_UNAVAILABLE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return PCC_UNAVAILABLE;
+  auto* h = new pcc_context;
+  Context& c = h->c;
+  c.device = device;
+  c.num_sms = prop.multiProcessorCount;
+  c.smem_optin = prop.sharedMemPerBlockOptin;
+  c.budget = hbm_budget_bytes;
+  if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return PCC_UNAVAILABLE;
+  }
+  // Keep freed pool memory cached between calls (no release to the OS).
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t threshold = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+  }
+  *out = h;
+  return PCC_OK;
+}
+
+void pcc_destroy(pcc_context* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->c.device);
+  cudaStreamSynchronize(ctx->c.stream);
+  cudaStreamDestroy(ctx->c.stream);
+  delete ctx;
+}
+
+const char* pcc_last_error(const pcc_context* ctx) { return ctx ? ctx->c.last_error.c_str() : "null context"; }
+
+uint64_t pcc_device_bytes_in_use(const pcc_context* ctx) { return ctx ? ctx->c.in_use.load() : 0; }
+
+pcc_status pcc_graph_upload(pcc_context* ctx, uint32_t n, uint64_t m, const uint64_t* offsets,
+                            const uint32_t* neighbors, const float* weights, pcc_graph** out) {
+  try {
+    if (ctx) cudaSetDevice(ctx->c.device);
+    return Done(ctx, Upload(ctx, n, m, offsets, neighbors, weights, false, out));
+  } catch (const std::exception& e) {
+    return Done(ctx, MakeError(PCC_INTERNAL, e.what()));
+  }
+}
+
+pcc_status pcc_graph_upload_device(pcc_context* ctx, uint32_t n, uint64_t m, const uint64_t* d_offsets,
+                                   const uint32_t* d_neighbors, const float* d_weights, pcc_graph** out) {
+  try {
+    if (ctx) cudaSetDevice(ctx->c.device);
+    return Done(ctx, Upload(ctx, n, m, d_offsets, d_neighbors, d_weights, true, out));
+  } catch (const std::exception& e) {
+    return Done(ctx, MakeError(PCC_INTERNAL, e.what()));
+  }
+}
+
+void pcc_graph_free(pcc_context* ctx, pcc_graph* graph) {
+  (void)ctx;
+  delete graph;
+}
+
+pcc_status pcc_graph_info(const pcc_graph* graph, uint32_t* n, uint64_t* m, int32_t* has_weights) {
+  if (!graph) return PCC_INVALID_ARGUMENT;
+  if (n) *n = graph->g.n;
+  if (m) *m = graph->g.m;
+  if (has_weights) *has_weights = graph->g.w.p != nullptr;
+  return PCC_OK;
+}
+
+pcc_status pcc_graph_download(pcc_context* pctx, const pcc_graph* graph, uint64_t* offsets, uint32_t* neighbors,
+                              float* weights) {
+  Status st;
+  if (!pctx || !graph || !offsets || !neighbors) st = MakeError(PCC_INVALID_ARGUMENT, "null argument");
+  if (st.ok()) st = graph->g.off.ToHost(offsets, uint64_t(graph->g.n) + 1);
+  if (st.ok()) st = graph->g.nbr.ToHost(neighbors, graph->g.m);
+  if (st.ok() && weights) {
+    if (graph->g.w.p) {
+      st = graph->g.w.ToHost(weights, graph->g.m);
+    } else {
+      for (uint64_t j = 0; j < graph->g.m; ++j) weights[j] = 1.0f;
+    }
+  }
+  if (st.ok()) st = Sync(&pctx->c);
+  return Done(pctx, st);
+}
+
+pcc_status pcc_graph_node_weights(pcc_context* pctx, const pcc_graph* graph, double* out) {
+  Status st;
+  if (!pctx || !graph || !out) st = MakeError(PCC_INVALID_ARGUMENT, "null argument");
+  if (st.ok()) {
+    if (graph->g.node_w.p) {
+      st = graph->g.node_w.ToHost(out, graph->g.n);
+    } else {
+      for (uint32_t i = 0; i < graph->g.n; ++i) out[i] = 1.0;
+    }
+  }
+  if (st.ok()) st = Sync(&pctx->c);
+  return Done(pctx, st);
+}
+
+}  // extern "C"

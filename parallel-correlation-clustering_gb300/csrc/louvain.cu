@@ -1,0 +1,1133 @@
+// louvain.cu -- the multilevel Louvain engine and the clustering C ABI.
+//
+// Restates ParallelCorrelationClusterer::RefineClusters_subroutine
+// (clustering/clusterers/parallel-correlation-clusterer.cc:476-629),
+// IterateBestMoves (:340-365), BestMovesForVertexSubset (:115-338, LOUVAIN
+// vertex moves), MoveNodesToCluster (parallel-correlation-clusterer-
+// internal.cc:256-369), FlattenClustering / OutputIndicesById
+// (parallel/parallel-graph-utils.cc:233-243, parallel-sequence-ops.h:183-209),
+// ComputeObjective (internal.cc:118-149) and the modularity wrapper
+// (parallel-modularity-clusterer.cc:36-111).
+//
+// Host code only enqueues work on the context stream; it reads back a few
+// counters once per best-move round and once per level.
+#include <chrono>
+#include <cmath>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "graphops.cuh"
+
+namespace pcc {
+
+Status CompressGraph(Context* ctx, const DevGraph& g, const uint32_t* C, const double* k,
+                     std::unique_ptr<DevGraph>* out);
+
+namespace {
+
+constexpr unsigned kT = 256;
+
+unsigned GridFor(Context* ctx, uint64_t items, unsigned per_block = kT) {
+  return Blocks(items, per_block, unsigned(ctx->num_sms) * 16);
+}
+
+// ---------------------------------------------------------------------------
+// Small kernels.
+// ---------------------------------------------------------------------------
+__global__ void IotaKernel(uint32_t n, uint32_t* out) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    out[i] = static_cast<uint32_t>(i);
+}
+
+__global__ void FillF64Kernel(uint64_t n, double v, double* out) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    out[i] = v;
+}
+
+// Singletons: C = i, s = 1, K = k (SetClustering with an empty clustering).
+__global__ void SingletonsKernel(uint32_t n, const double* __restrict__ k, uint32_t* C, uint32_t* s, double* K) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    C[i] = static_cast<uint32_t>(i);
+    s[i] = 1u;
+    K[i] = k[i];
+  }
+}
+
+// s[C[i]] += 1, K[C[i]] += k[i] (SetClustering with a clustering; exact for
+// integral node weights, which is every weight the clusterers create).
+__global__ void AccumulateClustersKernel(uint32_t n, const uint32_t* __restrict__ C, const double* __restrict__ k,
+                                         uint32_t* s, double* K) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t c = C[i];
+    atomicAdd(&s[c], 1u);
+    atomicAdd(&K[c], k[i]);
+  }
+}
+
+// cluster_ids[i] = C[cluster_ids[i]] (FlattenClustering).
+__global__ void FlattenKernel(uint32_t n, uint32_t* ids, const uint32_t* __restrict__ C) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    ids[i] = C[ids[i]];
+}
+
+// flat[j] = Cup[C[j]] and mark the flattened id as present.
+__global__ void ProjectKernel(uint32_t n, const uint32_t* __restrict__ C, const uint32_t* __restrict__ Cup,
+                              uint32_t* flat, uint32_t* present_stamp, uint32_t stamp) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t f = Cup[C[i]];
+    flat[i] = f;
+    present_stamp[f] = stamp;
+  }
+}
+
+__global__ void MarkStampKernel(uint32_t n, const uint32_t* ids, uint32_t* st, uint32_t stamp) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    st[ids[i]] = stamp;
+}
+
+struct StampInput {
+  const uint32_t* st;
+  uint32_t stamp;
+  __device__ uint32_t operator()(uint64_t i) const { return st[i] == stamp ? 1u : 0u; }
+};
+
+__global__ void GatherKernel(uint32_t n, const uint32_t* __restrict__ idx, const uint32_t* __restrict__ table,
+                             uint32_t* out) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    out[i] = table[idx[i]];
+}
+
+// ---------------------------------------------------------------------------
+// Degree binning of a vertex predicate over [0, n): count, starts, scatter.
+// ---------------------------------------------------------------------------
+struct PredAll {
+  __device__ bool operator()(uint32_t) const { return true; }
+};
+struct PredStamp {
+  const uint32_t* st;
+  uint32_t stamp;
+  __device__ bool operator()(uint32_t v) const { return st[v] == stamp; }
+};
+
+template <class P>
+__global__ void __launch_bounds__(kT) BinCountKernel(uint32_t n, const uint64_t* __restrict__ off, P pred,
+                                                     uint32_t* counts, DevCounters* ctr) {
+  __shared__ uint32_t sh[kNumBins];
+  __shared__ unsigned long long sh_deg;
+  if (threadIdx.x < kNumBins) sh[threadIdx.x] = 0;
+  if (threadIdx.x == 0) sh_deg = 0;
+  __syncthreads();
+  unsigned long long deg_acc = 0;
+  uint32_t cnt = 0;
+  for (uint64_t v = uint64_t(blockIdx.x) * kT + threadIdx.x; v < n; v += uint64_t(gridDim.x) * kT) {
+    if (!pred(static_cast<uint32_t>(v))) continue;
+    const uint64_t d = off[v + 1] - off[v];
+    atomicAdd(&sh[BinOf(d)], 1u);
+    deg_acc += d;
+    cnt++;
+  }
+  atomicAdd(&sh_deg, deg_acc);
+  __shared__ uint32_t sh_cnt;
+  if (threadIdx.x == 0) sh_cnt = 0;
+  __syncthreads();
+  atomicAdd(&sh_cnt, cnt);
+  __syncthreads();
+  if (threadIdx.x < kNumBins && sh[threadIdx.x]) atomicAdd(&counts[threadIdx.x], sh[threadIdx.x]);
+  if (threadIdx.x == 0) {
+    if (sh_deg) atomicAdd(&ctr->pend_edges, sh_deg);
+    if (sh_cnt) atomicAdd(&ctr->frontier, sh_cnt);
+  }
+}
+
+// counts[0..B) -> starts[0..B] and cursors zeroed.
+__global__ void BinStartsKernel(const uint32_t* counts, uint32_t* starts, uint32_t* cursor) {
+  uint32_t acc = 0;
+  for (int b = 0; b < kNumBins; ++b) {
+    starts[b] = acc;
+    acc += counts[b];
+    cursor[b] = 0;
+  }
+  starts[kNumBins] = acc;
+}
+
+template <class P>
+__global__ void __launch_bounds__(kT) BinScatterKernel(uint32_t n, const uint64_t* __restrict__ off, P pred,
+                                                       const uint32_t* __restrict__ starts, uint32_t* cursor,
+                                                       uint32_t* list) {
+  const uint64_t stride = uint64_t(gridDim.x) * kT;
+  const uint64_t limit = (uint64_t(n) + 31) & ~uint64_t(31);
+  for (uint64_t v = uint64_t(blockIdx.x) * kT + threadIdx.x; v < limit; v += stride) {
+    const bool in = v < n && pred(static_cast<uint32_t>(v));
+    const int bin = in ? BinOf(off[v + 1] - off[v]) : kNumBins + int(LaneId());
+    const unsigned peers = __match_any_sync(kFull, bin);
+    uint32_t base = 0;
+    const int leader = __ffs(peers) - 1;
+    if (in && int(LaneId()) == leader) base = atomicAdd(&cursor[bin], uint32_t(__popc(peers)));
+    base = __shfl_sync(kFull, base, leader);
+    if (in) list[starts[bin] + base + __popc(peers & LaneMaskLt())] = static_cast<uint32_t>(v);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Sync apply: MoveNodesToCluster.
+// ---------------------------------------------------------------------------
+struct ApplyArgs {
+  uint32_t n;
+  uint32_t* C;
+  uint32_t* s;
+  const double* k;
+  double* K;
+  const uint32_t* moves;
+  const uint32_t* movers;
+  uint32_t* mod_stamp;
+  uint32_t* new_stamp;
+  uint32_t stamp;
+  DevCounters* ctr;
+};
+
+// Leave: every mover leaves its cluster (sizes and weights), marks it
+// modified; movers to a new cluster are flagged for ranking.
+__global__ void __launch_bounds__(kT) ApplyLeaveKernel(ApplyArgs a) {
+  const uint32_t count = a.ctr->movers;
+  for (uint64_t i = uint64_t(blockIdx.x) * kT + threadIdx.x; i < count; i += uint64_t(gridDim.x) * kT) {
+    const uint32_t v = a.movers[i];
+    const uint32_t c = a.C[v];
+    atomicSub(&a.s[c], 1u);
+    atomicAdd(&a.K[c], -a.k[v]);
+    a.mod_stamp[c] = a.stamp;
+    if (a.moves[v] == a.n) {
+      a.new_stamp[v] = a.stamp;
+      atomicAdd(&a.ctr->new_movers, 1u);
+    }
+  }
+}
+
+// Join: movers to existing clusters enter them.
+__global__ void __launch_bounds__(kT) ApplyJoinKernel(ApplyArgs a) {
+  const uint32_t count = a.ctr->movers;
+  for (uint64_t i = uint64_t(blockIdx.x) * kT + threadIdx.x; i < count; i += uint64_t(gridDim.x) * kT) {
+    const uint32_t v = a.movers[i];
+    const uint32_t t = a.moves[v];
+    if (t == a.n) continue;
+    atomicAdd(&a.s[t], 1u);
+    atomicAdd(&a.K[t], a.k[v]);
+    a.mod_stamp[t] = a.stamp;
+    a.C[v] = t;
+  }
+}
+
+// Gated inputs for the new-cluster compactions: nothing to do when no
+// vertex moves to a new cluster.
+struct ZeroSizeInput {
+  const uint32_t* s;
+  const DevCounters* ctr;
+  __device__ uint32_t operator()(uint64_t i) const { return ctr->new_movers && s[i] == 0u ? 1u : 0u; }
+};
+struct NewMoverInput {
+  const uint32_t* st;
+  uint32_t stamp;
+  const DevCounters* ctr;
+  __device__ uint32_t operator()(uint64_t i) const { return ctr->new_movers && st[i] == stamp ? 1u : 0u; }
+};
+
+// New clusters take the ascending list of empty ids, in ascending node order.
+__global__ void __launch_bounds__(kT) AssignNewKernel(ApplyArgs a, const uint32_t* __restrict__ zero_ids,
+                                                      const uint32_t* __restrict__ new_list) {
+  const uint32_t count = a.ctr->new_movers;
+  for (uint64_t i = uint64_t(blockIdx.x) * kT + threadIdx.x; i < count; i += uint64_t(gridDim.x) * kT) {
+    const uint32_t v = new_list[i];
+    const uint32_t cid = zero_ids[i];
+    a.C[v] = cid;
+    a.s[cid] = 1u;
+    a.K[cid] = a.k[v];
+    a.mod_stamp[cid] = a.stamp;
+  }
+}
+
+// Marked vertices for the next frontier.
+struct MarkClusterInput {  // NBHR_CLUSTER_MOVE: vertices of modified clusters
+  const uint32_t* C;
+  const uint32_t* mod_stamp;
+  uint32_t stamp;
+  __device__ uint32_t operator()(uint64_t v) const { return mod_stamp[C[v]] == stamp ? 1u : 0u; }
+};
+
+struct PushNeighbors {  // gbbs::edgeMap with an always-true functor
+  const uint32_t* nbr;
+  uint32_t* next_stamp;
+  uint32_t stamp;
+  __device__ void operator()(uint32_t, uint64_t j) const { next_stamp[nbr[j]] = stamp; }
+};
+
+// ---------------------------------------------------------------------------
+// Objective / modularity.
+// ---------------------------------------------------------------------------
+struct ObjEdgeTerm {
+  const uint32_t* nbr;
+  const float* w;
+  const uint32_t* C;
+  double offset;
+  double* acc;  // per-thread accumulators (indexed by global thread id)
+  __device__ void operator()(uint32_t u, uint64_t j) const {
+    if (C[u] == C[nbr[j]]) {
+      const double x = Dsub(static_cast<double>(w ? w[j] : 1.0f), offset) / 2;
+      acc[uint64_t(blockIdx.x) * blockDim.x + threadIdx.x] += x;
+    }
+  }
+};
+
+struct ResTerm {
+  const uint32_t* C;
+  const double* k;
+  const double* K;
+  __device__ double operator()(uint64_t i) const { return Dmul(k[i], Dsub(K[C[i]], k[i])); }
+};
+
+struct ArrayInputF64 {
+  const double* a;
+  __device__ double operator()(uint64_t i) const { return a[i]; }
+};
+
+struct SameLabelCount {
+  const uint32_t* nbr;
+  const uint32_t* L;
+  unsigned long long* acc;
+  __device__ void operator()(uint32_t u, uint64_t j) const {
+    if (L[u] == L[nbr[j]]) atomicAdd(&acc[(uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) & 1023], 1ull);
+  }
+};
+
+__global__ void DegreeSumKernel(uint32_t n, const uint64_t* __restrict__ off, const uint32_t* __restrict__ L,
+                                unsigned long long* deg) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    atomicAdd(&deg[L[i]], static_cast<unsigned long long>(off[i + 1] - off[i]));
+}
+
+struct ModTerm {
+  const unsigned long long* deg;
+  double res;
+  double total;
+  __device__ double operator()(uint64_t c) const {
+    const double d = static_cast<double>(deg[c]);
+    return Dmul(Dmul(res, d), d) / total;
+  }
+};
+
+struct U64Input {
+  const unsigned long long* a;
+  __device__ unsigned long long operator()(uint64_t i) const { return a[i]; }
+};
+
+__global__ void DegreeF64Kernel(uint32_t n, const uint64_t* __restrict__ off, double* k) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    k[i] = static_cast<double>(off[i + 1] - off[i]);
+}
+
+// ---------------------------------------------------------------------------
+// Level state (one ClusteringHelper + its graph).
+// ---------------------------------------------------------------------------
+struct Level {
+  const DevGraph* g = nullptr;
+  std::unique_ptr<DevGraph> own;
+  DBuf<uint32_t> C, s;
+  DBuf<double> k, K;
+  BinSet all;
+  bool bins_ready = false;
+  bool int_mode = false;
+};
+
+struct RunResult {
+  uint64_t edge_visits = 0;
+  uint64_t vertex_visits = 0;
+  uint64_t moves = 0;
+  int32_t levels = 0;
+  int32_t rounds = 0;
+  int32_t refine_passes = 0;
+  uint64_t algo_bytes = 0;
+};
+
+bool IntModeFor(const DevGraph& g, double offset) {
+  if (!g.integral) return false;
+  if (offset != std::floor(offset) || std::fabs(offset) > 4194304.0) return false;
+  return g.max_abs_w + std::fabs(offset) <= 4194304.0;  // 2^22
+}
+
+class Engine {
+ public:
+  Engine(Context* ctx, const pcc_config& cfg) : ctx_(ctx), cfg_(cfg), timer_(ctx->stream) {}
+
+  Status Init(uint32_t n_max, uint32_t max_deg) {
+    n_max_ = n_max;
+    const uint64_t nn = std::max<uint64_t>(n_max, 1);
+    PCC_RETURN_IF_ERROR(moves_.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(movers_.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(moved_stamp_.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(mod_stamp_.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(next_stamp_.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(new_stamp_.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(aux_stamp_.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(moved_stamp_.Zero());
+    PCC_RETURN_IF_ERROR(mod_stamp_.Zero());
+    PCC_RETURN_IF_ERROR(next_stamp_.Zero());
+    PCC_RETURN_IF_ERROR(new_stamp_.Zero());
+    PCC_RETURN_IF_ERROR(aux_stamp_.Zero());
+    PCC_RETURN_IF_ERROR(zero_ids_.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(new_list_.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(marked_.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(dyn_.list.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(dyn_.counts.Alloc(ctx_, 3 * kNumBins + 1));
+    PCC_RETURN_IF_ERROR(ctr_.Alloc(ctx_, 1));
+    PCC_RETURN_IF_ERROR(ctr_.Zero());
+    PCC_RETURN_IF_ERROR(EnsureHubScratch(max_deg));
+    return Status::Ok();
+  }
+
+  Status EnsureHubScratch(uint32_t max_deg) {
+    const uint64_t slots = GlobalHashSlots(ctx_, max_deg);
+    if (slots > g_keys_.count) {
+      PCC_RETURN_IF_ERROR(g_keys_.Alloc(ctx_, slots));
+      PCC_RETURN_IF_ERROR(g_vals_.Alloc(ctx_, slots));
+      g_cap_ = uint32_t(slots / (uint64_t(ctx_->num_sms) * 2));
+    }
+    return Status::Ok();
+  }
+
+  // Builds level state over graph g: singletons with node weights k (device,
+  // copied) or from initial labels.
+  Status MakeLevel(const DevGraph* g, std::unique_ptr<DevGraph> own, const double* d_k, bool k_is_ones,
+                   const uint32_t* d_labels, std::unique_ptr<Level>* out) {
+    auto L = std::make_unique<Level>();
+    L->g = g;
+    L->own = std::move(own);
+    const uint32_t n = g->n;
+    const uint64_t nn = std::max<uint64_t>(n, 1);
+    PCC_RETURN_IF_ERROR(L->C.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(L->s.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(L->k.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(L->K.Alloc(ctx_, nn));
+    if (n) {
+      if (k_is_ones || !d_k) {
+        FillF64Kernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, 1.0, L->k.p); PCC_COUNT(1);
+      } else {
+        PCC_CUDA(cudaMemcpyAsync(L->k.p, d_k, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx_->stream));
+      }
+      if (d_labels) {
+        PCC_CUDA(cudaMemcpyAsync(L->C.p, d_labels, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, ctx_->stream));
+        PCC_RETURN_IF_ERROR(L->s.Zero());
+        PCC_RETURN_IF_ERROR(L->K.Zero());
+        AccumulateClustersKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->C.p, L->k.p, L->s.p, L->K.p); PCC_COUNT(1);
+      } else {
+        SingletonsKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->k.p, L->C.p, L->s.p, L->K.p); PCC_COUNT(1);
+      }
+      PCC_RETURN_IF_ERROR(LaunchCheck());
+    }
+    L->int_mode = IntModeFor(*g, cfg_.edge_weight_offset);
+    PCC_RETURN_IF_ERROR(EnsureHubScratch(g->max_deg));
+    *out = std::move(L);
+    return Status::Ok();
+  }
+
+  // Static bins of all vertices of a level (degrees only).
+  Status BuildAllBins(Level* L) {
+    if (L->bins_ready) return Status::Ok();
+    const uint32_t n = L->g->n;
+    BinSet& b = L->all;
+    PCC_RETURN_IF_ERROR(b.list.Alloc(ctx_, std::max<uint64_t>(n, 1)));
+    PCC_RETURN_IF_ERROR(b.counts.Alloc(ctx_, 3 * kNumBins + 1));
+    PCC_RETURN_IF_ERROR(b.counts.Zero());
+    PCC_RETURN_IF_ERROR(BinWith(L->g, PredAll{}, &b));
+    uint32_t host[3 * kNumBins + 1];
+    PCC_RETURN_IF_ERROR(b.counts.ToHost(host, 3 * kNumBins + 1));
+    PCC_RETURN_IF_ERROR(Sync(ctx_));
+    for (int i = 0; i < kNumBins; ++i) b.host_counts[i] = host[i];
+    b.size = n;
+    b.edges = L->g->m;
+    L->bins_ready = true;
+    return Status::Ok();
+  }
+
+  template <class P>
+  Status BinWith(const DevGraph* g, P pred, BinSet* b) {
+    const uint32_t n = g->n;
+    uint32_t* counts = b->counts.p;
+    uint32_t* starts = counts + kNumBins;
+    uint32_t* cursor = starts + kNumBins + 1;
+    PCC_CUDA(cudaMemsetAsync(counts, 0, sizeof(uint32_t) * kNumBins, ctx_->stream));
+    if (n) {
+      BinCountKernel<P><<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g->off.p, pred, counts, ctr_.p); PCC_COUNT(1);
+    }
+    BinStartsKernel<<<1, 1, 0, ctx_->stream>>>(counts, starts, cursor); PCC_COUNT(1);
+    if (n) {
+      BinScatterKernel<P><<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g->off.p, pred, starts, cursor,
+                                                                      b->list.p); PCC_COUNT(1);
+    }
+    return LaunchCheck();
+  }
+
+  // One best-move round over `front` (host_counts known).  Builds the next
+  // frontier in dyn_ unless ALL_MOVE.  Returns whether the next frontier is
+  // non-empty (local_moved).
+  Status Round(Level* L, const BinSet& front, const uint32_t* host_counts, uint64_t front_edges,
+               uint64_t front_size, bool* next_nonempty) {
+    const DevGraph& g = *L->g;
+    const uint32_t n = g.n;
+    stamp_++;
+    res_.rounds++;
+    res_.edge_visits += front_edges;
+    res_.vertex_visits += front_size;
+    res_.algo_bytes += (g.w.p ? 12ull : 8ull) * front_edges + 40ull * front_size;
+    // Reset per-round counters: frontier, movers, new_movers, marked, pend_edges.
+    PCC_CUDA(cudaMemsetAsync(&ctr_.p->frontier, 0, sizeof(uint32_t) * 4, ctx_->stream));
+    PCC_CUDA(cudaMemsetAsync(&ctr_.p->pend_edges, 0, sizeof(unsigned long long), ctx_->stream));
+
+    BMArgs a{};
+    a.n = n;
+    a.off = g.off.p;
+    a.nbr = g.nbr.p;
+    a.w = g.wp();
+    a.C = L->C.p;
+    a.s = L->s.p;
+    a.k = L->k.p;
+    a.K = L->K.p;
+    a.res = cfg_.resolution;
+    a.offset = cfg_.edge_weight_offset;
+    a.ioffset = static_cast<int32_t>(cfg_.edge_weight_offset);
+    a.stamp = stamp_;
+    a.moves = moves_.p;
+    a.moved_stamp = moved_stamp_.p;
+    a.movers = movers_.p;
+    a.ctr = ctr_.p;
+    a.g_keys = g_keys_.p;
+    a.g_vals = reinterpret_cast<unsigned long long*>(g_vals_.p);
+    a.g_cap = g_cap_;
+    a.async = cfg_.async ? 1 : 0;
+    a.s_mut = L->s.p;
+    a.K_mut = L->K.p;
+    a.C_mut = L->C.p;
+    a.moved_cluster_stamp = mod_stamp_.p;
+    const uint32_t* counts = front.counts.p;
+    timer_.Begin(kPhaseBestMoves);
+    PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx_, a, front.list.p, counts, counts + kNumBins, host_counts,
+                                        L->int_mode, g.max_deg));
+    timer_.End(kPhaseBestMoves);
+
+    if (!cfg_.async) {
+      ApplyArgs ap{n, L->C.p, L->s.p, L->k.p, L->K.p, moves_.p, movers_.p, mod_stamp_.p, new_stamp_.p, stamp_,
+                   ctr_.p};
+      const unsigned grid = GridFor(ctx_, front_size);
+      ApplyLeaveKernel<<<grid, kT, 0, ctx_->stream>>>(ap); PCC_COUNT(1);
+      ApplyJoinKernel<<<grid, kT, 0, ctx_->stream>>>(ap); PCC_COUNT(1);
+      PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, ZeroSizeInput{L->s.p, ctr_.p},
+                                              StoreIndexIfSet{zero_ids_.p}, scan_tiles_,
+                                              static_cast<uint32_t*>(nullptr)));
+      PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, NewMoverInput{new_stamp_.p, stamp_, ctr_.p},
+                                              StoreIndexIfSet{new_list_.p}, scan_tiles_,
+                                              static_cast<uint32_t*>(nullptr)));
+      AssignNewKernel<<<grid, kT, 0, ctx_->stream>>>(ap, zero_ids_.p, new_list_.p); PCC_COUNT(1);
+      PCC_RETURN_IF_ERROR(LaunchCheck());
+    }
+
+    if (cfg_.move_method == PCC_ALL_MOVE) {
+      DevCounters hc;
+      PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
+      PCC_RETURN_IF_ERROR(Sync(ctx_));
+      if (!cfg_.async) res_.moves += hc.movers;
+      *next_nonempty = n > 0;
+      return Status::Ok();
+    }
+    // Marked set, then its neighbourhood (edgeMap), then binning.
+    if (cfg_.move_method == PCC_NBHR_CLUSTER_MOVE) {
+      PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, MarkClusterInput{L->C.p, mod_stamp_.p, stamp_},
+                                              StoreIndexIfSet{marked_.p}, scan_tiles_, &ctr_.p->marked));
+    } else {
+      PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, StampInput{moved_stamp_.p, stamp_},
+                                              StoreIndexIfSet{marked_.p}, scan_tiles_, &ctr_.p->marked));
+    }
+    ForEachListEntryKernel<<<GridFor(ctx_, n, kT), kT, 0, ctx_->stream>>>(
+        marked_.p, &ctr_.p->marked, g.off.p, PushNeighbors{g.nbr.p, next_stamp_.p, stamp_}); PCC_COUNT(1);
+    PCC_RETURN_IF_ERROR(LaunchCheck());
+    PCC_RETURN_IF_ERROR(BinWith(&g, PredStamp{next_stamp_.p, stamp_}, &dyn_));
+    DevCounters hc;
+    PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
+    uint32_t hcounts[kNumBins];
+    PCC_RETURN_IF_ERROR(dyn_.counts.ToHost(hcounts, kNumBins));
+    PCC_RETURN_IF_ERROR(Sync(ctx_));
+    for (int i = 0; i < kNumBins; ++i) dyn_.host_counts[i] = hcounts[i];
+    if (!cfg_.async) res_.moves += hc.movers;
+    dyn_.size = hc.frontier;
+    dyn_.edges = hc.pend_edges;
+    *next_nonempty = hc.frontier > 0;
+    return Status::Ok();
+  }
+
+  // IterateBestMoves (parallel-correlation-clusterer.cc:340-365).
+  Status IterateBestMoves(Level* L, int64_t num_inner, bool* moved_out) {
+    PCC_RETURN_IF_ERROR(BuildAllBins(L));
+    bool moved = false;
+    bool local_moved = true;
+    bool use_static = true;
+    for (int64_t it = 0; it < num_inner && local_moved; ++it) {
+      const BinSet& front = use_static ? L->all : dyn_;
+      bool next = false;
+      PCC_RETURN_IF_ERROR(Round(L, front, front.host_counts, front.edges, front.size, &next));
+      local_moved = next;
+      moved |= local_moved;
+      use_static = cfg_.move_method == PCC_ALL_MOVE;
+    }
+    *moved_out = moved;
+    return Status::Ok();
+  }
+
+  // RefineClusters_subroutine (parallel-correlation-clusterer.cc:476-629).
+  // d_k: device node weights or null (all 1); d_init: device labels or null.
+  // On success d_out (device uint32[n]) holds the final dense labels.
+  Status Run(const DevGraph& g0, const double* d_k, const uint32_t* d_init, uint32_t* d_out,
+             uint32_t* num_clusters) {
+    int64_t num_iterations = 0, num_inner = 0;
+    if (cfg_.clustering_moves_method == PCC_LOUVAIN) {
+      num_iterations = cfg_.louvain_num_iterations > 0 ? cfg_.louvain_num_iterations : 10;
+      num_inner = cfg_.louvain_num_inner_iterations > 0 ? cfg_.louvain_num_inner_iterations : 10;
+    } else if (cfg_.clustering_moves_method == PCC_DEFAULT_CLUSTER_MOVES) {
+      return MakeError(PCC_UNIMPLEMENTED, "DEFAULT_CLUSTER_MOVES (whole-cluster moves) is not available on GB300 yet");
+    } else {
+      return MakeError(PCC_UNIMPLEMENTED,
+                       "Correlation clustering moves must be DEFAULT_CLUSTER_MOVES or LOUVAIN.");
+    }
+    if (cfg_.subclustering_method != PCC_NONE_SUBCLUSTERING)
+      return MakeError(PCC_UNIMPLEMENTED, "subclustering_method other than NONE_SUBCLUSTERING is not available");
+    const bool refine = cfg_.refine != 0;
+    const uint32_t n = g0.n;
+    PCC_RETURN_IF_ERROR(Init(n, g0.max_deg));
+
+    std::vector<std::unique_ptr<Level>> rec;
+    if (refine) rec.resize(static_cast<size_t>(num_iterations));
+    std::unique_ptr<Level> helper;
+    PCC_RETURN_IF_ERROR(MakeLevel(&g0, nullptr, d_k, d_k == nullptr, d_init, &helper));
+    DBuf<uint32_t> cluster_ids;
+    PCC_RETURN_IF_ERROR(cluster_ids.Alloc(ctx_, std::max<uint64_t>(n, 1)));
+    if (n) IotaKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, cluster_ids.p); PCC_COUNT(1);
+
+    int64_t iter = 0;
+    for (iter = 0; iter < num_iterations; ++iter) {
+      bool moved = false;
+      PCC_RETURN_IF_ERROR(IterateBestMoves(helper.get(), num_inner, &moved));
+      if (!moved) {
+        iter--;
+        break;
+      }
+      res_.levels++;
+      if (!refine) {
+        if (n) FlattenKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, cluster_ids.p, helper->C.p); PCC_COUNT(1);
+      } else if (iter == num_iterations - 1) {
+        rec[static_cast<size_t>(iter)] = std::move(helper);
+      }
+      if (iter == num_iterations - 1) break;
+      std::unique_ptr<DevGraph> next;
+      timer_.Begin(kPhaseCompress);
+      PCC_RETURN_IF_ERROR(CompressGraph(ctx_, *helper->g, helper->C.p, helper->k.p, &next));
+      timer_.End(kPhaseCompress);
+      DevGraph* ng = next.get();
+      std::unique_ptr<Level> nl;
+      PCC_RETURN_IF_ERROR(MakeLevel(ng, std::move(next), ng->node_w.p, false, nullptr, &nl));
+      if (refine) {
+        rec[static_cast<size_t>(iter)] = std::move(helper);
+      }
+      helper = std::move(nl);
+    }
+
+    if (refine && iter > 0) {
+      DBuf<uint32_t> flat, rank;
+      PCC_RETURN_IF_ERROR(flat.Alloc(ctx_, std::max<uint64_t>(n, 1)));
+      PCC_RETURN_IF_ERROR(rank.Alloc(ctx_, std::max<uint64_t>(n, 1)));
+      for (int64_t i = iter - 1; i >= 0; --i) {
+        Level* Li = rec[static_cast<size_t>(i)].get();
+        Level* Lu = rec[static_cast<size_t>(i + 1)].get();
+        const uint32_t ni = Li->g->n, nu = Lu->g->n;
+        stamp_++;
+        if (ni) {
+          ProjectKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->C.p, Lu->C.p, flat.p, aux_stamp_.p,
+                                                                    stamp_); PCC_COUNT(1);
+          PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, nu, StampInput{aux_stamp_.p, stamp_},
+                                                  StorePrefix<uint32_t>{rank.p}, scan_tiles_,
+                                                  static_cast<uint32_t*>(nullptr)));
+          GatherKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, flat.p, rank.p, Li->C.p); PCC_COUNT(1);
+          PCC_RETURN_IF_ERROR(Li->s.Zero());
+          PCC_RETURN_IF_ERROR(Li->K.Zero());
+          AccumulateClustersKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->C.p, Li->k.p, Li->s.p,
+                                                                                Li->K.p); PCC_COUNT(1);
+          PCC_RETURN_IF_ERROR(LaunchCheck());
+        }
+        bool moved = false;
+        PCC_RETURN_IF_ERROR(IterateBestMoves(Li, num_inner, &moved));
+        res_.refine_passes++;
+        rec[static_cast<size_t>(i + 1)].reset();
+      }
+      PCC_CUDA(cudaMemcpyAsync(cluster_ids.p, rec[0]->C.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice,
+                               ctx_->stream));
+    }
+    rec.clear();
+    helper.reset();
+    PCC_RETURN_IF_ERROR(DenseRank(n, cluster_ids.p, d_out, num_clusters));
+    DevCounters hc;
+    PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
+    PCC_RETURN_IF_ERROR(Sync(ctx_));
+    if (hc.error) return MakeError(PCC_INTERNAL, "device error flag " + std::to_string(hc.error));
+    res_.moves += hc.moves;
+    return Status::Ok();
+  }
+
+  // OutputIndicesById as labels: out[i] = rank of ids[i] among distinct ids.
+  Status DenseRank(uint32_t n, const uint32_t* ids, uint32_t* out, uint32_t* num_groups) {
+    if (n == 0) {
+      *num_groups = 0;
+      return Status::Ok();
+    }
+    stamp_++;
+    DBuf<uint32_t> rank, tot;
+    PCC_RETURN_IF_ERROR(rank.Alloc(ctx_, n));
+    PCC_RETURN_IF_ERROR(tot.Alloc(ctx_, 1));
+    MarkStampKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, ids, aux_stamp_.p, stamp_); PCC_COUNT(1);
+    PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, StampInput{aux_stamp_.p, stamp_},
+                                            StorePrefix<uint32_t>{rank.p}, scan_tiles_, tot.p));
+    GatherKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, ids, rank.p, out); PCC_COUNT(1);
+    PCC_RETURN_IF_ERROR(tot.ToHost(num_groups, 1));
+    PCC_RETURN_IF_ERROR(Sync(ctx_));
+    return Status::Ok();
+  }
+
+  const RunResult& result() const { return res_; }
+  double PhaseMs(int k) const { return timer_.TotalMs(k); }
+  DevCounters* ctr() { return ctr_.p; }
+
+ private:
+  Context* ctx_;
+  pcc_config cfg_;
+  uint32_t n_max_ = 0;
+  uint32_t stamp_ = 0;
+  DBuf<uint32_t> moves_, movers_, moved_stamp_, mod_stamp_, next_stamp_, new_stamp_, aux_stamp_;
+  DBuf<uint32_t> zero_ids_, new_list_, marked_;
+  DBuf<uint32_t> scan_tiles_;
+  DBuf<uint32_t> g_keys_;
+  DBuf<unsigned long long> g_vals_;
+  uint32_t g_cap_ = 0;
+  BinSet dyn_;
+  DBuf<DevCounters> ctr_;
+  RunResult res_;
+  PhaseTimer timer_;
+};
+
+// Objective of dense labels L (< n) with node weights k (device, or null).
+Status ComputeObjectiveDevice(Context* ctx, const DevGraph& g, const uint32_t* L, const double* d_k,
+                              double res, double offset, double* out) {
+  const uint32_t n = g.n;
+  if (n == 0) {
+    *out = 0;
+    return Status::Ok();
+  }
+  DBuf<uint32_t> s;
+  DBuf<double> k, K;
+  PCC_RETURN_IF_ERROR(s.Alloc(ctx, n));
+  PCC_RETURN_IF_ERROR(k.Alloc(ctx, n));
+  PCC_RETURN_IF_ERROR(K.Alloc(ctx, n));
+  if (d_k) {
+    PCC_CUDA(cudaMemcpyAsync(k.p, d_k, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  } else {
+    FillF64Kernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, 1.0, k.p); PCC_COUNT(1);
+  }
+  PCC_RETURN_IF_ERROR(s.Zero());
+  PCC_RETURN_IF_ERROR(K.Zero());
+  AccumulateClustersKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, L, k.p, s.p, K.p); PCC_COUNT(1);
+  const unsigned grid = GridFor(ctx, n, kT);
+  DBuf<double> acc;
+  PCC_RETURN_IF_ERROR(acc.Alloc(ctx, uint64_t(grid) * kT));
+  PCC_RETURN_IF_ERROR(acc.Zero());
+  ForEachEntryKernel<<<grid, kT, 0, ctx->stream>>>(n, g.off.p, ObjEdgeTerm{g.nbr.p, g.wp(), L, offset, acc.p}); PCC_COUNT(1);
+  DBuf<double> part, sums;
+  PCC_RETURN_IF_ERROR(sums.Alloc(ctx, 2));
+  PCC_RETURN_IF_ERROR(Reduce<double>(ctx, uint64_t(grid) * kT, ArrayInputF64{acc.p}, OpAdd{}, 0.0, sums.p, part));
+  PCC_RETURN_IF_ERROR(Reduce<double>(ctx, n, ResTerm{L, k.p, K.p}, OpAdd{}, 0.0, sums.p + 1, part));
+  double h[2];
+  PCC_RETURN_IF_ERROR(sums.ToHost(h, 2));
+  PCC_RETURN_IF_ERROR(Sync(ctx));
+  *out = h[0] - res * h[1] / 2;
+  return Status::Ok();
+}
+
+// ComputeModularity of dense labels (< n).
+Status ComputeModularityDevice(Context* ctx, const DevGraph& g, const uint32_t* L, double resolution,
+                               double* out) {
+  const uint32_t n = g.n;
+  if (n == 0 || g.m == 0) {
+    *out = 0;
+    return Status::Ok();
+  }
+  DBuf<unsigned long long> cnt, deg;
+  PCC_RETURN_IF_ERROR(cnt.Alloc(ctx, 1024));
+  PCC_RETURN_IF_ERROR(cnt.Zero());
+  PCC_RETURN_IF_ERROR(deg.Alloc(ctx, n));
+  PCC_RETURN_IF_ERROR(deg.Zero());
+  ForEachEntryKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, g.off.p, SameLabelCount{g.nbr.p, L, cnt.p}); PCC_COUNT(1);
+  DegreeSumKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, g.off.p, L, deg.p); PCC_COUNT(1);
+  DBuf<unsigned long long> part64, tot64;
+  PCC_RETURN_IF_ERROR(tot64.Alloc(ctx, 1));
+  PCC_RETURN_IF_ERROR(Reduce<unsigned long long>(ctx, 1024, U64Input{cnt.p}, OpAdd{}, 0ull, tot64.p, part64));
+  const double total = static_cast<double>(g.m);
+  DBuf<double> part, sum;
+  PCC_RETURN_IF_ERROR(sum.Alloc(ctx, 1));
+  PCC_RETURN_IF_ERROR(Reduce<double>(ctx, n, ModTerm{deg.p, resolution, total}, OpAdd{}, 0.0, sum.p, part));
+  unsigned long long same = 0;
+  double sub = 0;
+  PCC_RETURN_IF_ERROR(tot64.ToHost(&same, 1));
+  PCC_RETURN_IF_ERROR(sum.ToHost(&sub, 1));
+  PCC_RETURN_IF_ERROR(Sync(ctx));
+  *out = (static_cast<double>(same) - sub) / total;
+  return Status::Ok();
+}
+
+Status ValidateGraphArgs(pcc_context* ctx, const pcc_graph* graph, const pcc_config* cfg) {
+  if (!ctx) return MakeError(PCC_INVALID_ARGUMENT, "null context");
+  if (!graph) return MakeError(PCC_INVALID_ARGUMENT, "null graph");
+  if (!cfg) return MakeError(PCC_INVALID_ARGUMENT, "null config");
+  if (cfg->move_method < 0 || cfg->move_method > 2)
+    return MakeError(PCC_INVALID_ARGUMENT, "move_method must be NBHR_CLUSTER_MOVE, ALL_MOVE or NBHR_MOVE");
+  return Status::Ok();
+}
+
+Status CheckLabels(const uint32_t* labels, uint32_t n) {
+  if (!labels) return Status::Ok();
+  for (uint32_t i = 0; i < n; ++i)
+    if (labels[i] >= n)
+      return MakeError(PCC_INVALID_ARGUMENT, "label of node " + std::to_string(i) + " is " +
+                                                 std::to_string(labels[i]) + ", not below n = " + std::to_string(n));
+  return Status::Ok();
+}
+
+pcc_status Finish(pcc_context* ctx, const Status& st) {
+  if (ctx) ctx->c.last_error = st.ok() ? std::string() : st.msg;
+  return st.code;
+}
+
+struct EventTimer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaStream_t s;
+  explicit EventTimer(cudaStream_t st) : s(st) {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+  }
+  double StopMs() {
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+  }
+  ~EventTimer() {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+};
+
+// Shared body of the correlation / modularity entry points.  `modularity`
+// switches to ComputeModularityConfig's node weights and resolution.
+Status ClusterImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config* config, const double* node_weights,
+                   const uint32_t* initial_labels, uint32_t* out_labels, pcc_stats* stats, bool modularity) {
+  PCC_RETURN_IF_ERROR(ValidateGraphArgs(pctx, graph, config));
+  if (!out_labels) return MakeError(PCC_INVALID_ARGUMENT, "null out_labels");
+  Context* ctx = &pctx->c;
+  const DevGraph& g = graph->g;
+  const uint32_t n = g.n;
+  PCC_RETURN_IF_ERROR(CheckLabels(initial_labels, n));
+  EventTimer timer(ctx->stream);
+  const uint64_t launches0 = LaunchCounter().load();
+  pcc_config cfg = *config;
+  DBuf<double> dk;
+  DBuf<uint32_t> dinit, dout;
+  const uint64_t nn = std::max<uint64_t>(n, 1);
+  if (modularity) {
+    // ComputeModularityConfig (parallel/parallel-graph-utils.cc:141-153).
+    PCC_RETURN_IF_ERROR(dk.Alloc(ctx, nn));
+    if (n) DegreeF64Kernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, g.off.p, dk.p); PCC_COUNT(1);
+    const double total = static_cast<double>(g.m);  // sum of degrees, exact
+    cfg.resolution = config->resolution / total;
+    cfg.edge_weight_offset = 0;
+  } else if (node_weights) {
+    PCC_RETURN_IF_ERROR(dk.Alloc(ctx, nn));
+    PCC_RETURN_IF_ERROR(dk.FromHost(node_weights, n));
+  }
+  if (initial_labels) {
+    PCC_RETURN_IF_ERROR(dinit.Alloc(ctx, nn));
+    PCC_RETURN_IF_ERROR(dinit.FromHost(initial_labels, n));
+  }
+  PCC_RETURN_IF_ERROR(dout.Alloc(ctx, nn));
+  Engine eng(ctx, cfg);
+  uint32_t groups = 0;
+  PCC_RETURN_IF_ERROR(eng.Run(g, dk.p, dinit.p, dout.p, &groups));
+  double obj = 0;
+  PCC_RETURN_IF_ERROR(ComputeObjectiveDevice(ctx, g, dout.p, dk.p, cfg.resolution, cfg.edge_weight_offset, &obj));
+  double mod = 0;
+  if (modularity) PCC_RETURN_IF_ERROR(ComputeModularityDevice(ctx, g, dout.p, config->resolution, &mod));
+  PCC_RETURN_IF_ERROR(dout.ToHost(out_labels, n));
+  PCC_RETURN_IF_ERROR(Sync(ctx));
+  const double ms = timer.StopMs();
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    const RunResult& r = eng.result();
+    stats->edge_visits = r.edge_visits;
+    stats->vertex_visits = r.vertex_visits;
+    stats->moves = r.moves;
+    stats->levels = r.levels;
+    stats->rounds = r.rounds;
+    stats->refine_passes = r.refine_passes;
+    stats->num_clusters = static_cast<int32_t>(groups);
+    stats->objective = obj;
+    stats->modularity = mod;
+    stats->ms_total = ms;
+    stats->ms_best_moves = eng.PhaseMs(kPhaseBestMoves);
+    stats->ms_compress = eng.PhaseMs(kPhaseCompress);
+    stats->kernel_launches = LaunchCounter().load() - launches0;
+    stats->algo_bytes_best_moves = eng.result().algo_bytes;
+  }
+  return Status::Ok();
+}
+
+}  // namespace
+
+}  // namespace pcc
+
+using namespace pcc;
+
+extern "C" {
+
+pcc_status pcc_correlation_cluster(pcc_context* ctx, const pcc_graph* graph, const pcc_config* config,
+                                   const double* node_weights, const uint32_t* initial_labels,
+                                   uint32_t* out_labels, pcc_stats* stats) {
+  try {
+    return Finish(ctx, ClusterImpl(ctx, graph, config, node_weights, initial_labels, out_labels, stats, false));
+  } catch (const std::exception& e) {
+    return Finish(ctx, MakeError(PCC_INTERNAL, e.what()));
+  }
+}
+
+pcc_status pcc_modularity_cluster(pcc_context* ctx, const pcc_graph* graph, const pcc_config* config,
+                                  const uint32_t* initial_labels, uint32_t* out_labels, pcc_stats* stats) {
+  try {
+    return Finish(ctx, ClusterImpl(ctx, graph, config, nullptr, initial_labels, out_labels, stats, true));
+  } catch (const std::exception& e) {
+    return Finish(ctx, MakeError(PCC_INTERNAL, e.what()));
+  }
+}
+
+pcc_status pcc_objective(pcc_context* pctx, const pcc_graph* graph, const pcc_config* config,
+                         const double* node_weights, const uint32_t* labels, double* out_objective) {
+  Status st = ValidateGraphArgs(pctx, graph, config);
+  if (st.ok() && (!labels || !out_objective)) st = MakeError(PCC_INVALID_ARGUMENT, "null labels or output");
+  if (st.ok()) st = CheckLabels(labels, graph->g.n);
+  if (st.ok()) {
+    Context* ctx = &pctx->c;
+    const uint32_t n = graph->g.n;
+    const uint64_t nn = std::max<uint64_t>(n, 1);
+    DBuf<uint32_t> dl;
+    DBuf<double> dk;
+    st = dl.Alloc(ctx, nn);
+    if (st.ok()) st = dl.FromHost(labels, n);
+    if (st.ok() && node_weights) {
+      st = dk.Alloc(ctx, nn);
+      if (st.ok()) st = dk.FromHost(node_weights, n);
+    }
+    if (st.ok())
+      st = ComputeObjectiveDevice(ctx, graph->g, dl.p, dk.p, config->resolution, config->edge_weight_offset,
+                                  out_objective);
+  }
+  return Finish(pctx, st);
+}
+
+pcc_status pcc_modularity(pcc_context* pctx, const pcc_graph* graph, double resolution, const uint32_t* labels,
+                          double* out_modularity) {
+  Status st;
+  if (!pctx || !graph || !labels || !out_modularity) st = MakeError(PCC_INVALID_ARGUMENT, "null argument");
+  if (st.ok()) st = CheckLabels(labels, graph->g.n);
+  if (st.ok()) {
+    Context* ctx = &pctx->c;
+    const uint32_t n = graph->g.n;
+    // ComputeModularity walks the clustering in id order; dense ranks give it.
+    std::vector<uint32_t> present(n, 0), dense(n);
+    for (uint32_t i = 0; i < n; ++i) present[labels[i]] = 1;
+    uint32_t acc = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+      const uint32_t p = present[i];
+      present[i] = acc;
+      acc += p;
+    }
+    for (uint32_t i = 0; i < n; ++i) dense[i] = present[labels[i]];
+    DBuf<uint32_t> dl;
+    st = dl.Alloc(ctx, std::max<uint64_t>(n, 1));
+    if (st.ok()) st = dl.FromHost(dense.data(), n);
+    if (st.ok()) st = ComputeModularityDevice(ctx, graph->g, dl.p, resolution, out_modularity);
+  }
+  return Finish(pctx, st);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Kernel-level entry points used by replay tests: one best-move pass from a
+// given state, and one contraction.
+// ---------------------------------------------------------------------------
+namespace pcc {
+namespace {
+
+Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config* config, const uint32_t* C,
+                     const uint32_t* s, const double* k, const double* K, uint32_t* out_t, double* out_v,
+                     uint32_t* out_moves) {
+  PCC_RETURN_IF_ERROR(ValidateGraphArgs(pctx, graph, config));
+  if (!C || !s || !k || !K || !out_t || !out_v)
+    return MakeError(PCC_INVALID_ARGUMENT, "null state or output array");
+  Context* ctx = &pctx->c;
+  const DevGraph& g = graph->g;
+  const uint32_t n = g.n;
+  PCC_RETURN_IF_ERROR(CheckLabels(C, n));
+  const uint64_t nn = std::max<uint64_t>(n, 1);
+  DBuf<uint32_t> dC, ds, dt, dm, dmoves, dmovers, dstamp;
+  DBuf<double> dk, dK, dv;
+  PCC_RETURN_IF_ERROR(dC.Alloc(ctx, nn));
+  PCC_RETURN_IF_ERROR(ds.Alloc(ctx, nn));
+  PCC_RETURN_IF_ERROR(dk.Alloc(ctx, nn));
+  PCC_RETURN_IF_ERROR(dK.Alloc(ctx, nn));
+  PCC_RETURN_IF_ERROR(dt.Alloc(ctx, nn));
+  PCC_RETURN_IF_ERROR(dv.Alloc(ctx, nn));
+  PCC_RETURN_IF_ERROR(dm.Alloc(ctx, nn));
+  PCC_RETURN_IF_ERROR(dmoves.Alloc(ctx, nn));
+  PCC_RETURN_IF_ERROR(dmovers.Alloc(ctx, nn));
+  PCC_RETURN_IF_ERROR(dstamp.Alloc(ctx, nn));
+  PCC_RETURN_IF_ERROR(dstamp.Zero());
+  PCC_RETURN_IF_ERROR(dC.FromHost(C, n));
+  PCC_RETURN_IF_ERROR(ds.FromHost(s, n));
+  PCC_RETURN_IF_ERROR(dk.FromHost(k, n));
+  PCC_RETURN_IF_ERROR(dK.FromHost(K, n));
+  DBuf<DevCounters> ctr;
+  PCC_RETURN_IF_ERROR(ctr.Alloc(ctx, 1));
+  PCC_RETURN_IF_ERROR(ctr.Zero());
+  BinSet b;
+  PCC_RETURN_IF_ERROR(b.list.Alloc(ctx, nn));
+  PCC_RETURN_IF_ERROR(b.counts.Alloc(ctx, 3 * kNumBins + 1));
+  {
+    uint32_t* counts = b.counts.p;
+    PCC_CUDA(cudaMemsetAsync(counts, 0, sizeof(uint32_t) * kNumBins, ctx->stream));
+    if (n) BinCountKernel<PredAll><<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, g.off.p, PredAll{}, counts, ctr.p); PCC_COUNT(1);
+    BinStartsKernel<<<1, 1, 0, ctx->stream>>>(counts, counts + kNumBins, counts + 2 * kNumBins + 1); PCC_COUNT(1);
+    if (n)
+      BinScatterKernel<PredAll><<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, g.off.p, PredAll{}, counts + kNumBins,
+                                                                         counts + 2 * kNumBins + 1, b.list.p); PCC_COUNT(1);
+    PCC_RETURN_IF_ERROR(LaunchCheck());
+  }
+  DBuf<uint32_t> gk;
+  DBuf<unsigned long long> gv;
+  const uint64_t slots = GlobalHashSlots(ctx, g.max_deg);
+  if (slots) {
+    PCC_RETURN_IF_ERROR(gk.Alloc(ctx, slots));
+    PCC_RETURN_IF_ERROR(gv.Alloc(ctx, slots));
+  }
+  BMArgs a{};
+  a.n = n;
+  a.off = g.off.p;
+  a.nbr = g.nbr.p;
+  a.w = g.wp();
+  a.C = dC.p;
+  a.s = ds.p;
+  a.k = dk.p;
+  a.K = dK.p;
+  a.res = config->resolution;
+  a.offset = config->edge_weight_offset;
+  a.ioffset = static_cast<int32_t>(config->edge_weight_offset);
+  a.stamp = 1;
+  a.moves = dmoves.p;
+  a.moved_stamp = dstamp.p;
+  a.movers = dmovers.p;
+  a.ctr = ctr.p;
+  a.out_target = dt.p;
+  a.out_value = dv.p;
+  a.out_moves = dm.p;
+  a.g_keys = gk.p;
+  a.g_vals = gv.p;
+  a.g_cap = slots ? uint32_t(slots / (uint64_t(ctx->num_sms) * 2)) : 0;
+  a.async = 0;
+  PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx, a, b.list.p, b.counts.p, b.counts.p + kNumBins, nullptr,
+                                      IntModeFor(g, config->edge_weight_offset), g.max_deg));
+  PCC_RETURN_IF_ERROR(dt.ToHost(out_t, n));
+  PCC_RETURN_IF_ERROR(dv.ToHost(out_v, n));
+  if (out_moves) PCC_RETURN_IF_ERROR(dm.ToHost(out_moves, n));
+  DevCounters hc;
+  PCC_RETURN_IF_ERROR(ctr.ToHost(&hc, 1));
+  PCC_RETURN_IF_ERROR(Sync(ctx));
+  if (hc.error) return MakeError(PCC_INTERNAL, "device error flag " + std::to_string(hc.error));
+  return Status::Ok();
+}
+
+}  // namespace
+}  // namespace pcc
+
+extern "C" {
+
+pcc_status pcc_best_moves(pcc_context* ctx, const pcc_graph* graph, const pcc_config* config,
+                          const uint32_t* cluster_ids, const uint32_t* cluster_sizes, const double* node_weights,
+                          const double* cluster_weights, uint32_t* out_targets, double* out_values,
+                          uint32_t* out_moves) {
+  try {
+    return Finish(ctx, BestMovesImpl(ctx, graph, config, cluster_ids, cluster_sizes, node_weights, cluster_weights,
+                                     out_targets, out_values, out_moves));
+  } catch (const std::exception& e) {
+    return Finish(ctx, MakeError(PCC_INTERNAL, e.what()));
+  }
+}
+
+pcc_status pcc_compress(pcc_context* pctx, const pcc_graph* graph, const uint32_t* cluster_ids,
+                        const double* node_weights, pcc_graph** out) {
+  Status st;
+  if (!pctx || !graph || !cluster_ids || !out) st = MakeError(PCC_INVALID_ARGUMENT, "null argument");
+  if (st.ok()) st = CheckLabels(cluster_ids, graph->g.n);
+  if (st.ok()) {
+    Context* ctx = &pctx->c;
+    const uint32_t n = graph->g.n;
+    const uint64_t nn = std::max<uint64_t>(n, 1);
+    DBuf<uint32_t> dC;
+    DBuf<double> dk;
+    st = dC.Alloc(ctx, nn);
+    if (st.ok()) st = dC.FromHost(cluster_ids, n);
+    if (st.ok() && node_weights) {
+      st = dk.Alloc(ctx, nn);
+      if (st.ok()) st = dk.FromHost(node_weights, n);
+    }
+    std::unique_ptr<DevGraph> res;
+    if (st.ok()) st = CompressGraph(ctx, graph->g, dC.p, dk.p, &res);
+    if (st.ok()) st = Sync(ctx);
+    if (st.ok()) {
+      auto* h = new pcc_graph;
+      h->g = std::move(*res);
+      *out = h;
+    }
+  }
+  return Finish(pctx, st);
+}
+
+pcc_status pcc_cluster_host_csr(pcc_context* ctx, uint32_t n, uint64_t m, const uint64_t* offsets,
+                                const uint32_t* neighbors, const float* weights, const pcc_config* config,
+                                int32_t objective, const double* node_weights, uint32_t* out_labels,
+                                pcc_stats* stats) {
+  pcc_graph* g = nullptr;
+  pcc_status st = pcc_graph_upload(ctx, n, m, offsets, neighbors, weights, &g);
+  if (st != PCC_OK) return st;
+  if (objective == 1)
+    st = pcc_modularity_cluster(ctx, g, config, nullptr, out_labels, stats);
+  else if (objective == 0)
+    st = pcc_correlation_cluster(ctx, g, config, node_weights, nullptr, out_labels, stats);
+  else
+    st = Finish(ctx, MakeError(PCC_INVALID_ARGUMENT, "objective must be 0 (correlation) or 1 (modularity)"));
+  std::string err = ctx ? ctx->c.last_error : std::string();
+  pcc_graph_free(ctx, g);
+  if (ctx) ctx->c.last_error = err;
+  return st;
+}
+
+}  // extern "C"

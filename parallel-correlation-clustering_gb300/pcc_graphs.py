@@ -1,0 +1,117 @@
+"""Synthetic graphs and GBBS adjacency I/O (bindings of libpcc_host.so).
+
+The generators make the seeded stand-ins for the reference's evaluation
+graphs: stochastic block models, RMAT (Graph500 quadrant recursion) and
+LFR-like planted partitions.  Outputs are deterministic for a seed on any
+machine and thread count.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from pcc_gb300 import CsrGraph, PccError
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+HOST_LIB = os.path.join(_HERE, "_build", "libpcc_host.so")
+
+
+class _PcchGraph(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_uint32),
+        ("m", ctypes.c_uint64),
+        ("off", ctypes.POINTER(ctypes.c_uint64)),
+        ("nbr", ctypes.POINTER(ctypes.c_uint32)),
+        ("w", ctypes.POINTER(ctypes.c_float)),
+        ("truth", ctypes.POINTER(ctypes.c_uint32)),
+    ]
+
+
+_lib = None
+
+
+def host_lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(HOST_LIB):
+            raise PccError(14, f"host library not built: {HOST_LIB}")
+        L = ctypes.CDLL(HOST_LIB)
+        GP = ctypes.POINTER(_PcchGraph)
+        L.pcch_graph_free.argtypes = [GP]
+        L.pcch_gen_sbm.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_uint64]
+        L.pcch_gen_sbm.restype = GP
+        L.pcch_gen_rmat.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_uint64]
+        L.pcch_gen_rmat.restype = GP
+        L.pcch_gen_lfr.argtypes = [ctypes.c_uint32, ctypes.c_double, ctypes.c_uint32, ctypes.c_double,
+                                   ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_uint64]
+        L.pcch_gen_lfr.restype = GP
+        _lib = L
+    return _lib
+
+
+def _take(gp):
+    """Copies a library-owned graph into numpy arrays and frees it."""
+    g = gp.contents
+    n, m = int(g.n), int(g.m)
+    off = np.ctypeslib.as_array(g.off, shape=(n + 1,)).copy()
+    nbr = np.ctypeslib.as_array(g.nbr, shape=(max(m, 1),))[:m].copy()
+    w = np.ctypeslib.as_array(g.w, shape=(max(m, 1),))[:m].copy() if g.w else None
+    truth = np.ctypeslib.as_array(g.truth, shape=(max(n, 1),))[:n].copy() if g.truth else None
+    host_lib().pcch_graph_free(gp)
+    return CsrGraph(off, nbr, w), truth
+
+
+def sbm(n: int, blocks: int, p_in: float, p_out: float, seed: int):
+    """Stochastic block model; returns (CsrGraph, block of each vertex)."""
+    return _take(host_lib().pcch_gen_sbm(n, blocks, p_in, p_out, seed))
+
+
+def rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+         seed: int = 1) -> CsrGraph:
+    """RMAT graph (symmetrised, deduplicated, no self-loops, unit weights)."""
+    g, _ = _take(host_lib().pcch_gen_rmat(scale, edge_factor, a, b, c, seed))
+    return g
+
+
+def lfr(n: int, mean_degree: float = 20.0, dmax: int = 2000, tau1: float = 2.2, cmin: int = 5,
+        cmax: int = 5000, tau2: float = 2.5, mu: float = 0.3, w_lo: float = 0.5, w_hi: float = 1.5,
+        seed: int = 1):
+    """LFR-like planted partition; returns (CsrGraph, community of each vertex)."""
+    return _take(host_lib().pcch_gen_lfr(n, mean_degree, dmax, tau1, cmin, cmax, tau2, mu, w_lo, w_hi, seed))
+
+
+def write_gbbs(path: str, g: CsrGraph) -> None:
+    """Writes the GBBS text adjacency format (AdjacencyGraph /
+    WeightedAdjacencyGraph: header, n, m, n offsets, m targets, [m weights])."""
+    with open(path, "w") as f:
+        f.write("WeightedAdjacencyGraph\n" if g.weights is not None else "AdjacencyGraph\n")
+        f.write(f"{g.n}\n{g.m}\n")
+        np.savetxt(f, g.offsets[:-1].astype(np.uint64), fmt="%d")
+        np.savetxt(f, g.neighbors.astype(np.uint32), fmt="%d")
+        if g.weights is not None:
+            np.savetxt(f, g.weights.astype(np.float32), fmt="%.9g")
+
+
+def read_gbbs(path: str) -> CsrGraph:
+    """Reads the GBBS text adjacency format."""
+    with open(path) as f:
+        header = f.readline().strip()
+        if header not in ("AdjacencyGraph", "WeightedAdjacencyGraph"):
+            raise PccError(3, f"not a GBBS adjacency graph: {header!r}")
+        data = np.array(f.read().split(), dtype=np.float64)
+    n, m = int(data[0]), int(data[1])
+    need = 2 + n + m + (m if header.startswith("Weighted") else 0)
+    if data.size < need:
+        raise PccError(3, f"truncated GBBS file: {data.size} numbers, need {need}")
+    off = np.empty(n + 1, dtype=np.uint64)
+    off[:n] = data[2:2 + n].astype(np.uint64)
+    off[n] = m
+    nbr = data[2 + n:2 + n + m].astype(np.uint32)
+    w = data[2 + n + m:2 + n + 2 * m].astype(np.float32) if header.startswith("Weighted") else None
+    return CsrGraph(off, nbr, w)

@@ -1,0 +1,242 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the oracle.
+
+Bar (from the clustering path's contract):
+  * integer-weight graphs: best-move decisions, contraction and full sync
+    clusterings are bit-exact;
+  * real weights: objective within 1e-9 relative and >= 99.9% of single-round
+    decisions identical (in practice all, since the <= 1000-degree sums run
+    in the reference's order);
+"""
+
+import numpy as np
+import pytest
+
+import oracle as O
+import pcc_gb300 as P
+import pcc_graphs as G
+from conftest import rand_state
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-9
+
+
+def _graphs():
+    """Named test graphs covering every degree bin and both arithmetic modes."""
+    out = {}
+    g, _ = G.sbm(2000, 20, 0.05, 0.001, 7)
+    out["sbm2k"] = g
+    out["rmat14"] = G.rmat(14, 16, seed=3)          # hubs > 1000 (CTA bin)
+    out["rmat16"] = G.rmat(16, 16, seed=5)          # hubs > 4096 (global-hash bin)
+    lg, _ = G.lfr(20000, mean_degree=20, dmax=1500, seed=9)
+    out["lfr20k_real"] = lg                         # real weights -> FP64 mode
+    rng = np.random.default_rng(11)
+    gi, _ = G.sbm(3000, 10, 0.03, 0.002, 13)
+    src = np.repeat(np.arange(gi.n), np.diff(gi.offsets).astype(np.int64))
+    keep = src < gi.neighbors
+    s, d = src[keep], gi.neighbors[keep].astype(np.int64)
+    w = rng.integers(1, 6, size=s.size).astype(np.float32)
+    out["sbm3k_int"] = P.CsrGraph.from_edges(gi.n, s, d, w)   # integer weights -> INT mode
+    return out
+
+
+@pytest.fixture(scope="module")
+def graphs(built):
+    return _graphs()
+
+
+def _both(ctx, g):
+    return ctx.upload(g), O.OracleGraph(g)
+
+
+@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "rmat16", "sbm3k_int", "lfr20k_real"])
+@pytest.mark.parametrize("nclusters_div", [1, 7, 300])
+def test_best_moves_replay(ctx, graphs, name, nclusters_div):
+    """One sync best-move pass from a random state: GPU == oracle."""
+    g = graphs[name]
+    dg, og = _both(ctx, g)
+    C, s, k, K = rand_state(g.n, g.n // nclusters_div, seed=nclusters_div)
+    for res, off in ((0.01, 0.0), (0.3, 0.0), (0.05, 1.0)):
+        cfg = P.make_config(resolution=res, edge_weight_offset=off)
+        t_g, v_g, m_g = P.best_moves(dg, cfg, C, s, k, K)
+        t_o, v_o, m_o = O.best_moves(og, cfg, C, s, k, K)
+        deg = g.degrees()
+        if g.weights is None or np.all(g.weights == np.round(g.weights)):
+            np.testing.assert_array_equal(t_g, t_o)
+            np.testing.assert_array_equal(v_g.view(np.uint64), v_o.view(np.uint64))
+            np.testing.assert_array_equal(m_g, m_o)
+        else:
+            low = deg <= 1000   # the reference's sequential path: same order, bit-exact
+            np.testing.assert_array_equal(t_g[low], t_o[low])
+            np.testing.assert_array_equal(v_g[low].view(np.uint64), v_o[low].view(np.uint64))
+            agree = np.mean(m_g == m_o)
+            assert agree >= 0.999, agree
+            np.testing.assert_allclose(v_g, v_o, rtol=REL_TOL, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "sbm3k_int", "lfr20k_real"])
+def test_compress_bit_exact(ctx, graphs, name):
+    """CompressGraph: same CSR (ids, order, FP32 sums) and node weights."""
+    g = graphs[name]
+    dg, og = _both(ctx, g)
+    for nclusters_div in (3, 50):
+        C, s, k, K = rand_state(g.n, max(1, g.n // nclusters_div), seed=nclusters_div)
+        k = np.arange(g.n, dtype=np.float64) % 5 + 1
+        gc = P.compress(dg, C, k)
+        got = gc.download()
+        got_k = gc.node_weights()
+        want, want_k = O.compress(og, C, k)
+        np.testing.assert_array_equal(got.offsets, want.offsets)
+        np.testing.assert_array_equal(got.neighbors, want.neighbors)
+        np.testing.assert_array_equal(got.weights.view(np.uint32), want.weights.view(np.uint32))
+        np.testing.assert_array_equal(got_k, want_k)
+        gc.free()
+
+
+CONFIGS = [
+    dict(resolution=0.01, refine=True, move_method=P.ALL_MOVE),
+    dict(resolution=0.05, refine=True, move_method=P.NBHR_MOVE),
+    dict(resolution=0.1, refine=False, move_method=P.NBHR_CLUSTER_MOVE),
+    dict(resolution=0.2, refine=True, move_method=P.NBHR_CLUSTER_MOVE,
+         louvain_num_iterations=3, louvain_num_inner_iterations=4),
+    dict(resolution=0.02, edge_weight_offset=0.0, refine=False, move_method=P.ALL_MOVE,
+         louvain_num_iterations=1),
+]
+
+
+@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "sbm3k_int"])
+@pytest.mark.parametrize("ci", range(len(CONFIGS)))
+def test_correlation_cluster_bit_exact(ctx, graphs, name, ci):
+    g = graphs[name]
+    dg, og = _both(ctx, g)
+    cfg = P.make_config(**CONFIGS[ci])
+    lab_g, st_g = P.correlation_cluster(dg, cfg)
+    lab_o, st_o = O.correlation_cluster(og, cfg)
+    np.testing.assert_array_equal(lab_g, lab_o)
+    assert st_g["num_clusters"] == st_o["num_clusters"]
+    assert st_g["edge_visits"] == st_o["edge_visits"]
+    assert st_g["rounds"] == st_o["rounds"]
+    assert st_g["levels"] == st_o["levels"]
+    assert st_g["objective"] == pytest.approx(st_o["objective"], rel=REL_TOL, abs=1e-9)
+
+
+@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "rmat16"])
+@pytest.mark.parametrize("move", [P.NBHR_MOVE, P.ALL_MOVE])
+def test_modularity_cluster_bit_exact(ctx, graphs, name, move):
+    g = graphs[name]
+    dg, og = _both(ctx, g)
+    cfg = P.make_config(resolution=1.0, refine=True, move_method=move)
+    lab_g, st_g = P.modularity_cluster(dg, cfg)
+    lab_o, st_o = O.modularity_cluster(og, cfg)
+    np.testing.assert_array_equal(lab_g, lab_o)
+    assert st_g["edge_visits"] == st_o["edge_visits"]
+    assert st_g["modularity"] == pytest.approx(st_o["modularity"], rel=REL_TOL, abs=1e-12)
+    assert st_g["objective"] == pytest.approx(st_o["objective"], rel=REL_TOL, abs=1e-12)
+
+
+def test_real_weights_full_run(ctx, graphs):
+    """FP64 mode end to end: objective within 1e-9 relative of the oracle."""
+    g = graphs["lfr20k_real"]
+    dg, og = _both(ctx, g)
+    cfg = P.make_config(resolution=0.1, refine=True, move_method=P.NBHR_CLUSTER_MOVE)
+    lab_g, st_g = P.correlation_cluster(dg, cfg)
+    lab_o, st_o = O.correlation_cluster(og, cfg)
+    assert st_g["objective"] == pytest.approx(st_o["objective"], rel=REL_TOL)
+    assert np.mean(lab_g == lab_o) >= 0.999
+
+
+def test_objective_and_modularity_api(ctx, graphs):
+    g = graphs["sbm2k"]
+    dg, og = _both(ctx, g)
+    rng = np.random.default_rng(0)
+    lab = rng.integers(0, 40, size=g.n).astype(np.uint32)
+    for res, off in ((0.01, 0.0), (0.5, 0.25)):
+        cfg = P.make_config(resolution=res, edge_weight_offset=off)
+        assert P.objective(dg, cfg, lab) == pytest.approx(O.objective(og, cfg, lab), rel=REL_TOL)
+    assert P.modularity(dg, 1.0, lab) == pytest.approx(O.modularity(og, 1.0, lab), rel=REL_TOL)
+
+
+def test_initial_clustering_and_node_weights(ctx, graphs):
+    """RefineClusters(config, &clustering) with node weights (integral)."""
+    g = graphs["sbm3k_int"]
+    dg, og = _both(ctx, g)
+    rng = np.random.default_rng(5)
+    init = rng.integers(0, 200, size=g.n).astype(np.uint32)
+    k = rng.integers(1, 4, size=g.n).astype(np.float64)
+    cfg = P.make_config(resolution=0.05, refine=True, move_method=P.NBHR_MOVE)
+    lab_g, st_g = P.correlation_cluster(dg, cfg, node_weights=k, initial_labels=init)
+    lab_o, st_o = O.correlation_cluster(og, cfg, node_weights=k, initial_labels=init)
+    np.testing.assert_array_equal(lab_g, lab_o)
+
+
+def test_edge_cases(ctx):
+    # isolated vertices, a self-loop, a duplicate entry, a star hub > 4096
+    n = 6000
+    src = [0] * 5000 + [5001, 5002, 5003, 5003]
+    dst = list(range(1, 5001)) + [5002, 5001, 5003, 5004]
+    g = P.CsrGraph.from_edges(n, src, dst, dedupe=False)
+    dg, og = _both(ctx, g)
+    for cfg in (P.make_config(resolution=0.01, refine=True, move_method=P.NBHR_MOVE),
+                P.make_config(resolution=0.5, refine=False, move_method=P.ALL_MOVE)):
+        lab_g, _ = P.correlation_cluster(dg, cfg)
+        lab_o, _ = O.correlation_cluster(og, cfg)
+        np.testing.assert_array_equal(lab_g, lab_o)
+    # a single vertex, no edges
+    g1 = P.CsrGraph(np.zeros(2, np.uint64), np.zeros(0, np.uint32))
+    d1 = ctx.upload(g1)
+    lab, st = P.correlation_cluster(d1, P.make_config(resolution=0.1))
+    assert lab.tolist() == [0] and st["num_clusters"] == 1
+
+
+def test_errors_are_status_codes(ctx, graphs):
+    g = graphs["sbm2k"]
+    dg = ctx.upload(g)
+    with pytest.raises(P.PccError) as e:
+        P.correlation_cluster(dg, P.make_config(clustering_moves_method=7))
+    assert e.value.code == 12  # UNIMPLEMENTED, as the reference
+    with pytest.raises(P.PccError) as e:
+        P.correlation_cluster(dg, P.make_config(subclustering_method=1))
+    assert e.value.code == 12
+    bad = np.full(g.n, g.n + 5, np.uint32)
+    with pytest.raises(P.PccError) as e:
+        P.correlation_cluster(dg, P.make_config(), initial_labels=bad)
+    assert e.value.code == 3  # INVALID_ARGUMENT
+    with pytest.raises(P.PccError) as e:
+        ctx.upload(P.CsrGraph(np.array([0, 1], np.uint64), np.array([7], np.uint32)))
+    assert e.value.code == 3
+
+
+def test_hbm_budget_admission(built):
+    c = P.Context(0, hbm_budget_bytes=1 << 20)
+    g = G.rmat(14, 16, seed=3)
+    with pytest.raises(P.PccError) as e:
+        c.upload(g)
+    assert e.value.code == 8  # RESOURCE_EXHAUSTED
+    c.close()
+
+
+def test_host_csr_end_to_end(ctx, graphs):
+    g = graphs["sbm2k"]
+    og = O.OracleGraph(g)
+    cfg = P.make_config(resolution=1.0, refine=True, move_method=P.NBHR_MOVE)
+    lab_g, _ = P.cluster_host_csr(ctx, g, cfg, objective=1)
+    lab_o, _ = O.modularity_cluster(og, cfg)
+    np.testing.assert_array_equal(lab_g, lab_o)
+
+
+def test_clusterer_class_dropin(ctx, graphs):
+    g = graphs["sbm2k"]
+    og = O.OracleGraph(g)
+    cl = P.ParallelModularityClustererGB300(ctx)
+    cl.set_graph(g)
+    cfg = P.make_config(resolution=1.0, refine=True, move_method=P.NBHR_MOVE)
+    clustering = cl.cluster(cfg)
+    lab_o, _ = O.modularity_cluster(og, cfg)
+    assert clustering == P.labels_to_clustering(lab_o)
+    # RefineClusters from that clustering
+    refined = cl.refine_clusters(cfg, clustering)
+    init = np.empty(g.n, np.uint32)
+    for i, grp in enumerate(clustering):
+        init[grp] = i
+    lab_o2, _ = O.modularity_cluster(og, cfg, initial_labels=init)
+    assert refined == P.labels_to_clustering(lab_o2)
