@@ -35,6 +35,9 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "parallel-correlation-clustering_gb300")
 sys.path.insert(0, PKG)
+# The oracle (CPU restatement) is imported only by the CPU-baseline leg and
+# --impl reference.
+ORACLE_DIR = os.path.join(ROOT, "oracle")
 
 METRIC = "best-move edge-visits/s"
 UNIT = "edge-visits/s"
@@ -140,6 +143,7 @@ class ClockSampler:
 def cpu_baseline(args, P, G):
     """The oracle on the host cores, bounded sample: the same config on an
     RMAT graph of scale --cpu-scale (edge visits/s is size-normalised)."""
+    sys.path.insert(0, ORACLE_DIR)
     import oracle as O
     O.set_threads(0)
     threads = O.get_threads()
@@ -164,6 +168,7 @@ def run_reference(args):
         return
     import pcc_gb300 as P
     import pcc_graphs as G
+    sys.path.insert(0, ORACLE_DIR)
     import oracle as O
     import build_native
     build_native.build_host()
@@ -243,6 +248,8 @@ def main():
     dev_ms = 0.0
     bm_ms = 0.0
     comp_ms = 0.0
+    apply_ms = 0.0
+    front_ms = 0.0
     algo_bytes = 0
     launches = 0
     quality = {}
@@ -253,6 +260,8 @@ def main():
         dev_ms += st["ms_total"]
         bm_ms += st["ms_best_moves"]
         comp_ms += st["ms_compress"]
+        apply_ms += st["ms_apply"]
+        front_ms += st["ms_frontier"]
         launches += st["kernel_launches"]
         algo_bytes += st["algo_bytes_best_moves"]
         quality = {"modularity": st["modularity"], "objective": st["objective"],
@@ -314,7 +323,8 @@ def main():
             "clocks": clocks,
             "gpu_launches": launches,
             "phases_ms_per_step": {"total": dev_ms / args.steps, "best_moves": bm_ms / args.steps,
-                                   "compress": comp_ms / args.steps},
+                                   "compress": comp_ms / args.steps, "apply": apply_ms / args.steps,
+                                   "frontier": front_ms / args.steps},
             "wall_s": wall,
             "quality": quality,
         }

@@ -97,6 +97,8 @@ typedef struct pcc_stats {
   double ms_total;           /* device time of the whole call (CUDA events) */
   double ms_best_moves;      /* device time spent in best-move kernels */
   double ms_compress;        /* device time spent in graph compression */
+  double ms_apply;           /* device time applying sync moves */
+  double ms_frontier;        /* device time building next frontiers */
   uint64_t kernel_launches;  /* CUDA kernels this call launched */
   uint64_t algo_bytes_best_moves; /* algorithmic bytes of the best-move kernels:
                                      (8 or 12) per edge visit + 40 per vertex

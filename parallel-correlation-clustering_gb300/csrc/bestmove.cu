@@ -26,6 +26,8 @@
 
 #include <math_constants.h>
 
+#include <type_traits>
+
 namespace pcc {
 
 namespace {
@@ -56,32 +58,6 @@ __device__ __forceinline__ uint32_t HashSlot(uint32_t key, uint32_t mask) {
 
 // Open addressing with linear probing; keys are cluster ids, kNone = empty.
 // Capacity is at least twice the number of keys, so a free slot exists.
-__device__ __forceinline__ uint32_t FindOrInsert(uint32_t* keys, uint32_t cap, uint32_t key) {
-  const uint32_t mask = cap - 1;
-  uint32_t h = HashSlot(key, mask);
-  for (uint32_t probes = 0; probes < cap; ++probes) {
-    const uint32_t k = keys[h];
-    if (k == key) return h;
-    if (k == kNone) {
-      const uint32_t old = atomicCAS(&keys[h], kNone, key);
-      if (old == kNone || old == key) return h;
-    }
-    h = (h + 1) & mask;
-  }
-  return kNone;
-}
-
-__device__ __forceinline__ uint32_t Find(const uint32_t* keys, uint32_t cap, uint32_t key) {
-  const uint32_t mask = cap - 1;
-  uint32_t h = HashSlot(key, mask);
-  for (uint32_t probes = 0; probes < cap; ++probes) {
-    const uint32_t k = keys[h];
-    if (k == key) return h;
-    if (k == kNone) return kNone;
-    h = (h + 1) & mask;
-  }
-  return kNone;
-}
 
 // (val desc, id asc) ordering used by every argmax.
 __device__ __forceinline__ bool Better(double va, uint32_t ia, double vb, uint32_t ib) {
@@ -277,137 +253,11 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
 }
 
 // ---------------------------------------------------------------------------
-// One warp per vertex, degree <= 1000, shared-memory hash of HC slots.
-// Chunks of 32 entries in adjacency order; per chunk the leader of each
-// cluster id adds its peers one by one (FP64) onto the slot's running sum,
-// which keeps the reference's adjacency-order summation exactly.
+// Hash tables with an occupied-slot list.  The table starts clean (keys
+// kNone, values 0); each insert appends its slot to `used`, and after the
+// vertex only the used slots are read and cleared, so the cost per vertex is
+// proportional to its distinct neighbour clusters, not to the capacity.
 // ---------------------------------------------------------------------------
-constexpr int kWarpKernelWarps = 4;
-
-template <int HC>
-constexpr size_t WarpKernelSmem() {
-  return size_t(kWarpKernelWarps) * HC * (8 + 4) + size_t(kWarpKernelWarps) * 32 * 8;
-}
-
-template <int HC, bool kInt, bool kAsync>
-__global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMArgs a,
-                                                                           const uint32_t* __restrict__ list,
-                                                                           const uint32_t* __restrict__ bin_counts,
-                                                                           const uint32_t* __restrict__ bin_starts,
-                                                                           int bin) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const uint32_t count = bin_counts[bin];
-  const uint32_t start = bin_starts[bin];
-  const unsigned lane = LaneId(), warp = threadIdx.x >> 5;
-  unsigned long long* vals = reinterpret_cast<unsigned long long*>(smem) + size_t(warp) * HC;
-  uint32_t* keys = reinterpret_cast<uint32_t*>(smem + size_t(kWarpKernelWarps) * HC * 8) + size_t(warp) * HC;
-  double* stage = reinterpret_cast<double*>(smem + size_t(kWarpKernelWarps) * HC * 12) + size_t(warp) * 32;
-  for (uint64_t idx = uint64_t(blockIdx.x) * kWarpKernelWarps + warp; idx < count;
-       idx += uint64_t(gridDim.x) * kWarpKernelWarps) {
-    const VertexCtx x = LoadVertex<kAsync>(a, list[start + idx]);
-    for (int i = lane; i < HC; i += 32) {
-      keys[i] = kNone;
-      vals[i] = 0ull;
-    }
-    __syncwarp();
-    for (uint32_t e0 = 0; e0 < x.d; e0 += 32) {
-      const uint32_t e = e0 + lane;
-      const bool has = e < x.d;
-      uint32_t u = x.v;
-      float wt = 0.f;
-      if (has) {
-        u = a.nbr[x.b + e];
-        wt = a.w ? a.w[x.b + e] : 1.0f;
-      }
-      const bool cand = has && u != x.v;
-      const uint32_t cu = cand ? LdC<kAsync>(a.C + u) : kNone;
-      const unsigned long long key = cand ? cu : (0x100000000ull | lane);
-      const unsigned peers = __match_any_sync(kFull, key);
-      const bool leader = cand && int(lane) == __ffs(peers) - 1;
-      if (kInt) {
-        const int xi = cand ? (static_cast<int>(wt) - a.ioffset) : 0;
-        const int S = __reduce_add_sync(peers, xi);
-        if (leader) {
-          const uint32_t slot = FindOrInsert(keys, HC, cu);
-          if (slot != kNone)
-            vals[slot] += static_cast<unsigned long long>(static_cast<long long>(S));
-          else
-            atomicExch(&a.ctr->error, kErrHashFull);
-        }
-      } else {
-        stage[lane] = cand ? Dsub(static_cast<double>(wt), a.offset) : 0.0;
-        __syncwarp();
-        if (leader) {
-          const uint32_t slot = FindOrInsert(keys, HC, cu);
-          if (slot == kNone) {
-            atomicExch(&a.ctr->error, kErrHashFull);
-          } else {
-          double acc = __longlong_as_double(static_cast<long long>(vals[slot]));
-          unsigned mm = peers;
-          while (mm) {
-            const int j = __ffs(mm) - 1;
-            acc = Dadd(acc, stage[j]);
-            mm &= mm - 1;
-          }
-          vals[slot] = static_cast<unsigned long long>(__double_as_longlong(acc));
-          }
-        }
-      }
-      __syncwarp();
-    }
-    double T = 0.0;
-    if (lane == 0) {
-      const uint32_t slot = Find(keys, HC, x.c);
-      if (slot != kNone)
-        T = kInt ? static_cast<double>(static_cast<long long>(vals[slot]))
-                 : __longlong_as_double(static_cast<long long>(vals[slot]));
-    }
-    T = __shfl_sync(kFull, T, 0);
-    const double change = ChangeOf(a, x, T);
-    double best = -CUDART_INF;
-    uint32_t bid = kNone;
-    for (int i = lane; i < HC; i += 32) {
-      const uint32_t key = keys[i];
-      if (key == kNone) continue;
-      const double S = kInt ? static_cast<double>(static_cast<long long>(vals[i]))
-                            : __longlong_as_double(static_cast<long long>(vals[i]));
-      const double val = ValOf(a, x.kv, change, S, LdK<kAsync>(a.K + key));
-      if (Better(val, key, best, bid)) {
-        best = val;
-        bid = key;
-      }
-    }
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
-      const double ov = __shfl_xor_sync(kFull, best, o);
-      const uint32_t oid = __shfl_xor_sync(kFull, bid, o);
-      if (Better(ov, oid, best, bid)) {
-        best = ov;
-        bid = oid;
-      }
-    }
-    bool append = false;
-    if (lane == 0) append = Decide<kAsync>(a, x, best, bid, change);
-    if (!kAsync) {
-      const uint32_t slot = WarpAppendFull(&a.ctr->movers, append);
-      if (append) a.movers[slot] = x.v;
-    }
-    __syncwarp();
-  }
-}
-
-// ---------------------------------------------------------------------------
-// One CTA per hub vertex (degree > 1000).  The hash lives in shared memory
-// (kCtaHashSlots) or, for kGlobal, in a per-CTA region of global scratch.
-// Warp-level pre-aggregation (match.any), then atomic adds into the table.
-// FP64 mode follows the reference's hub path: w - offset rounded to float.
-// ---------------------------------------------------------------------------
-constexpr int kCtaThreads = 512;
-constexpr size_t kCtaStage = size_t(kCtaThreads / 32) * 32 * 8;
-constexpr size_t kCtaSmem = kCtaStage + size_t(kCtaHashSlots) * 12;
-
-// Loads from the hash table; the global-memory table is read from L2 so a
-// line cached in L1 before another warp's atomic never hides the update.
 template <bool kGlobal>
 __device__ __forceinline__ uint32_t HKey(const uint32_t* keys, uint32_t i) {
   return kGlobal ? __ldcg(keys + i) : keys[i];
@@ -417,16 +267,22 @@ __device__ __forceinline__ unsigned long long HVal(const unsigned long long* val
   return kGlobal ? __ldcg(vals + i) : vals[i];
 }
 
+// Finds or inserts `key`; *inserted is set when this call claimed the slot.
 template <bool kGlobal>
-__device__ __forceinline__ uint32_t FindOrInsertT(uint32_t* keys, uint32_t cap, uint32_t key) {
+__device__ __forceinline__ uint32_t FindOrInsertT(uint32_t* keys, uint32_t cap, uint32_t key, bool* inserted) {
   const uint32_t mask = cap - 1;
   uint32_t h = HashSlot(key, mask);
+  *inserted = false;
   for (uint32_t probes = 0; probes < cap; ++probes) {
     const uint32_t k = HKey<kGlobal>(keys, h);
     if (k == key) return h;
     if (k == kNone) {
       const uint32_t old = atomicCAS(&keys[h], kNone, key);
-      if (old == kNone || old == key) return h;
+      if (old == kNone) {
+        *inserted = true;
+        return h;
+      }
+      if (old == key) return h;
     }
     h = (h + 1) & mask;
   }
@@ -452,6 +308,147 @@ __device__ __forceinline__ double AsDouble(unsigned long long bits) {
               : __longlong_as_double(static_cast<long long>(bits));
 }
 
+// ---------------------------------------------------------------------------
+// One warp per vertex, degree <= 1000, shared-memory hash of HC slots.
+// Chunks of 32 entries in adjacency order; per chunk the leader of each
+// cluster id adds its peers one by one (FP64) onto the slot's running sum,
+// which keeps the reference's adjacency-order summation exactly.
+// ---------------------------------------------------------------------------
+constexpr int kWarpKernelWarps = 4;
+
+template <int HC>
+constexpr size_t WarpKernelSmem() {
+  // per warp: vals HC*8, keys HC*4, used HC/2 * 2, stage 32*8, count 16
+  return size_t(kWarpKernelWarps) * (size_t(HC) * 13 + 32 * 8 + 16);
+}
+
+template <int HC, bool kInt, bool kAsync>
+__global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMArgs a,
+                                                                           const uint32_t* __restrict__ list,
+                                                                           const uint32_t* __restrict__ bin_counts,
+                                                                           const uint32_t* __restrict__ bin_starts,
+                                                                           int bin) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const uint32_t count = bin_counts[bin];
+  const uint32_t start = bin_starts[bin];
+  const unsigned lane = LaneId(), warp = threadIdx.x >> 5;
+  unsigned char* base = smem + size_t(warp) * (size_t(HC) * 13 + 32 * 8 + 16);
+  unsigned long long* vals = reinterpret_cast<unsigned long long*>(base);
+  uint32_t* keys = reinterpret_cast<uint32_t*>(base + size_t(HC) * 8);
+  double* stage = reinterpret_cast<double*>(base + size_t(HC) * 12);
+  uint16_t* used = reinterpret_cast<uint16_t*>(base + size_t(HC) * 12 + 32 * 8);
+  uint32_t* used_count = reinterpret_cast<uint32_t*>(base + size_t(HC) * 13 + 32 * 8);
+  for (int i = lane; i < HC; i += 32) {
+    keys[i] = kNone;
+    vals[i] = 0ull;
+  }
+  if (lane == 0) *used_count = 0;
+  __syncwarp();
+  for (uint64_t idx = uint64_t(blockIdx.x) * kWarpKernelWarps + warp; idx < count;
+       idx += uint64_t(gridDim.x) * kWarpKernelWarps) {
+    const VertexCtx x = LoadVertex<kAsync>(a, list[start + idx]);
+    for (uint32_t e0 = 0; e0 < x.d; e0 += 32) {
+      const uint32_t e = e0 + lane;
+      const bool has = e < x.d;
+      uint32_t u = x.v;
+      float wt = 0.f;
+      if (has) {
+        u = a.nbr[x.b + e];
+        wt = a.w ? a.w[x.b + e] : 1.0f;
+      }
+      const bool cand = has && u != x.v;
+      const uint32_t cu = cand ? LdC<kAsync>(a.C + u) : kNone;
+      const unsigned long long key = cand ? cu : (0x100000000ull | lane);
+      const unsigned peers = __match_any_sync(kFull, key);
+      const bool leader = cand && int(lane) == __ffs(peers) - 1;
+      uint32_t slot = kNone;
+      if (leader) {
+        bool ins = false;
+        slot = FindOrInsertT<false>(keys, HC, cu, &ins);
+        if (slot == kNone) {
+          atomicExch(&a.ctr->error, kErrHashFull);
+        } else if (ins) {
+          used[atomicAdd(used_count, 1u)] = static_cast<uint16_t>(slot);
+        }
+      }
+      if (kInt) {
+        const int xi = cand ? (static_cast<int>(wt) - a.ioffset) : 0;
+        const int S = __reduce_add_sync(peers, xi);
+        if (slot != kNone) vals[slot] += static_cast<unsigned long long>(static_cast<long long>(S));
+      } else {
+        stage[lane] = cand ? Dsub(static_cast<double>(wt), a.offset) : 0.0;
+        __syncwarp();
+        if (slot != kNone) {
+          double acc = __longlong_as_double(static_cast<long long>(vals[slot]));
+          unsigned mm = peers;
+          while (mm) {
+            const int j = __ffs(mm) - 1;
+            acc = Dadd(acc, stage[j]);
+            mm &= mm - 1;
+          }
+          vals[slot] = static_cast<unsigned long long>(__double_as_longlong(acc));
+        }
+      }
+      __syncwarp();
+    }
+    double T = 0.0;
+    if (lane == 0) {
+      const uint32_t slot = FindT<false>(keys, HC, x.c);
+      if (slot != kNone) T = AsDouble<kInt>(vals[slot]);
+    }
+    T = __shfl_sync(kFull, T, 0);
+    const double change = ChangeOf(a, x, T);
+    const uint32_t nused = *used_count;
+    double best = -CUDART_INF;
+    uint32_t bid = kNone;
+    for (uint32_t i = lane; i < nused; i += 32) {
+      const uint32_t slot = used[i];
+      const uint32_t key = keys[slot];
+      const double S = AsDouble<kInt>(vals[slot]);
+      const double val = ValOf(a, x.kv, change, S, LdK<kAsync>(a.K + key));
+      if (Better(val, key, best, bid)) {
+        best = val;
+        bid = key;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+      const double ov = __shfl_xor_sync(kFull, best, o);
+      const uint32_t oid = __shfl_xor_sync(kFull, bid, o);
+      if (Better(ov, oid, best, bid)) {
+        best = ov;
+        bid = oid;
+      }
+    }
+    __syncwarp();
+    for (uint32_t i = lane; i < nused; i += 32) {
+      const uint32_t slot = used[i];
+      keys[slot] = kNone;
+      vals[slot] = 0ull;
+    }
+    bool append = false;
+    if (lane == 0) append = Decide<kAsync>(a, x, best, bid, change);
+    if (!kAsync) {
+      const uint32_t pos = WarpAppendFull(&a.ctr->movers, append);
+      if (append) a.movers[pos] = x.v;
+    }
+    __syncwarp();
+    if (lane == 0) *used_count = 0;
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// One CTA per hub vertex (degree > 1000).  The hash lives in shared memory
+// (kCtaHashSlots) or, for kGlobal, in a per-CTA region of global scratch
+// that stays clean between vertices (only used slots are cleared).
+// Warp-level pre-aggregation (match.any), then atomic adds into the table.
+// FP64 mode follows the reference's hub path: w - offset rounded to float.
+// ---------------------------------------------------------------------------
+constexpr int kCtaThreads = 512;
+constexpr size_t kCtaStage = size_t(kCtaThreads / 32) * 32 * 8;
+constexpr size_t kCtaSmem = kCtaStage + size_t(kCtaHashSlots) * 12 + size_t(kCtaHashSlots / 2) * 2;
+
 template <bool kInt, bool kGlobal, bool kAsync>
 __global__ void __launch_bounds__(kCtaThreads) BestMoveCtaKernel(BMArgs a, const uint32_t* __restrict__ list,
                                                                 const uint32_t* __restrict__ bin_counts,
@@ -460,19 +457,30 @@ __global__ void __launch_bounds__(kCtaThreads) BestMoveCtaKernel(BMArgs a, const
   __shared__ double red_val[kCtaThreads / 32];
   __shared__ uint32_t red_id[kCtaThreads / 32];
   __shared__ double sh_T;
+  __shared__ uint32_t sh_used;
   const uint32_t count = bin_counts[bin];
   const uint32_t start = bin_starts[bin];
   const unsigned lane = LaneId(), warp = threadIdx.x >> 5;
   double* stage = reinterpret_cast<double*>(smem) + size_t(warp) * 32;
+  using UsedT = typename std::conditional<kGlobal, uint32_t, uint16_t>::type;
   unsigned long long* vals;
   uint32_t* keys;
+  UsedT* used;
   if (kGlobal) {
     vals = a.g_vals + size_t(blockIdx.x) * a.g_cap;
     keys = a.g_keys + size_t(blockIdx.x) * a.g_cap;
+    used = reinterpret_cast<UsedT*>(a.g_used + size_t(blockIdx.x) * (a.g_cap / 2));
   } else {
     vals = reinterpret_cast<unsigned long long*>(smem + kCtaStage);
     keys = reinterpret_cast<uint32_t*>(smem + kCtaStage + size_t(kCtaHashSlots) * 8);
+    used = reinterpret_cast<UsedT*>(smem + kCtaStage + size_t(kCtaHashSlots) * 12);
+    for (uint32_t i = threadIdx.x; i < kCtaHashSlots; i += kCtaThreads) {
+      keys[i] = kNone;
+      vals[i] = 0ull;
+    }
   }
+  if (threadIdx.x == 0) sh_used = 0;
+  __syncthreads();
   for (uint64_t idx = blockIdx.x; idx < count; idx += gridDim.x) {
     const VertexCtx x = LoadVertex<kAsync>(a, list[start + idx]);
     uint32_t cap = kCtaHashSlots;
@@ -484,11 +492,6 @@ __global__ void __launch_bounds__(kCtaThreads) BestMoveCtaKernel(BMArgs a, const
         continue;
       }
     }
-    for (uint32_t i = threadIdx.x; i < cap; i += kCtaThreads) {
-      keys[i] = kNone;
-      vals[i] = 0ull;
-    }
-    __syncthreads();
     const uint32_t rounds = (x.d + kCtaThreads - 1) / kCtaThreads;
     for (uint32_t r = 0; r < rounds; ++r) {
       const uint32_t e = r * kCtaThreads + threadIdx.x;
@@ -504,22 +507,26 @@ __global__ void __launch_bounds__(kCtaThreads) BestMoveCtaKernel(BMArgs a, const
       const unsigned long long key = cand ? cu : (0x100000000ull | lane);
       const unsigned peers = __match_any_sync(kFull, key);
       const bool leader = cand && int(lane) == __ffs(peers) - 1;
+      uint32_t slot = kNone;
+      if (leader) {
+        bool ins = false;
+        slot = FindOrInsertT<kGlobal>(keys, cap, cu, &ins);
+        if (slot == kNone) {
+          atomicExch(&a.ctr->error, kErrHashFull);
+        } else if (ins) {
+          used[atomicAdd(&sh_used, 1u)] = static_cast<UsedT>(slot);
+        }
+      }
       if (kInt) {
         const int xi = cand ? (static_cast<int>(wt) - a.ioffset) : 0;
         const int S = __reduce_add_sync(peers, xi);
-        if (leader) {
-          const uint32_t slot = FindOrInsertT<kGlobal>(keys, cap, cu);
-          if (slot != kNone)
-            atomicAdd(&vals[slot], static_cast<unsigned long long>(static_cast<long long>(S)));
-          else
-            atomicExch(&a.ctr->error, kErrHashFull);
-        }
+        if (slot != kNone) atomicAdd(&vals[slot], static_cast<unsigned long long>(static_cast<long long>(S)));
       } else {
         // Hub path of the reference: `float weight; weight -= offset;`
         const float wf = static_cast<float>(Dsub(static_cast<double>(wt), a.offset));
         stage[lane] = cand ? static_cast<double>(wf) : 0.0;
         __syncwarp();
-        if (leader) {
+        if (slot != kNone) {
           double acc = 0.0;
           unsigned mm = peers;
           while (mm) {
@@ -527,11 +534,7 @@ __global__ void __launch_bounds__(kCtaThreads) BestMoveCtaKernel(BMArgs a, const
             acc = Dadd(acc, stage[j]);
             mm &= mm - 1;
           }
-          const uint32_t slot = FindOrInsertT<kGlobal>(keys, cap, cu);
-          if (slot != kNone)
-            atomicAdd(reinterpret_cast<double*>(&vals[slot]), acc);
-          else
-            atomicExch(&a.ctr->error, kErrHashFull);
+          atomicAdd(reinterpret_cast<double*>(&vals[slot]), acc);
         }
         __syncwarp();
       }
@@ -543,12 +546,13 @@ __global__ void __launch_bounds__(kCtaThreads) BestMoveCtaKernel(BMArgs a, const
     }
     __syncthreads();
     const double change = ChangeOf(a, x, sh_T);
+    const uint32_t nused = sh_used;
     double best = -CUDART_INF;
     uint32_t bid = kNone;
-    for (uint32_t i = threadIdx.x; i < cap; i += kCtaThreads) {
-      const uint32_t key = HKey<kGlobal>(keys, i);
-      if (key == kNone) continue;
-      const double S = AsDouble<kInt>(HVal<kGlobal>(vals, i));
+    for (uint32_t i = threadIdx.x; i < nused; i += kCtaThreads) {
+      const uint32_t slot = kGlobal ? __ldcg(reinterpret_cast<const uint32_t*>(used) + i) : uint32_t(used[i]);
+      const uint32_t key = HKey<kGlobal>(keys, slot);
+      const double S = AsDouble<kInt>(HVal<kGlobal>(vals, slot));
       const double val = ValOf(a, x.kv, change, S, LdK<kAsync>(a.K + key));
       if (Better(val, key, best, bid)) {
         best = val;
@@ -569,6 +573,11 @@ __global__ void __launch_bounds__(kCtaThreads) BestMoveCtaKernel(BMArgs a, const
       red_id[warp] = bid;
     }
     __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nused; i += kCtaThreads) {
+      const uint32_t slot = kGlobal ? __ldcg(reinterpret_cast<const uint32_t*>(used) + i) : uint32_t(used[i]);
+      keys[slot] = kNone;
+      vals[slot] = 0ull;
+    }
     if (threadIdx.x == 0) {
       for (int w = 1; w < kCtaThreads / 32; ++w) {
         if (Better(red_val[w], red_id[w], best, bid)) {
@@ -578,6 +587,7 @@ __global__ void __launch_bounds__(kCtaThreads) BestMoveCtaKernel(BMArgs a, const
       }
       const bool append = Decide<kAsync>(a, x, best, bid, change);
       if (!kAsync && append) a.movers[atomicAdd(&a.ctr->movers, 1u)] = x.v;
+      sh_used = 0;
     }
     __syncthreads();
   }
@@ -646,6 +656,8 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
 }  // namespace
 
 uint64_t GlobalHashSlots(Context* ctx, uint32_t max_deg) {
+  // Per CTA: a table of the next power of two >= 2 * max degree; one CTA per
+  // grid slot of the hub kernel (2 per SM).
   if (max_deg <= kBinMaxDeg[kBinCta]) return 0;
   uint64_t cap = 1024;
   while (cap < 2ull * max_deg + 2) cap <<= 1;

@@ -219,6 +219,8 @@ struct PhaseTimer {
 };
 constexpr int kPhaseBestMoves = 0;
 constexpr int kPhaseCompress = 1;
+constexpr int kPhaseApply = 2;
+constexpr int kPhaseFrontier = 3;
 
 inline unsigned Blocks(uint64_t items, unsigned per_block, unsigned cap) {
   uint64_t b = (items + per_block - 1) / per_block;

@@ -51,7 +51,7 @@ struct KeyBuilder {
   uint32_t bits;
   uint8_t* keep;
   uint64_t* key;
-  __device__ void operator()(uint32_t u, uint64_t j) const {
+  __device__ void operator()(uint32_t u, uint64_t j, uint64_t) const {
     const uint32_t v = nbr[j];
     const uint32_t cu = C[u], cv = C[v];
     const bool k = v <= u || cu != cv;
@@ -219,8 +219,9 @@ Status CompressGraph(Context* ctx, const DevGraph& g, const uint32_t* C, const d
   PCC_RETURN_IF_ERROR(keep.Alloc(ctx, g.m ? g.m : 1));
   PCC_RETURN_IF_ERROR(key_full.Alloc(ctx, g.m ? g.m : 1));
   if (g.m) {
-    ForEachEntryKernel<<<Blocks(n, 256, ctx->num_sms * 16), 256, 0, st>>>(
-        n, g.off.p, KeyBuilder{g.nbr.p, C, rank.p, bits, keep.p, key_full.p}); PCC_COUNT(1);
+    LaunchEdgeIter(ctx, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins, g.bins.host_counts, g.off.p,
+                   KeyBuilder{g.nbr.p, C, rank.p, bits, keep.p, key_full.p});
+    PCC_RETURN_IF_ERROR(LaunchCheck());
   }
   DBuf<uint64_t> keys;
   DBuf<uint32_t> vals;

@@ -16,25 +16,6 @@
 namespace pcc {
 
 // ---------------------------------------------------------------------------
-// Graph resident in HBM.
-// ---------------------------------------------------------------------------
-struct DevGraph {
-  uint32_t n = 0;
-  uint64_t m = 0;
-  DBuf<uint64_t> off;
-  DBuf<uint32_t> nbr;
-  DBuf<float> w;          // empty => unit weights
-  DBuf<double> node_w;    // node weights attached by compression
-  uint32_t max_deg = 0;
-  bool integral = true;   // every weight is an integer value
-  double max_abs_w = 1.0; // max |w| (1 for unit weights)
-  const float* wp() const { return w.p; }
-};
-
-// Computes max degree / weight properties on the device (one sync).
-Status ComputeGraphProperties(Context* ctx, DevGraph* g);
-
-// ---------------------------------------------------------------------------
 // Degree bins.  Each bin is served by one best-move kernel shape:
 //   d <= 4, 8, 16, 32    lane groups of 4/8/16/32 lanes, one chunk
 //   d <= 128/256/512     one warp, shared-memory hash of 256/512/1024 slots
@@ -65,6 +46,36 @@ __host__ __device__ inline int BinOf(uint64_t d) {
   return kBinGlobal;
 }
 
+// Degree-binned vertex list: bins are contiguous segments of `list`.
+struct BinSet {
+  DBuf<uint32_t> list;       // n entries
+  DBuf<uint32_t> counts;     // [kNumBins] counts, then [kNumBins+1] starts
+  uint64_t edges = 0;        // sum of degrees (host copy, static bins only)
+  uint32_t size = 0;         // vertices (host copy, static bins only)
+  uint32_t host_counts[kNumBins] = {0};
+};
+
+// ---------------------------------------------------------------------------
+// Graph resident in HBM.
+// ---------------------------------------------------------------------------
+struct DevGraph {
+  uint32_t n = 0;
+  uint64_t m = 0;
+  DBuf<uint64_t> off;
+  DBuf<uint32_t> nbr;
+  DBuf<float> w;          // empty => unit weights
+  DBuf<double> node_w;    // node weights attached by compression
+  BinSet bins;            // static degree bins of all vertices
+  uint32_t max_deg = 0;
+  bool integral = true;   // every weight is an integer value
+  double max_abs_w = 1.0; // max |w| (1 for unit weights)
+  const float* wp() const { return w.p; }
+};
+
+// Computes max degree / weight properties and the static degree bins on
+// the device (one sync).
+Status ComputeGraphProperties(Context* ctx, DevGraph* g);
+
 // Device counters of one call (all in one allocation).
 struct DevCounters {
   uint32_t bin_count[kNumBins];
@@ -87,15 +98,6 @@ struct DevCounters {
 
 constexpr int kErrProbeLimit = 1;   // async new-cluster probe exceeded its bound
 constexpr int kErrHashFull = 2;     // a best-move hash table filled up
-
-// Degree-binned vertex list: bins are contiguous segments of `list`.
-struct BinSet {
-  DBuf<uint32_t> list;       // n entries
-  DBuf<uint32_t> counts;     // [kNumBins] counts, then [kNumBins+1] starts
-  uint64_t edges = 0;        // sum of degrees (host copy, static bins only)
-  uint32_t size = 0;         // vertices (host copy, static bins only)
-  uint32_t host_counts[kNumBins] = {0};
-};
 
 // Best-move kernel arguments.
 struct BMArgs {
@@ -121,8 +123,9 @@ struct BMArgs {
   double* out_value;
   uint32_t* out_moves;
   // global-hash scratch for the hub bin
-  uint32_t* g_keys;
-  unsigned long long* g_vals;
+  uint32_t* g_keys;         // clean (kNone) between vertices
+  unsigned long long* g_vals;  // clean (0) between vertices
+  uint32_t* g_used;         // per-CTA occupied-slot lists (g_cap / 2 each)
   uint32_t g_cap;           // slots per CTA
   // async mode: apply moves immediately with atomics
   int async;

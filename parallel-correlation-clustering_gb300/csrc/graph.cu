@@ -5,7 +5,7 @@
 // once into HBM and stay there for every clustering call.
 #include <cmath>
 
-#include "engine.cuh"
+#include "graphops.cuh"
 
 namespace pcc {
 
@@ -53,6 +53,16 @@ __global__ void CheckCsrKernel(uint32_t n, uint64_t m, const uint64_t* __restric
 
 }  // namespace
 
+__global__ void BinStartsKernel(const uint32_t* counts, uint32_t* starts, uint32_t* cursor) {
+  uint32_t acc = 0;
+  for (int b = 0; b < kNumBins; ++b) {
+    starts[b] = acc;
+    acc += counts[b];
+    cursor[b] = 0;
+  }
+  starts[kNumBins] = acc;
+}
+
 Status ComputeGraphProperties(Context* ctx, DevGraph* g) {
   DBuf<uint32_t> part, out;
   PCC_RETURN_IF_ERROR(out.Alloc(ctx, 1));
@@ -70,7 +80,14 @@ Status ComputeGraphProperties(Context* ctx, DevGraph* g) {
     PCC_RETURN_IF_ERROR(wout.ToHost(&ws, 1));
     PCC_RETURN_IF_ERROR(Sync(ctx));
   }
+  PCC_RETURN_IF_ERROR(AllocBins(ctx, g->n, &g->bins));
+  PCC_RETURN_IF_ERROR(BinVertices(ctx, g->n, g->off.p, PredAll{}, &g->bins, nullptr, nullptr));
+  uint32_t hc[kNumBins];
+  PCC_RETURN_IF_ERROR(g->bins.counts.ToHost(hc, kNumBins));
   PCC_RETURN_IF_ERROR(Sync(ctx));
+  for (int b = 0; b < kNumBins; ++b) g->bins.host_counts[b] = hc[b];
+  g->bins.size = g->n;
+  g->bins.edges = g->m;
   g->max_deg = maxd;
   g->integral = ws.nonint == 0;
   g->max_abs_w = ws.maxabs;

@@ -58,10 +58,23 @@ __global__ void SingletonsKernel(uint32_t n, const double* __restrict__ k, uint3
 // integral node weights, which is every weight the clusterers create).
 __global__ void AccumulateClustersKernel(uint32_t n, const uint32_t* __restrict__ C, const double* __restrict__ k,
                                          uint32_t* s, double* K) {
-  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
-    const uint32_t c = C[i];
-    atomicAdd(&s[c], 1u);
-    atomicAdd(&K[c], k[i]);
+  const uint64_t limit = (uint64_t(n) + 31) & ~uint64_t(31);
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < limit; i += uint64_t(gridDim.x) * blockDim.x) {
+    const bool in = i < n;
+    const uint32_t c = in ? C[i] : kNone;
+    const double x = in ? k[i] : 0.0;
+    const unsigned peers = __match_any_sync(kFull, c);
+    double tot = 0.0;
+    unsigned mm = peers;
+    while (mm) {
+      const int j = __ffs(mm) - 1;
+      tot += __shfl_sync(peers, x, j);
+      mm &= mm - 1;
+    }
+    if (in && int(LaneId()) == __ffs(peers) - 1) {
+      atomicAdd(&s[c], uint32_t(__popc(peers)));
+      atomicAdd(&K[c], tot);
+    }
   }
 }
 
@@ -99,77 +112,6 @@ __global__ void GatherKernel(uint32_t n, const uint32_t* __restrict__ idx, const
 }
 
 // ---------------------------------------------------------------------------
-// Degree binning of a vertex predicate over [0, n): count, starts, scatter.
-// ---------------------------------------------------------------------------
-struct PredAll {
-  __device__ bool operator()(uint32_t) const { return true; }
-};
-struct PredStamp {
-  const uint32_t* st;
-  uint32_t stamp;
-  __device__ bool operator()(uint32_t v) const { return st[v] == stamp; }
-};
-
-template <class P>
-__global__ void __launch_bounds__(kT) BinCountKernel(uint32_t n, const uint64_t* __restrict__ off, P pred,
-                                                     uint32_t* counts, DevCounters* ctr) {
-  __shared__ uint32_t sh[kNumBins];
-  __shared__ unsigned long long sh_deg;
-  if (threadIdx.x < kNumBins) sh[threadIdx.x] = 0;
-  if (threadIdx.x == 0) sh_deg = 0;
-  __syncthreads();
-  unsigned long long deg_acc = 0;
-  uint32_t cnt = 0;
-  for (uint64_t v = uint64_t(blockIdx.x) * kT + threadIdx.x; v < n; v += uint64_t(gridDim.x) * kT) {
-    if (!pred(static_cast<uint32_t>(v))) continue;
-    const uint64_t d = off[v + 1] - off[v];
-    atomicAdd(&sh[BinOf(d)], 1u);
-    deg_acc += d;
-    cnt++;
-  }
-  atomicAdd(&sh_deg, deg_acc);
-  __shared__ uint32_t sh_cnt;
-  if (threadIdx.x == 0) sh_cnt = 0;
-  __syncthreads();
-  atomicAdd(&sh_cnt, cnt);
-  __syncthreads();
-  if (threadIdx.x < kNumBins && sh[threadIdx.x]) atomicAdd(&counts[threadIdx.x], sh[threadIdx.x]);
-  if (threadIdx.x == 0) {
-    if (sh_deg) atomicAdd(&ctr->pend_edges, sh_deg);
-    if (sh_cnt) atomicAdd(&ctr->frontier, sh_cnt);
-  }
-}
-
-// counts[0..B) -> starts[0..B] and cursors zeroed.
-__global__ void BinStartsKernel(const uint32_t* counts, uint32_t* starts, uint32_t* cursor) {
-  uint32_t acc = 0;
-  for (int b = 0; b < kNumBins; ++b) {
-    starts[b] = acc;
-    acc += counts[b];
-    cursor[b] = 0;
-  }
-  starts[kNumBins] = acc;
-}
-
-template <class P>
-__global__ void __launch_bounds__(kT) BinScatterKernel(uint32_t n, const uint64_t* __restrict__ off, P pred,
-                                                       const uint32_t* __restrict__ starts, uint32_t* cursor,
-                                                       uint32_t* list) {
-  const uint64_t stride = uint64_t(gridDim.x) * kT;
-  const uint64_t limit = (uint64_t(n) + 31) & ~uint64_t(31);
-  for (uint64_t v = uint64_t(blockIdx.x) * kT + threadIdx.x; v < limit; v += stride) {
-    const bool in = v < n && pred(static_cast<uint32_t>(v));
-    const int bin = in ? BinOf(off[v + 1] - off[v]) : kNumBins + int(LaneId());
-    const unsigned peers = __match_any_sync(kFull, bin);
-    uint32_t base = 0;
-    const int leader = __ffs(peers) - 1;
-    if (in && int(LaneId()) == leader) base = atomicAdd(&cursor[bin], uint32_t(__popc(peers)));
-    base = __shfl_sync(kFull, base, leader);
-    if (in) list[starts[bin] + base + __popc(peers & LaneMaskLt())] = static_cast<uint32_t>(v);
-  }
-}
-
-// ---------------------------------------------------------------------------
 // Sync apply: MoveNodesToCluster.
 // ---------------------------------------------------------------------------
 struct ApplyArgs {
@@ -186,34 +128,63 @@ struct ApplyArgs {
   DevCounters* ctr;
 };
 
+// Sum of x over the lanes of `peers` (the caller's match group), in lane
+// order; every lane of the group gets the result.
+__device__ __forceinline__ double GroupSum(unsigned peers, double x) {
+  double tot = 0.0;
+  unsigned mm = peers;
+  while (mm) {
+    const int j = __ffs(mm) - 1;
+    tot += __shfl_sync(peers, x, j);
+    mm &= mm - 1;
+  }
+  return tot;
+}
+
 // Leave: every mover leaves its cluster (sizes and weights), marks it
-// modified; movers to a new cluster are flagged for ranking.
+// modified; movers to a new cluster are flagged for ranking.  Equal
+// clusters inside a warp are combined first (one atomic per cluster and
+// warp); the FP64 sums are exact because node weights are integral.
 __global__ void __launch_bounds__(kT) ApplyLeaveKernel(ApplyArgs a) {
   const uint32_t count = a.ctr->movers;
-  for (uint64_t i = uint64_t(blockIdx.x) * kT + threadIdx.x; i < count; i += uint64_t(gridDim.x) * kT) {
-    const uint32_t v = a.movers[i];
-    const uint32_t c = a.C[v];
-    atomicSub(&a.s[c], 1u);
-    atomicAdd(&a.K[c], -a.k[v]);
-    a.mod_stamp[c] = a.stamp;
-    if (a.moves[v] == a.n) {
-      a.new_stamp[v] = a.stamp;
-      atomicAdd(&a.ctr->new_movers, 1u);
+  const uint64_t limit = (uint64_t(count) + 31) & ~uint64_t(31);
+  for (uint64_t i = uint64_t(blockIdx.x) * kT + threadIdx.x; i < limit; i += uint64_t(gridDim.x) * kT) {
+    const bool in = i < count;
+    const uint32_t v = in ? a.movers[i] : 0u;
+    const uint32_t c = in ? a.C[v] : kNone;
+    const double kv = in ? a.k[v] : 0.0;
+    const unsigned peers = __match_any_sync(kFull, c);
+    const double tot = GroupSum(peers, kv);
+    if (in && int(LaneId()) == __ffs(peers) - 1) {
+      atomicSub(&a.s[c], uint32_t(__popc(peers)));
+      atomicAdd(&a.K[c], -tot);
+      a.mod_stamp[c] = a.stamp;
     }
+    const bool isnew = in && a.moves[v] == a.n;
+    if (isnew) a.new_stamp[v] = a.stamp;
+    const unsigned nb = __ballot_sync(kFull, isnew);
+    if (nb && LaneId() == 0) atomicAdd(&a.ctr->new_movers, uint32_t(__popc(nb)));
   }
 }
 
 // Join: movers to existing clusters enter them.
 __global__ void __launch_bounds__(kT) ApplyJoinKernel(ApplyArgs a) {
   const uint32_t count = a.ctr->movers;
-  for (uint64_t i = uint64_t(blockIdx.x) * kT + threadIdx.x; i < count; i += uint64_t(gridDim.x) * kT) {
-    const uint32_t v = a.movers[i];
-    const uint32_t t = a.moves[v];
-    if (t == a.n) continue;
-    atomicAdd(&a.s[t], 1u);
-    atomicAdd(&a.K[t], a.k[v]);
-    a.mod_stamp[t] = a.stamp;
-    a.C[v] = t;
+  const uint64_t limit = (uint64_t(count) + 31) & ~uint64_t(31);
+  for (uint64_t i = uint64_t(blockIdx.x) * kT + threadIdx.x; i < limit; i += uint64_t(gridDim.x) * kT) {
+    const uint32_t v = i < count ? a.movers[i] : 0u;
+    const uint32_t t = i < count ? a.moves[v] : a.n;
+    const bool in = i < count && t != a.n;
+    const uint32_t key = in ? t : kNone;
+    const double kv = in ? a.k[v] : 0.0;
+    const unsigned peers = __match_any_sync(kFull, key);
+    const double tot = GroupSum(peers, kv);
+    if (in && int(LaneId()) == __ffs(peers) - 1) {
+      atomicAdd(&a.s[t], uint32_t(__popc(peers)));
+      atomicAdd(&a.K[t], tot);
+      a.mod_stamp[t] = a.stamp;
+    }
+    if (in) a.C[v] = t;
   }
 }
 
@@ -246,18 +217,20 @@ __global__ void __launch_bounds__(kT) AssignNewKernel(ApplyArgs a, const uint32_
 }
 
 // Marked vertices for the next frontier.
-struct MarkClusterInput {  // NBHR_CLUSTER_MOVE: vertices of modified clusters
-  const uint32_t* C;
-  const uint32_t* mod_stamp;
-  uint32_t stamp;
-  __device__ uint32_t operator()(uint64_t v) const { return mod_stamp[C[v]] == stamp ? 1u : 0u; }
-};
 
 struct PushNeighbors {  // gbbs::edgeMap with an always-true functor
   const uint32_t* nbr;
   uint32_t* next_stamp;
   uint32_t stamp;
-  __device__ void operator()(uint32_t, uint64_t j) const { next_stamp[nbr[j]] = stamp; }
+  __device__ void operator()(uint32_t, uint64_t j, uint64_t) const { next_stamp[nbr[j]] = stamp; }
+};
+
+// Marked vertices of the next frontier.
+struct PredModifiedCluster {  // NBHR_CLUSTER_MOVE: vertices of modified clusters
+  const uint32_t* C;
+  const uint32_t* mod_stamp;
+  uint32_t stamp;
+  __device__ bool operator()(uint32_t v) const { return mod_stamp[C[v]] == stamp; }
 };
 
 // ---------------------------------------------------------------------------
@@ -268,11 +241,11 @@ struct ObjEdgeTerm {
   const float* w;
   const uint32_t* C;
   double offset;
-  double* acc;  // per-thread accumulators (indexed by global thread id)
-  __device__ void operator()(uint32_t u, uint64_t j) const {
+  double* acc;  // per-thread accumulators (indexed by the iteration slot)
+  __device__ void operator()(uint32_t u, uint64_t j, uint64_t slot) const {
     if (C[u] == C[nbr[j]]) {
       const double x = Dsub(static_cast<double>(w ? w[j] : 1.0f), offset) / 2;
-      acc[uint64_t(blockIdx.x) * blockDim.x + threadIdx.x] += x;
+      acc[slot] += x;
     }
   }
 };
@@ -293,15 +266,30 @@ struct SameLabelCount {
   const uint32_t* nbr;
   const uint32_t* L;
   unsigned long long* acc;
-  __device__ void operator()(uint32_t u, uint64_t j) const {
-    if (L[u] == L[nbr[j]]) atomicAdd(&acc[(uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) & 1023], 1ull);
+  __device__ void operator()(uint32_t u, uint64_t j, uint64_t slot) const {
+    if (L[u] == L[nbr[j]]) acc[slot] += 1ull;
   }
 };
 
+// deg[L[i]] += deg(i), one atomic per distinct label per warp.
 __global__ void DegreeSumKernel(uint32_t n, const uint64_t* __restrict__ off, const uint32_t* __restrict__ L,
                                 unsigned long long* deg) {
-  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
-    atomicAdd(&deg[L[i]], static_cast<unsigned long long>(off[i + 1] - off[i]));
+  const uint64_t limit = (uint64_t(n) + 31) & ~uint64_t(31);
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < limit; i += uint64_t(gridDim.x) * blockDim.x) {
+    const bool in = i < n;
+    const uint32_t lab = in ? L[i] : kNone;
+    unsigned long long d = in ? static_cast<unsigned long long>(off[i + 1] - off[i]) : 0ull;
+    const unsigned peers = __match_any_sync(kFull, lab);
+    // Sum over peers (any order: integers).
+    unsigned long long tot = 0;
+    unsigned mm = peers;
+    while (mm) {
+      const int j = __ffs(mm) - 1;
+      tot += __shfl_sync(peers, d, j);
+      mm &= mm - 1;
+    }
+    if (in && int(LaneId()) == __ffs(peers) - 1) atomicAdd(&deg[lab], tot);
+  }
 }
 
 struct ModTerm {
@@ -332,8 +320,6 @@ struct Level {
   std::unique_ptr<DevGraph> own;
   DBuf<uint32_t> C, s;
   DBuf<double> k, K;
-  BinSet all;
-  bool bins_ready = false;
   bool int_mode = false;
 };
 
@@ -346,6 +332,17 @@ struct RunResult {
   int32_t refine_passes = 0;
   uint64_t algo_bytes = 0;
 };
+
+// Global-hash scratch of the hub best-move kernel, allocated clean.
+Status AllocHubScratch(Context* ctx, uint64_t slots, DBuf<uint32_t>* keys, DBuf<unsigned long long>* vals,
+                       DBuf<uint32_t>* used) {
+  PCC_RETURN_IF_ERROR(keys->Alloc(ctx, slots));
+  PCC_RETURN_IF_ERROR(vals->Alloc(ctx, slots));
+  PCC_RETURN_IF_ERROR(used->Alloc(ctx, slots / 2 + 1));
+  PCC_RETURN_IF_ERROR(keys->Fill(0xFF));
+  PCC_RETURN_IF_ERROR(vals->Zero());
+  return Status::Ok();
+}
 
 bool IntModeFor(const DevGraph& g, double offset) {
   if (!g.integral) return false;
@@ -374,9 +371,8 @@ class Engine {
     PCC_RETURN_IF_ERROR(aux_stamp_.Zero());
     PCC_RETURN_IF_ERROR(zero_ids_.Alloc(ctx_, nn));
     PCC_RETURN_IF_ERROR(new_list_.Alloc(ctx_, nn));
-    PCC_RETURN_IF_ERROR(marked_.Alloc(ctx_, nn));
-    PCC_RETURN_IF_ERROR(dyn_.list.Alloc(ctx_, nn));
-    PCC_RETURN_IF_ERROR(dyn_.counts.Alloc(ctx_, 3 * kNumBins + 1));
+    PCC_RETURN_IF_ERROR(AllocBins(ctx_, n_max, &marked_bins_));
+    PCC_RETURN_IF_ERROR(AllocBins(ctx_, n_max, &dyn_));
     PCC_RETURN_IF_ERROR(ctr_.Alloc(ctx_, 1));
     PCC_RETURN_IF_ERROR(ctr_.Zero());
     PCC_RETURN_IF_ERROR(EnsureHubScratch(max_deg));
@@ -386,8 +382,7 @@ class Engine {
   Status EnsureHubScratch(uint32_t max_deg) {
     const uint64_t slots = GlobalHashSlots(ctx_, max_deg);
     if (slots > g_keys_.count) {
-      PCC_RETURN_IF_ERROR(g_keys_.Alloc(ctx_, slots));
-      PCC_RETURN_IF_ERROR(g_vals_.Alloc(ctx_, slots));
+      PCC_RETURN_IF_ERROR(AllocHubScratch(ctx_, slots, &g_keys_, &g_vals_, &g_used_));
       g_cap_ = uint32_t(slots / (uint64_t(ctx_->num_sms) * 2));
     }
     return Status::Ok();
@@ -428,43 +423,6 @@ class Engine {
     return Status::Ok();
   }
 
-  // Static bins of all vertices of a level (degrees only).
-  Status BuildAllBins(Level* L) {
-    if (L->bins_ready) return Status::Ok();
-    const uint32_t n = L->g->n;
-    BinSet& b = L->all;
-    PCC_RETURN_IF_ERROR(b.list.Alloc(ctx_, std::max<uint64_t>(n, 1)));
-    PCC_RETURN_IF_ERROR(b.counts.Alloc(ctx_, 3 * kNumBins + 1));
-    PCC_RETURN_IF_ERROR(b.counts.Zero());
-    PCC_RETURN_IF_ERROR(BinWith(L->g, PredAll{}, &b));
-    uint32_t host[3 * kNumBins + 1];
-    PCC_RETURN_IF_ERROR(b.counts.ToHost(host, 3 * kNumBins + 1));
-    PCC_RETURN_IF_ERROR(Sync(ctx_));
-    for (int i = 0; i < kNumBins; ++i) b.host_counts[i] = host[i];
-    b.size = n;
-    b.edges = L->g->m;
-    L->bins_ready = true;
-    return Status::Ok();
-  }
-
-  template <class P>
-  Status BinWith(const DevGraph* g, P pred, BinSet* b) {
-    const uint32_t n = g->n;
-    uint32_t* counts = b->counts.p;
-    uint32_t* starts = counts + kNumBins;
-    uint32_t* cursor = starts + kNumBins + 1;
-    PCC_CUDA(cudaMemsetAsync(counts, 0, sizeof(uint32_t) * kNumBins, ctx_->stream));
-    if (n) {
-      BinCountKernel<P><<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g->off.p, pred, counts, ctr_.p); PCC_COUNT(1);
-    }
-    BinStartsKernel<<<1, 1, 0, ctx_->stream>>>(counts, starts, cursor); PCC_COUNT(1);
-    if (n) {
-      BinScatterKernel<P><<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g->off.p, pred, starts, cursor,
-                                                                      b->list.p); PCC_COUNT(1);
-    }
-    return LaunchCheck();
-  }
-
   // One best-move round over `front` (host_counts known).  Builds the next
   // frontier in dyn_ unless ALL_MOVE.  Returns whether the next frontier is
   // non-empty (local_moved).
@@ -499,7 +457,8 @@ class Engine {
     a.movers = movers_.p;
     a.ctr = ctr_.p;
     a.g_keys = g_keys_.p;
-    a.g_vals = reinterpret_cast<unsigned long long*>(g_vals_.p);
+    a.g_vals = g_vals_.p;
+    a.g_used = g_used_.p;
     a.g_cap = g_cap_;
     a.async = cfg_.async ? 1 : 0;
     a.s_mut = L->s.p;
@@ -512,6 +471,7 @@ class Engine {
                                         L->int_mode, g.max_deg));
     timer_.End(kPhaseBestMoves);
 
+    timer_.Begin(kPhaseApply);
     if (!cfg_.async) {
       ApplyArgs ap{n, L->C.p, L->s.p, L->k.p, L->K.p, moves_.p, movers_.p, mod_stamp_.p, new_stamp_.p, stamp_,
                    ctr_.p};
@@ -527,6 +487,7 @@ class Engine {
       AssignNewKernel<<<grid, kT, 0, ctx_->stream>>>(ap, zero_ids_.p, new_list_.p); PCC_COUNT(1);
       PCC_RETURN_IF_ERROR(LaunchCheck());
     }
+    timer_.End(kPhaseApply);
 
     if (cfg_.move_method == PCC_ALL_MOVE) {
       DevCounters hc;
@@ -536,18 +497,22 @@ class Engine {
       *next_nonempty = n > 0;
       return Status::Ok();
     }
-    // Marked set, then its neighbourhood (edgeMap), then binning.
+    // Marked set (binned by degree), then its neighbourhood (edgeMap), then
+    // the degree-binned next frontier.
+    timer_.Begin(kPhaseFrontier);
     if (cfg_.move_method == PCC_NBHR_CLUSTER_MOVE) {
-      PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, MarkClusterInput{L->C.p, mod_stamp_.p, stamp_},
-                                              StoreIndexIfSet{marked_.p}, scan_tiles_, &ctr_.p->marked));
+      PCC_RETURN_IF_ERROR(BinVertices(ctx_, n, g.off.p, PredModifiedCluster{L->C.p, mod_stamp_.p, stamp_},
+                                      &marked_bins_, nullptr, &ctr_.p->marked));
     } else {
-      PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, StampInput{moved_stamp_.p, stamp_},
-                                              StoreIndexIfSet{marked_.p}, scan_tiles_, &ctr_.p->marked));
+      PCC_RETURN_IF_ERROR(BinVertices(ctx_, n, g.off.p, PredStamp{moved_stamp_.p, stamp_}, &marked_bins_, nullptr,
+                                      &ctr_.p->marked));
     }
-    ForEachListEntryKernel<<<GridFor(ctx_, n, kT), kT, 0, ctx_->stream>>>(
-        marked_.p, &ctr_.p->marked, g.off.p, PushNeighbors{g.nbr.p, next_stamp_.p, stamp_}); PCC_COUNT(1);
+    LaunchEdgeIter(ctx_, marked_bins_.list.p, marked_bins_.counts.p, marked_bins_.counts.p + kNumBins, nullptr,
+                   g.off.p, PushNeighbors{g.nbr.p, next_stamp_.p, stamp_});
     PCC_RETURN_IF_ERROR(LaunchCheck());
-    PCC_RETURN_IF_ERROR(BinWith(&g, PredStamp{next_stamp_.p, stamp_}, &dyn_));
+    PCC_RETURN_IF_ERROR(BinVertices(ctx_, n, g.off.p, PredStamp{next_stamp_.p, stamp_}, &dyn_,
+                                    &ctr_.p->pend_edges, &ctr_.p->frontier));
+    timer_.End(kPhaseFrontier);
     DevCounters hc;
     PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
     uint32_t hcounts[kNumBins];
@@ -563,12 +528,11 @@ class Engine {
 
   // IterateBestMoves (parallel-correlation-clusterer.cc:340-365).
   Status IterateBestMoves(Level* L, int64_t num_inner, bool* moved_out) {
-    PCC_RETURN_IF_ERROR(BuildAllBins(L));
     bool moved = false;
     bool local_moved = true;
     bool use_static = true;
     for (int64_t it = 0; it < num_inner && local_moved; ++it) {
-      const BinSet& front = use_static ? L->all : dyn_;
+      const BinSet& front = use_static ? L->g->bins : dyn_;
       bool next = false;
       PCC_RETURN_IF_ERROR(Round(L, front, front.host_counts, front.edges, front.size, &next));
       local_moved = next;
@@ -706,9 +670,10 @@ class Engine {
   uint32_t n_max_ = 0;
   uint32_t stamp_ = 0;
   DBuf<uint32_t> moves_, movers_, moved_stamp_, mod_stamp_, next_stamp_, new_stamp_, aux_stamp_;
-  DBuf<uint32_t> zero_ids_, new_list_, marked_;
+  DBuf<uint32_t> zero_ids_, new_list_;
+  BinSet marked_bins_;
   DBuf<uint32_t> scan_tiles_;
-  DBuf<uint32_t> g_keys_;
+  DBuf<uint32_t> g_keys_, g_used_;
   DBuf<unsigned long long> g_vals_;
   uint32_t g_cap_ = 0;
   BinSet dyn_;
@@ -738,14 +703,15 @@ Status ComputeObjectiveDevice(Context* ctx, const DevGraph& g, const uint32_t* L
   PCC_RETURN_IF_ERROR(s.Zero());
   PCC_RETURN_IF_ERROR(K.Zero());
   AccumulateClustersKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, L, k.p, s.p, K.p); PCC_COUNT(1);
-  const unsigned grid = GridFor(ctx, n, kT);
+  const uint64_t slots = EdgeIterSlots(ctx);
   DBuf<double> acc;
-  PCC_RETURN_IF_ERROR(acc.Alloc(ctx, uint64_t(grid) * kT));
+  PCC_RETURN_IF_ERROR(acc.Alloc(ctx, slots));
   PCC_RETURN_IF_ERROR(acc.Zero());
-  ForEachEntryKernel<<<grid, kT, 0, ctx->stream>>>(n, g.off.p, ObjEdgeTerm{g.nbr.p, g.wp(), L, offset, acc.p}); PCC_COUNT(1);
+  LaunchEdgeIter(ctx, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins, g.bins.host_counts, g.off.p,
+                 ObjEdgeTerm{g.nbr.p, g.wp(), L, offset, acc.p});
   DBuf<double> part, sums;
   PCC_RETURN_IF_ERROR(sums.Alloc(ctx, 2));
-  PCC_RETURN_IF_ERROR(Reduce<double>(ctx, uint64_t(grid) * kT, ArrayInputF64{acc.p}, OpAdd{}, 0.0, sums.p, part));
+  PCC_RETURN_IF_ERROR(Reduce<double>(ctx, slots, ArrayInputF64{acc.p}, OpAdd{}, 0.0, sums.p, part));
   PCC_RETURN_IF_ERROR(Reduce<double>(ctx, n, ResTerm{L, k.p, K.p}, OpAdd{}, 0.0, sums.p + 1, part));
   double h[2];
   PCC_RETURN_IF_ERROR(sums.ToHost(h, 2));
@@ -763,15 +729,17 @@ Status ComputeModularityDevice(Context* ctx, const DevGraph& g, const uint32_t* 
     return Status::Ok();
   }
   DBuf<unsigned long long> cnt, deg;
-  PCC_RETURN_IF_ERROR(cnt.Alloc(ctx, 1024));
+  const uint64_t slots = EdgeIterSlots(ctx);
+  PCC_RETURN_IF_ERROR(cnt.Alloc(ctx, slots));
   PCC_RETURN_IF_ERROR(cnt.Zero());
   PCC_RETURN_IF_ERROR(deg.Alloc(ctx, n));
   PCC_RETURN_IF_ERROR(deg.Zero());
-  ForEachEntryKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, g.off.p, SameLabelCount{g.nbr.p, L, cnt.p}); PCC_COUNT(1);
+  LaunchEdgeIter(ctx, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins, g.bins.host_counts, g.off.p,
+                 SameLabelCount{g.nbr.p, L, cnt.p});
   DegreeSumKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, g.off.p, L, deg.p); PCC_COUNT(1);
   DBuf<unsigned long long> part64, tot64;
   PCC_RETURN_IF_ERROR(tot64.Alloc(ctx, 1));
-  PCC_RETURN_IF_ERROR(Reduce<unsigned long long>(ctx, 1024, U64Input{cnt.p}, OpAdd{}, 0ull, tot64.p, part64));
+  PCC_RETURN_IF_ERROR(Reduce<unsigned long long>(ctx, slots, U64Input{cnt.p}, OpAdd{}, 0ull, tot64.p, part64));
   const double total = static_cast<double>(g.m);
   DBuf<double> part, sum;
   PCC_RETURN_IF_ERROR(sum.Alloc(ctx, 1));
@@ -886,6 +854,8 @@ Status ClusterImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config* 
     stats->ms_total = ms;
     stats->ms_best_moves = eng.PhaseMs(kPhaseBestMoves);
     stats->ms_compress = eng.PhaseMs(kPhaseCompress);
+    stats->ms_apply = eng.PhaseMs(kPhaseApply);
+    stats->ms_frontier = eng.PhaseMs(kPhaseFrontier);
     stats->kernel_launches = LaunchCounter().load() - launches0;
     stats->algo_bytes_best_moves = eng.result().algo_bytes;
   }
@@ -1009,26 +979,10 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   DBuf<DevCounters> ctr;
   PCC_RETURN_IF_ERROR(ctr.Alloc(ctx, 1));
   PCC_RETURN_IF_ERROR(ctr.Zero());
-  BinSet b;
-  PCC_RETURN_IF_ERROR(b.list.Alloc(ctx, nn));
-  PCC_RETURN_IF_ERROR(b.counts.Alloc(ctx, 3 * kNumBins + 1));
-  {
-    uint32_t* counts = b.counts.p;
-    PCC_CUDA(cudaMemsetAsync(counts, 0, sizeof(uint32_t) * kNumBins, ctx->stream));
-    if (n) BinCountKernel<PredAll><<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, g.off.p, PredAll{}, counts, ctr.p); PCC_COUNT(1);
-    BinStartsKernel<<<1, 1, 0, ctx->stream>>>(counts, counts + kNumBins, counts + 2 * kNumBins + 1); PCC_COUNT(1);
-    if (n)
-      BinScatterKernel<PredAll><<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, g.off.p, PredAll{}, counts + kNumBins,
-                                                                         counts + 2 * kNumBins + 1, b.list.p); PCC_COUNT(1);
-    PCC_RETURN_IF_ERROR(LaunchCheck());
-  }
-  DBuf<uint32_t> gk;
+  DBuf<uint32_t> gk, gu;
   DBuf<unsigned long long> gv;
   const uint64_t slots = GlobalHashSlots(ctx, g.max_deg);
-  if (slots) {
-    PCC_RETURN_IF_ERROR(gk.Alloc(ctx, slots));
-    PCC_RETURN_IF_ERROR(gv.Alloc(ctx, slots));
-  }
+  if (slots) PCC_RETURN_IF_ERROR(AllocHubScratch(ctx, slots, &gk, &gv, &gu));
   BMArgs a{};
   a.n = n;
   a.off = g.off.p;
@@ -1051,10 +1005,11 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   a.out_moves = dm.p;
   a.g_keys = gk.p;
   a.g_vals = gv.p;
+  a.g_used = gu.p;
   a.g_cap = slots ? uint32_t(slots / (uint64_t(ctx->num_sms) * 2)) : 0;
   a.async = 0;
-  PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx, a, b.list.p, b.counts.p, b.counts.p + kNumBins, nullptr,
-                                      IntModeFor(g, config->edge_weight_offset), g.max_deg));
+  PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx, a, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins,
+                                      g.bins.host_counts, IntModeFor(g, config->edge_weight_offset), g.max_deg));
   PCC_RETURN_IF_ERROR(dt.ToHost(out_t, n));
   PCC_RETURN_IF_ERROR(dv.ToHost(out_v, n));
   if (out_moves) PCC_RETURN_IF_ERROR(dm.ToHost(out_moves, n));

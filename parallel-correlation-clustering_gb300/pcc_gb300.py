@@ -83,6 +83,8 @@ class PccStats(ctypes.Structure):
         ("ms_total", ctypes.c_double),
         ("ms_best_moves", ctypes.c_double),
         ("ms_compress", ctypes.c_double),
+        ("ms_apply", ctypes.c_double),
+        ("ms_frontier", ctypes.c_double),
         ("kernel_launches", ctypes.c_uint64),
         ("algo_bytes_best_moves", ctypes.c_uint64),
     ]
