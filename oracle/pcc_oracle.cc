@@ -178,7 +178,9 @@ struct SumTable {
     mask = static_cast<uint32_t>(cap - 1);
   }
   void Add(uint32_t key, double v) {
-    uint32_t h = (key * 2654435761u) & mask;
+    // Fibonacci hashing on the high bits of the product (like absl's
+    // flat_hash_map, it mixes all key bits into the slot index).
+    uint32_t h = static_cast<uint32_t>((uint64_t(key) * 0x9E3779B97F4A7C15ull) >> 32) & mask;
     while (true) {
       if (keys[h] == key) {
         vals[h] += v;

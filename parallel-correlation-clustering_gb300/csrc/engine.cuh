@@ -46,6 +46,8 @@ __host__ __device__ inline int BinOf(uint64_t d) {
   return kBinGlobal;
 }
 
+struct BatchPlan;
+
 // Degree-binned vertex list: bins are contiguous segments of `list`.
 struct BinSet {
   DBuf<uint32_t> list;       // n entries
@@ -53,7 +55,10 @@ struct BinSet {
   uint64_t edges = 0;        // sum of degrees (host copy, static bins only)
   uint32_t size = 0;         // vertices (host copy, static bins only)
   uint32_t host_counts[kNumBins] = {0};
+  mutable std::shared_ptr<BatchPlan> batch_plan;  // built on first use
 };
+
+struct HubPlan;
 
 // ---------------------------------------------------------------------------
 // Graph resident in HBM.
@@ -65,7 +70,9 @@ struct DevGraph {
   DBuf<uint32_t> nbr;
   DBuf<float> w;          // empty => unit weights
   DBuf<double> node_w;    // node weights attached by compression
-  BinSet bins;            // static degree bins of all vertices
+  BinSet bins;            // static degree bins of the vertices with degree > 0
+  mutable BinSet bins_all;  // all vertices (built on first use)
+  mutable std::shared_ptr<HubPlan> hub_plan;  // degree > 1000 (built on first use)
   uint32_t max_deg = 0;
   bool integral = true;   // every weight is an integer value
   double max_abs_w = 1.0; // max |w| (1 for unit weights)
@@ -75,6 +82,8 @@ struct DevGraph {
 // Computes max degree / weight properties and the static degree bins on
 // the device (one sync).
 Status ComputeGraphProperties(Context* ctx, DevGraph* g);
+// Builds g->bins_all (degree bins including isolated vertices) if absent.
+Status EnsureAllBins(Context* ctx, const DevGraph* g);
 
 // Device counters of one call (all in one allocation).
 struct DevCounters {
@@ -109,10 +118,15 @@ struct BMArgs {
   const uint32_t* s;
   const double* k;
   const double* K;
+  const float* Kf;          // fl32(K), current for the sync round (filter input)
   double res;
+  float res32;
   double offset;
   int32_t ioffset;          // integer offset (INT mode)
   uint32_t stamp;
+  // frontier: vertices v with front_stamp[v] == front_val (all when null)
+  const uint32_t* front_stamp;
+  uint32_t front_val;
   // sync outputs
   uint32_t* moves;          // decided target per vertex (read for movers)
   uint32_t* moved_stamp;    // moved_vertex: = stamp when value > 0
@@ -122,11 +136,6 @@ struct BMArgs {
   uint32_t* out_target;
   double* out_value;
   uint32_t* out_moves;
-  // global-hash scratch for the hub bin
-  uint32_t* g_keys;         // clean (kNone) between vertices
-  unsigned long long* g_vals;  // clean (0) between vertices
-  uint32_t* g_used;         // per-CTA occupied-slot lists (g_cap / 2 each)
-  uint32_t g_cap;           // slots per CTA
   // async mode: apply moves immediately with atomics
   int async;
   uint32_t* s_mut;
@@ -135,15 +144,17 @@ struct BMArgs {
   uint32_t* moved_cluster_stamp;
 };
 
-// Launches every best-move kernel over `bins` (counts read on the device).
+// Launches the best-move kernels of the bins up to degree 1000 over `bins`
+// (counts read on the device); hubs go through LaunchHubBestMoves.
 // int_mode selects exact integer accumulation (all weights and the offset
 // integral and small) over FP64 accumulation in adjacency order.
 Status LaunchBestMoves(Context* ctx, const BMArgs& a, const uint32_t* list, const uint32_t* bin_counts,
                        const uint32_t* bin_starts, const uint32_t* host_counts, bool int_mode,
                        uint32_t max_deg);
 
-// Bytes of global scratch the hub bin needs for a graph of this max degree.
-uint64_t GlobalHashSlots(Context* ctx, uint32_t max_deg);
+// The hub plan of a graph / the batch plan of a bin set (built on first use).
+Status EnsureHubPlan(Context* ctx, const DevGraph* g);
+Status EnsureBatchPlan(Context* ctx, const DevGraph* g, const BinSet* bins);
 
 }  // namespace pcc
 

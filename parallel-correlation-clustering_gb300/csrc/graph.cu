@@ -6,6 +6,8 @@
 #include <cmath>
 
 #include "graphops.cuh"
+#include "hubs.cuh"
+#include "batch.cuh"
 
 namespace pcc {
 
@@ -51,7 +53,59 @@ __global__ void CheckCsrKernel(uint32_t n, uint64_t m, const uint64_t* __restric
     if (nbr[j] >= n) atomicExch(bad, 4);
 }
 
+struct PredNonZeroDegree {
+  const uint64_t* off;
+  __device__ bool operator()(uint32_t v) const { return off[v + 1] > off[v]; }
+};
+
+Status BuildBins(Context* ctx, const DevGraph* g, BinSet* b, bool include_isolated) {
+  PCC_RETURN_IF_ERROR(AllocBins(ctx, g->n, b));
+  DBuf<unsigned long long> sum;
+  DBuf<uint32_t> cnt;
+  PCC_RETURN_IF_ERROR(sum.Alloc(ctx, 1));
+  PCC_RETURN_IF_ERROR(cnt.Alloc(ctx, 1));
+  PCC_RETURN_IF_ERROR(sum.Zero());
+  PCC_RETURN_IF_ERROR(cnt.Zero());
+  if (include_isolated) {
+    PCC_RETURN_IF_ERROR(BinVertices(ctx, g->n, g->off.p, PredAll{}, b, sum.p, cnt.p));
+  } else {
+    PCC_RETURN_IF_ERROR(BinVertices(ctx, g->n, g->off.p, PredNonZeroDegree{g->off.p}, b, sum.p, cnt.p));
+  }
+  uint32_t hc[kNumBins];
+  uint32_t hcnt = 0;
+  unsigned long long hsum = 0;
+  PCC_RETURN_IF_ERROR(b->counts.ToHost(hc, kNumBins));
+  PCC_RETURN_IF_ERROR(cnt.ToHost(&hcnt, 1));
+  PCC_RETURN_IF_ERROR(sum.ToHost(&hsum, 1));
+  PCC_RETURN_IF_ERROR(Sync(ctx));
+  for (int i = 0; i < kNumBins; ++i) b->host_counts[i] = hc[i];
+  b->size = hcnt;
+  b->edges = hsum;
+  return Status::Ok();
+}
+
 }  // namespace
+
+Status EnsureHubPlan(Context* ctx, const DevGraph* g) {
+  if (g->hub_plan) return Status::Ok();
+  auto plan = std::make_shared<HubPlan>();
+  PCC_RETURN_IF_ERROR(BuildHubPlan(ctx, *g, g->bins, plan.get()));
+  g->hub_plan = std::move(plan);
+  return Status::Ok();
+}
+
+Status EnsureBatchPlan(Context* ctx, const DevGraph* g, const BinSet* bins) {
+  if (bins->batch_plan) return Status::Ok();
+  auto plan = std::make_shared<BatchPlan>();
+  PCC_RETURN_IF_ERROR(BuildBatchPlan(ctx, *g, *bins, plan.get()));
+  bins->batch_plan = std::move(plan);
+  return Status::Ok();
+}
+
+Status EnsureAllBins(Context* ctx, const DevGraph* g) {
+  if (g->bins_all.list.p) return Status::Ok();
+  return BuildBins(ctx, g, &g->bins_all, true);
+}
 
 __global__ void BinStartsKernel(const uint32_t* counts, uint32_t* starts, uint32_t* cursor) {
   uint32_t acc = 0;
@@ -80,14 +134,7 @@ Status ComputeGraphProperties(Context* ctx, DevGraph* g) {
     PCC_RETURN_IF_ERROR(wout.ToHost(&ws, 1));
     PCC_RETURN_IF_ERROR(Sync(ctx));
   }
-  PCC_RETURN_IF_ERROR(AllocBins(ctx, g->n, &g->bins));
-  PCC_RETURN_IF_ERROR(BinVertices(ctx, g->n, g->off.p, PredAll{}, &g->bins, nullptr, nullptr));
-  uint32_t hc[kNumBins];
-  PCC_RETURN_IF_ERROR(g->bins.counts.ToHost(hc, kNumBins));
-  PCC_RETURN_IF_ERROR(Sync(ctx));
-  for (int b = 0; b < kNumBins; ++b) g->bins.host_counts[b] = hc[b];
-  g->bins.size = g->n;
-  g->bins.edges = g->m;
+  PCC_RETURN_IF_ERROR(BuildBins(ctx, g, &g->bins, false));
   g->max_deg = maxd;
   g->integral = ws.nonint == 0;
   g->max_abs_w = ws.maxabs;

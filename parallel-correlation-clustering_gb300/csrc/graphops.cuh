@@ -28,11 +28,15 @@ inline uint64_t EdgeIterSlots(const Context* ctx) {
          uint64_t(IterBigGrid(ctx)) * kIterBigThreads;
 }
 
-template <class F>
+struct RowAll {
+  __device__ bool operator()(uint32_t) const { return true; }
+};
+
+template <class F, class R>
 __global__ void __launch_bounds__(kIterThreads) EdgeIterSmallKernel(const uint32_t* __restrict__ list,
                                                                    const uint32_t* __restrict__ counts,
                                                                    const uint32_t* __restrict__ starts,
-                                                                   const uint64_t* __restrict__ off, F f) {
+                                                                   const uint64_t* __restrict__ off, F f, R row) {
   __shared__ uint32_t incl[kIterThreads / 32][32];
   __shared__ uint64_t begin[kIterThreads / 32][32];
   __shared__ uint32_t vert[kIterThreads / 32][32];
@@ -47,8 +51,10 @@ __global__ void __launch_bounds__(kIterThreads) EdgeIterSmallKernel(const uint32
     uint64_t b = 0;
     if (i < count) {
       v = list[s0 + i];
-      b = off[v];
-      d = static_cast<uint32_t>(off[v + 1] - b);
+      if (row(v)) {
+        b = off[v];
+        d = static_cast<uint32_t>(off[v + 1] - b);
+      }
     }
     const uint32_t inc = WarpInclusiveScan<uint32_t>(d);
     incl[warp][lane] = inc;
@@ -70,12 +76,12 @@ __global__ void __launch_bounds__(kIterThreads) EdgeIterSmallKernel(const uint32
   (void)counts;
 }
 
-template <class F>
+template <class F, class R>
 __global__ void __launch_bounds__(kIterThreads) EdgeIterMidKernel(const uint32_t* __restrict__ list,
                                                                  const uint32_t* __restrict__ counts,
                                                                  const uint32_t* __restrict__ starts,
                                                                  const uint64_t* __restrict__ off, F f,
-                                                                 uint64_t slot_base) {
+                                                                 uint64_t slot_base, R row) {
   const uint32_t s0 = starts[kBinW128];
   const uint32_t count = starts[kBinCta] - s0;  // bins W128..W1000
   const unsigned lane = LaneId(), warp = threadIdx.x >> 5;
@@ -83,6 +89,7 @@ __global__ void __launch_bounds__(kIterThreads) EdgeIterMidKernel(const uint32_t
   for (uint64_t i = uint64_t(blockIdx.x) * (kIterThreads / 32) + warp; i < count;
        i += uint64_t(gridDim.x) * (kIterThreads / 32)) {
     const uint32_t v = list[s0 + i];
+    if (!row(v)) continue;
     const uint64_t b = off[v], e = off[v + 1];
     for (uint64_t j = b + lane; j < e; j += 128) {
 #pragma unroll
@@ -93,17 +100,18 @@ __global__ void __launch_bounds__(kIterThreads) EdgeIterMidKernel(const uint32_t
   (void)counts;
 }
 
-template <class F>
+template <class F, class R>
 __global__ void __launch_bounds__(kIterBigThreads) EdgeIterBigKernel(const uint32_t* __restrict__ list,
                                                                     const uint32_t* __restrict__ counts,
                                                                     const uint32_t* __restrict__ starts,
                                                                     const uint64_t* __restrict__ off, F f,
-                                                                    uint64_t slot_base) {
+                                                                    uint64_t slot_base, R row) {
   const uint32_t s0 = starts[kBinCta];
   const uint32_t count = starts[kNumBins] - s0;  // bins Cta, Global
   const uint64_t slot = slot_base + uint64_t(blockIdx.x) * kIterBigThreads + threadIdx.x;
   for (uint64_t i = blockIdx.x; i < count; i += gridDim.x) {
     const uint32_t v = list[s0 + i];
+    if (!row(v)) continue;
     const uint64_t b = off[v], e = off[v + 1];
     for (uint64_t j = b + threadIdx.x; j < e; j += 4 * kIterBigThreads) {
 #pragma unroll
@@ -114,11 +122,12 @@ __global__ void __launch_bounds__(kIterBigThreads) EdgeIterBigKernel(const uint3
   (void)counts;
 }
 
-// Launches the three shapes over a BinSet-layout list (starts on device).
-// host_counts (per bin) may be null; then every shape is launched.
-template <class F>
+// Launches the three shapes over a BinSet-layout list (starts on device);
+// rows failing `row` are skipped.  host_counts (per bin) may be null; then
+// every shape is launched.
+template <class F, class R = RowAll>
 inline void LaunchEdgeIter(Context* ctx, const uint32_t* list, const uint32_t* counts, const uint32_t* starts,
-                           const uint32_t* host_counts, const uint64_t* off, F f) {
+                           const uint32_t* host_counts, const uint64_t* off, F f, R row = R()) {
   auto any = [&](int b0, int b1) {
     if (!host_counts) return true;
     for (int b = b0; b < b1; ++b)
@@ -127,17 +136,18 @@ inline void LaunchEdgeIter(Context* ctx, const uint32_t* list, const uint32_t* c
   };
   cudaStream_t st = ctx->stream;
   if (any(kBinG4, kBinW128)) {
-    EdgeIterSmallKernel<F><<<IterSmallGrid(ctx), kIterThreads, 0, st>>>(list, counts, starts, off, f);
+    EdgeIterSmallKernel<F, R><<<IterSmallGrid(ctx), kIterThreads, 0, st>>>(list, counts, starts, off, f, row);
     PCC_COUNT(1);
   }
   const uint64_t base_mid = uint64_t(IterSmallGrid(ctx)) * kIterThreads;
   if (any(kBinW128, kBinCta)) {
-    EdgeIterMidKernel<F><<<IterMidGrid(ctx), kIterThreads, 0, st>>>(list, counts, starts, off, f, base_mid);
+    EdgeIterMidKernel<F, R><<<IterMidGrid(ctx), kIterThreads, 0, st>>>(list, counts, starts, off, f, base_mid, row);
     PCC_COUNT(1);
   }
   const uint64_t base_big = base_mid + uint64_t(IterMidGrid(ctx)) * kIterThreads;
   if (any(kBinCta, kNumBins)) {
-    EdgeIterBigKernel<F><<<IterBigGrid(ctx), kIterBigThreads, 0, st>>>(list, counts, starts, off, f, base_big);
+    EdgeIterBigKernel<F, R><<<IterBigGrid(ctx), kIterBigThreads, 0, st>>>(list, counts, starts, off, f, base_big,
+                                                                          row);
     PCC_COUNT(1);
   }
 }
@@ -192,6 +202,40 @@ __global__ void __launch_bounds__(256) BinCountKernel(uint32_t n, const uint64_t
   if (threadIdx.x == 0) {
     if (deg_sum && sh_deg) atomicAdd(deg_sum, sh_deg);
     if (vcount && sh_cnt) atomicAdd(vcount, sh_cnt);
+  }
+}
+
+// Number and degree sum of the vertices satisfying pred (one pass over n).
+template <class P>
+__global__ void __launch_bounds__(256) CountDegreesKernel(uint32_t n, const uint64_t* __restrict__ off, P pred,
+                                                          unsigned long long* deg_sum, uint32_t* vcount) {
+  unsigned long long dacc = 0;
+  uint32_t cnt = 0;
+  for (uint64_t v = uint64_t(blockIdx.x) * 256 + threadIdx.x; v < n; v += uint64_t(gridDim.x) * 256) {
+    if (!pred(static_cast<uint32_t>(v))) continue;
+    dacc += off[v + 1] - off[v];
+    cnt++;
+  }
+  for (int o = 16; o >= 1; o >>= 1) {
+    dacc += __shfl_xor_sync(kFull, dacc, o);
+    cnt += __shfl_xor_sync(kFull, cnt, o);
+  }
+  __shared__ unsigned long long sd[8];
+  __shared__ uint32_t sc[8];
+  if (LaneId() == 0) {
+    sd[threadIdx.x >> 5] = dacc;
+    sc[threadIdx.x >> 5] = cnt;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    uint32_t c = 0;
+    for (int w = 0; w < 8; ++w) {
+      t += sd[w];
+      c += sc[w];
+    }
+    if (t) atomicAdd(deg_sum, t);
+    if (c) atomicAdd(vcount, c);
   }
 }
 

@@ -18,6 +18,8 @@
 #include <vector>
 
 #include "graphops.cuh"
+#include "hubs.cuh"
+#include "batch.cuh"
 
 namespace pcc {
 
@@ -76,6 +78,15 @@ __global__ void AccumulateClustersKernel(uint32_t n, const uint32_t* __restrict_
       atomicAdd(&K[c], tot);
     }
   }
+}
+
+// Kf[c] = fl32(K[c]) for every c (stamp == 0) or for the clusters modified
+// in the round `stamp` (the FP32 pre-filter of the best-move kernels needs
+// Kf == fl32(K) exactly).
+__global__ void RefreshKfKernel(uint32_t n, const double* __restrict__ K, float* Kf,
+                                const uint32_t* __restrict__ mod_stamp, uint32_t stamp) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    if (stamp == 0 || mod_stamp[i] == stamp) Kf[i] = static_cast<float>(K[i]);
 }
 
 // cluster_ids[i] = C[cluster_ids[i]] (FlattenClustering).
@@ -320,6 +331,12 @@ struct Level {
   std::unique_ptr<DevGraph> own;
   DBuf<uint32_t> C, s;
   DBuf<double> k, K;
+  DBuf<float> Kf;  // fl32(K)
+  // Vertices the best-move kernels visit: the degree > 0 bins, or all
+  // vertices when isolated ones may sit in shared clusters (level 0 started
+  // from given labels).  From singletons an isolated vertex never moves:
+  // its value is 0 and no vertex can join it.
+  const BinSet* bins = nullptr;
   bool int_mode = false;
 };
 
@@ -332,17 +349,6 @@ struct RunResult {
   int32_t refine_passes = 0;
   uint64_t algo_bytes = 0;
 };
-
-// Global-hash scratch of the hub best-move kernel, allocated clean.
-Status AllocHubScratch(Context* ctx, uint64_t slots, DBuf<uint32_t>* keys, DBuf<unsigned long long>* vals,
-                       DBuf<uint32_t>* used) {
-  PCC_RETURN_IF_ERROR(keys->Alloc(ctx, slots));
-  PCC_RETURN_IF_ERROR(vals->Alloc(ctx, slots));
-  PCC_RETURN_IF_ERROR(used->Alloc(ctx, slots / 2 + 1));
-  PCC_RETURN_IF_ERROR(keys->Fill(0xFF));
-  PCC_RETURN_IF_ERROR(vals->Zero());
-  return Status::Ok();
-}
 
 bool IntModeFor(const DevGraph& g, double offset) {
   if (!g.integral) return false;
@@ -371,20 +377,10 @@ class Engine {
     PCC_RETURN_IF_ERROR(aux_stamp_.Zero());
     PCC_RETURN_IF_ERROR(zero_ids_.Alloc(ctx_, nn));
     PCC_RETURN_IF_ERROR(new_list_.Alloc(ctx_, nn));
-    PCC_RETURN_IF_ERROR(AllocBins(ctx_, n_max, &marked_bins_));
-    PCC_RETURN_IF_ERROR(AllocBins(ctx_, n_max, &dyn_));
+
     PCC_RETURN_IF_ERROR(ctr_.Alloc(ctx_, 1));
     PCC_RETURN_IF_ERROR(ctr_.Zero());
-    PCC_RETURN_IF_ERROR(EnsureHubScratch(max_deg));
-    return Status::Ok();
-  }
-
-  Status EnsureHubScratch(uint32_t max_deg) {
-    const uint64_t slots = GlobalHashSlots(ctx_, max_deg);
-    if (slots > g_keys_.count) {
-      PCC_RETURN_IF_ERROR(AllocHubScratch(ctx_, slots, &g_keys_, &g_vals_, &g_used_));
-      g_cap_ = uint32_t(slots / (uint64_t(ctx_->num_sms) * 2));
-    }
+    (void)max_deg;
     return Status::Ok();
   }
 
@@ -401,6 +397,7 @@ class Engine {
     PCC_RETURN_IF_ERROR(L->s.Alloc(ctx_, nn));
     PCC_RETURN_IF_ERROR(L->k.Alloc(ctx_, nn));
     PCC_RETURN_IF_ERROR(L->K.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(L->Kf.Alloc(ctx_, nn));
     if (n) {
       if (k_is_ones || !d_k) {
         FillF64Kernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, 1.0, L->k.p); PCC_COUNT(1);
@@ -415,10 +412,18 @@ class Engine {
       } else {
         SingletonsKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->k.p, L->C.p, L->s.p, L->K.p); PCC_COUNT(1);
       }
+      RefreshKfKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->K.p, L->Kf.p, nullptr, 0); PCC_COUNT(1);
       PCC_RETURN_IF_ERROR(LaunchCheck());
     }
     L->int_mode = IntModeFor(*g, cfg_.edge_weight_offset);
-    PCC_RETURN_IF_ERROR(EnsureHubScratch(g->max_deg));
+    if (d_labels) {
+      PCC_RETURN_IF_ERROR(EnsureAllBins(ctx_, g));
+      L->bins = &g->bins_all;
+    } else {
+      L->bins = &g->bins;
+    }
+    PCC_RETURN_IF_ERROR(EnsureHubPlan(ctx_, g));
+    PCC_RETURN_IF_ERROR(AllocHubState(ctx_, *g->hub_plan, &hub_state_));
     *out = std::move(L);
     return Status::Ok();
   }
@@ -426,15 +431,18 @@ class Engine {
   // One best-move round over `front` (host_counts known).  Builds the next
   // frontier in dyn_ unless ALL_MOVE.  Returns whether the next frontier is
   // non-empty (local_moved).
-  Status Round(Level* L, const BinSet& front, const uint32_t* host_counts, uint64_t front_edges,
-               uint64_t front_size, bool* next_nonempty) {
+  // front_stamp == 0: all vertices; else vertices with next_stamp == it.
+  Status Round(Level* L, uint32_t front_stamp, uint64_t front_edges, uint64_t front_size, bool* next_nonempty,
+               uint32_t* next_front_stamp, uint64_t* next_edges, uint64_t* next_size) {
     const DevGraph& g = *L->g;
     const uint32_t n = g.n;
     stamp_++;
     res_.rounds++;
     res_.edge_visits += front_edges;
     res_.vertex_visits += front_size;
-    res_.algo_bytes += (g.w.p ? 12ull : 8ull) * front_edges + 40ull * front_size;
+    // Isolated vertices outside L->bins are not visited by any kernel.
+    const uint64_t visited = front_stamp ? front_size : L->bins->size;
+    res_.algo_bytes += (g.w.p ? 12ull : 8ull) * front_edges + 40ull * visited;
     // Reset per-round counters: frontier, movers, new_movers, marked, pend_edges.
     PCC_CUDA(cudaMemsetAsync(&ctr_.p->frontier, 0, sizeof(uint32_t) * 4, ctx_->stream));
     PCC_CUDA(cudaMemsetAsync(&ctr_.p->pend_edges, 0, sizeof(unsigned long long), ctx_->stream));
@@ -448,7 +456,9 @@ class Engine {
     a.s = L->s.p;
     a.k = L->k.p;
     a.K = L->K.p;
+    a.Kf = L->Kf.p;
     a.res = cfg_.resolution;
+    a.res32 = static_cast<float>(cfg_.resolution);
     a.offset = cfg_.edge_weight_offset;
     a.ioffset = static_cast<int32_t>(cfg_.edge_weight_offset);
     a.stamp = stamp_;
@@ -456,19 +466,23 @@ class Engine {
     a.moved_stamp = moved_stamp_.p;
     a.movers = movers_.p;
     a.ctr = ctr_.p;
-    a.g_keys = g_keys_.p;
-    a.g_vals = g_vals_.p;
-    a.g_used = g_used_.p;
-    a.g_cap = g_cap_;
     a.async = cfg_.async ? 1 : 0;
     a.s_mut = L->s.p;
     a.K_mut = L->K.p;
     a.C_mut = L->C.p;
     a.moved_cluster_stamp = mod_stamp_.p;
-    const uint32_t* counts = front.counts.p;
+    a.front_stamp = front_stamp ? next_stamp_.p : nullptr;
+    a.front_val = front_stamp;
+    const BinSet& bins = *L->bins;
     timer_.Begin(kPhaseBestMoves);
-    PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx_, a, front.list.p, counts, counts + kNumBins, host_counts,
-                                        L->int_mode, g.max_deg));
+    if (L->int_mode && !cfg_.async) {
+      PCC_RETURN_IF_ERROR(EnsureBatchPlan(ctx_, &g, &bins));
+      PCC_RETURN_IF_ERROR(LaunchBatchBestMoves(ctx_, a, *bins.batch_plan));
+    } else {
+      PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx_, a, bins.list.p, bins.counts.p, bins.counts.p + kNumBins,
+                                          bins.host_counts, L->int_mode, g.max_deg));
+    }
+    PCC_RETURN_IF_ERROR(LaunchHubBestMoves(ctx_, a, *g.hub_plan, hub_state_, L->int_mode));
     timer_.End(kPhaseBestMoves);
 
     timer_.Begin(kPhaseApply);
@@ -485,6 +499,10 @@ class Engine {
                                               StoreIndexIfSet{new_list_.p}, scan_tiles_,
                                               static_cast<uint32_t*>(nullptr)));
       AssignNewKernel<<<grid, kT, 0, ctx_->stream>>>(ap, zero_ids_.p, new_list_.p); PCC_COUNT(1);
+      if (n) {
+        RefreshKfKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->K.p, L->Kf.p, mod_stamp_.p, stamp_);
+        PCC_COUNT(1);
+      }
       PCC_RETURN_IF_ERROR(LaunchCheck());
     }
     timer_.End(kPhaseApply);
@@ -495,33 +513,36 @@ class Engine {
       PCC_RETURN_IF_ERROR(Sync(ctx_));
       if (!cfg_.async) res_.moves += hc.movers;
       *next_nonempty = n > 0;
+      *next_front_stamp = 0;
+      *next_size = n;
+      *next_edges = g.m;
       return Status::Ok();
     }
-    // Marked set (binned by degree), then its neighbourhood (edgeMap), then
-    // the degree-binned next frontier.
+    // Neighbourhood of the marked set (edgeMap), rows taken from the static
+    // degree bins with a marked-row predicate, then the next frontier's size.
     timer_.Begin(kPhaseFrontier);
+    const PushNeighbors push{g.nbr.p, next_stamp_.p, stamp_};
     if (cfg_.move_method == PCC_NBHR_CLUSTER_MOVE) {
-      PCC_RETURN_IF_ERROR(BinVertices(ctx_, n, g.off.p, PredModifiedCluster{L->C.p, mod_stamp_.p, stamp_},
-                                      &marked_bins_, nullptr, &ctr_.p->marked));
+      LaunchEdgeIter(ctx_, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins, g.bins.host_counts,
+                     g.off.p, push, PredModifiedCluster{L->C.p, mod_stamp_.p, stamp_});  // rows with d > 0
     } else {
-      PCC_RETURN_IF_ERROR(BinVertices(ctx_, n, g.off.p, PredStamp{moved_stamp_.p, stamp_}, &marked_bins_, nullptr,
-                                      &ctr_.p->marked));
+      LaunchEdgeIter(ctx_, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins, g.bins.host_counts,
+                     g.off.p, push, PredStamp{moved_stamp_.p, stamp_});
     }
-    LaunchEdgeIter(ctx_, marked_bins_.list.p, marked_bins_.counts.p, marked_bins_.counts.p + kNumBins, nullptr,
-                   g.off.p, PushNeighbors{g.nbr.p, next_stamp_.p, stamp_});
+    if (n) {
+      CountDegreesKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g.off.p, PredStamp{next_stamp_.p, stamp_},
+                                                                    &ctr_.p->pend_edges, &ctr_.p->frontier);
+      PCC_COUNT(1);
+    }
     PCC_RETURN_IF_ERROR(LaunchCheck());
-    PCC_RETURN_IF_ERROR(BinVertices(ctx_, n, g.off.p, PredStamp{next_stamp_.p, stamp_}, &dyn_,
-                                    &ctr_.p->pend_edges, &ctr_.p->frontier));
     timer_.End(kPhaseFrontier);
     DevCounters hc;
     PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
-    uint32_t hcounts[kNumBins];
-    PCC_RETURN_IF_ERROR(dyn_.counts.ToHost(hcounts, kNumBins));
     PCC_RETURN_IF_ERROR(Sync(ctx_));
-    for (int i = 0; i < kNumBins; ++i) dyn_.host_counts[i] = hcounts[i];
     if (!cfg_.async) res_.moves += hc.movers;
-    dyn_.size = hc.frontier;
-    dyn_.edges = hc.pend_edges;
+    *next_front_stamp = stamp_;
+    *next_size = hc.frontier;
+    *next_edges = hc.pend_edges;
     *next_nonempty = hc.frontier > 0;
     return Status::Ok();
   }
@@ -530,14 +551,13 @@ class Engine {
   Status IterateBestMoves(Level* L, int64_t num_inner, bool* moved_out) {
     bool moved = false;
     bool local_moved = true;
-    bool use_static = true;
+    uint32_t front = 0;  // all vertices
+    uint64_t front_edges = L->g->m, front_size = L->g->n;
     for (int64_t it = 0; it < num_inner && local_moved; ++it) {
-      const BinSet& front = use_static ? L->g->bins : dyn_;
       bool next = false;
-      PCC_RETURN_IF_ERROR(Round(L, front, front.host_counts, front.edges, front.size, &next));
+      PCC_RETURN_IF_ERROR(Round(L, front, front_edges, front_size, &next, &front, &front_edges, &front_size));
       local_moved = next;
       moved |= local_moved;
-      use_static = cfg_.move_method == PCC_ALL_MOVE;
     }
     *moved_out = moved;
     return Status::Ok();
@@ -620,6 +640,8 @@ class Engine {
           PCC_RETURN_IF_ERROR(Li->K.Zero());
           AccumulateClustersKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->C.p, Li->k.p, Li->s.p,
                                                                                 Li->K.p); PCC_COUNT(1);
+          RefreshKfKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->K.p, Li->Kf.p, nullptr, 0);
+          PCC_COUNT(1);
           PCC_RETURN_IF_ERROR(LaunchCheck());
         }
         bool moved = false;
@@ -671,12 +693,8 @@ class Engine {
   uint32_t stamp_ = 0;
   DBuf<uint32_t> moves_, movers_, moved_stamp_, mod_stamp_, next_stamp_, new_stamp_, aux_stamp_;
   DBuf<uint32_t> zero_ids_, new_list_;
-  BinSet marked_bins_;
   DBuf<uint32_t> scan_tiles_;
-  DBuf<uint32_t> g_keys_, g_used_;
-  DBuf<unsigned long long> g_vals_;
-  uint32_t g_cap_ = 0;
-  BinSet dyn_;
+  HubState hub_state_;
   DBuf<DevCounters> ctr_;
   RunResult res_;
   PhaseTimer timer_;
@@ -961,6 +979,8 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   const uint64_t nn = std::max<uint64_t>(n, 1);
   DBuf<uint32_t> dC, ds, dt, dm, dmoves, dmovers, dstamp;
   DBuf<double> dk, dK, dv;
+  DBuf<float> dKf;
+  PCC_RETURN_IF_ERROR(dKf.Alloc(ctx, nn));
   PCC_RETURN_IF_ERROR(dC.Alloc(ctx, nn));
   PCC_RETURN_IF_ERROR(ds.Alloc(ctx, nn));
   PCC_RETURN_IF_ERROR(dk.Alloc(ctx, nn));
@@ -976,13 +996,16 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   PCC_RETURN_IF_ERROR(ds.FromHost(s, n));
   PCC_RETURN_IF_ERROR(dk.FromHost(k, n));
   PCC_RETURN_IF_ERROR(dK.FromHost(K, n));
+  if (n) {
+    RefreshKfKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, dK.p, dKf.p, nullptr, 0);
+    PCC_COUNT(1);
+  }
   DBuf<DevCounters> ctr;
   PCC_RETURN_IF_ERROR(ctr.Alloc(ctx, 1));
   PCC_RETURN_IF_ERROR(ctr.Zero());
-  DBuf<uint32_t> gk, gu;
-  DBuf<unsigned long long> gv;
-  const uint64_t slots = GlobalHashSlots(ctx, g.max_deg);
-  if (slots) PCC_RETURN_IF_ERROR(AllocHubScratch(ctx, slots, &gk, &gv, &gu));
+  PCC_RETURN_IF_ERROR(EnsureHubPlan(ctx, &g));
+  HubState hs;
+  PCC_RETURN_IF_ERROR(AllocHubState(ctx, *g.hub_plan, &hs));
   BMArgs a{};
   a.n = n;
   a.off = g.off.p;
@@ -992,7 +1015,9 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   a.s = ds.p;
   a.k = dk.p;
   a.K = dK.p;
+  a.Kf = dKf.p;
   a.res = config->resolution;
+  a.res32 = static_cast<float>(config->resolution);
   a.offset = config->edge_weight_offset;
   a.ioffset = static_cast<int32_t>(config->edge_weight_offset);
   a.stamp = 1;
@@ -1003,13 +1028,17 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   a.out_target = dt.p;
   a.out_value = dv.p;
   a.out_moves = dm.p;
-  a.g_keys = gk.p;
-  a.g_vals = gv.p;
-  a.g_used = gu.p;
-  a.g_cap = slots ? uint32_t(slots / (uint64_t(ctx->num_sms) * 2)) : 0;
   a.async = 0;
-  PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx, a, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins,
-                                      g.bins.host_counts, IntModeFor(g, config->edge_weight_offset), g.max_deg));
+  PCC_RETURN_IF_ERROR(EnsureAllBins(ctx, &g));
+  const BinSet& ab = g.bins_all;
+  if (IntModeFor(g, config->edge_weight_offset)) {
+    PCC_RETURN_IF_ERROR(EnsureBatchPlan(ctx, &g, &ab));
+    PCC_RETURN_IF_ERROR(LaunchBatchBestMoves(ctx, a, *ab.batch_plan));
+  } else {
+    PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx, a, ab.list.p, ab.counts.p, ab.counts.p + kNumBins, ab.host_counts,
+                                        false, g.max_deg));
+  }
+  PCC_RETURN_IF_ERROR(LaunchHubBestMoves(ctx, a, *g.hub_plan, hs, IntModeFor(g, config->edge_weight_offset)));
   PCC_RETURN_IF_ERROR(dt.ToHost(out_t, n));
   PCC_RETURN_IF_ERROR(dv.ToHost(out_v, n));
   if (out_moves) PCC_RETURN_IF_ERROR(dm.ToHost(out_moves, n));

@@ -1,0 +1,238 @@
+// moves.cuh -- device helpers shared by the best-move kernels: the move
+// value formulas of ClusteringHelper::EfficientBestMove
+// (parallel-correlation-clusterer-internal.cc:448-583, EdgeSum in
+// correlation-clusterer-util.h:26-43), the sync / async decision
+// (parallel-correlation-clusterer.cc:139-157, internal.cc:371-403), the FP32
+// pre-filter bound and the open-addressing hash used for aggregation.
+#pragma once
+
+#include <math_constants.h>
+
+#include <climits>
+#include <type_traits>
+
+#include "engine.cuh"
+
+namespace pcc {
+namespace {
+
+__device__ __forceinline__ uint32_t WarpAppendFull(uint32_t* counter, bool pred) {
+  const unsigned mask = __ballot_sync(kFull, pred);
+  uint32_t base = 0;
+  if (mask) {
+    const int leader = __ffs(mask) - 1;
+    if (int(LaneId()) == leader) base = atomicAdd(counter, uint32_t(__popc(mask)));
+    base = __shfl_sync(kFull, base, leader);
+  }
+  return base + __popc(mask & LaneMaskLt());
+}
+
+template <bool kAsync>
+__device__ __forceinline__ uint32_t LdC(const uint32_t* p) {
+  return kAsync ? __ldcg(p) : __ldg(p);
+}
+template <bool kAsync>
+__device__ __forceinline__ double LdK(const double* p) {
+  return kAsync ? __ldcg(p) : __ldg(p);
+}
+
+// Fibonacci hashing: the HIGH bits of key * 2^32/phi.  (The low bits of the
+// product depend only on the key's low bits, which are shared by many
+// structured ids -- e.g. RMAT vertex ids -- and would chain the probes.)
+__device__ __forceinline__ uint32_t HashSlot(uint32_t key, uint32_t mask) {
+  const uint32_t shift = __clz(mask) & 31u;  // mask = cap - 1, cap a power of two
+  return ((key * 0x9E3779B1u) >> shift) & mask;
+}
+
+// Open addressing with linear probing; keys are cluster ids, kNone = empty.
+// Capacity is at least twice the number of keys, so a free slot exists.
+
+// (val desc, id asc) ordering used by every argmax.
+__device__ __forceinline__ bool Better(double va, uint32_t ia, double vb, uint32_t ib) {
+  return va > vb || (va == vb && ia < ib);
+}
+
+__device__ __forceinline__ bool InFront(const BMArgs& a, uint32_t v) {
+  return a.front_stamp == nullptr || a.front_stamp[v] == a.front_val;
+}
+
+struct VertexCtx {
+  uint32_t v;
+  uint64_t b;
+  uint32_t d;
+  uint32_t c;
+  double kv;
+  double Kc;
+};
+
+template <bool kAsync>
+__device__ __forceinline__ VertexCtx LoadVertex(const BMArgs& a, uint32_t v) {
+  VertexCtx x;
+  x.v = v;
+  x.b = a.off[v];
+  x.d = uint32_t(a.off[v + 1] - x.b);
+  x.c = LdC<kAsync>(a.C + v);
+  x.kv = a.k[v];
+  x.Kc = LdK<kAsync>(a.K + x.c);
+  return x;
+}
+
+__device__ __forceinline__ double ChangeOf(const BMArgs& a, const VertexCtx& x, double T) {
+  // change_in_objective -= together.NetWeight(kv * (K_c - kv))   (:483-488)
+  return Dsub(0.0, Dsub(T, Dmul(a.res, Dmul(x.kv, Dsub(x.Kc, x.kv)))));
+}
+
+__device__ __forceinline__ double ValOf(const BMArgs& a, double kv, double change, double S, double KD) {
+  // change + data.NetWeight(moving_nodes_weight * K_D)   (:493-497)
+  return Dadd(change, Dsub(S, Dmul(a.res, Dmul(kv, KD))));
+}
+
+// FP32 pre-filter of the INT-mode sync path.  For candidate D with exact
+// integer sum S_D, Y_D = (S_D - S_max) - res*kv*K_D orders the candidates
+// exactly like the reference's val_D = change + (S_D - res*(kv*K_D)).  Y' is
+// Y in FP32 from fl32 inputs: |Y' - Y| <= 2^-21 (R + |Y|) (five roundings of
+// 2^-24 in R, one in the subtraction; S_D - S_max is an exact integer).  The
+// bound below adds a 4x margin plus an absolute term that covers the FP64
+// roundings of val_D (<= 2^-50 (|change| + |S| + R)), so a candidate with
+// Y' + e < max(Y' - e) is strictly below the best in FP64 as well and never
+// needs its FP64 value; the survivors are evaluated exactly.
+__device__ __forceinline__ float FilterBound(float R, float Y, float S, float change32) {
+  return __fadd_rn(__fmul_rn(3.814697265625e-06f /* 2^-18 */, __fadd_rn(R, fabsf(Y))),
+                   __fmul_rn(3.552713678800501e-15f /* 2^-48 */,
+                             __fadd_rn(__fadd_rn(fabsf(change32), fabsf(S)), R)));
+}
+
+// Finishes one vertex: the chosen move and the sync / async decision.
+// Returns true when the vertex must be appended to the movers list (sync).
+template <bool kAsync>
+__device__ __forceinline__ bool Decide(const BMArgs& a, const VertexCtx& x, double best, uint32_t bid,
+                                       double change) {
+  uint32_t target;
+  double value;
+  if (bid == kNone || change >= best) {
+    target = a.n;
+    value = change;
+  } else {
+    target = bid;
+    value = best;
+  }
+  if (a.out_target) {
+    a.out_target[x.v] = target;
+    a.out_value[x.v] = value;
+  }
+  if (kAsync) {
+    // AsyncMove (internal.cc:371-403): apply immediately.
+    if (!(value > 0)) return false;
+    const uint32_t cur = x.c;
+    atomicSub(&a.s_mut[cur], 1u);
+    atomicAdd(&a.K_mut[cur], -1 * x.kv);
+    uint32_t dest = target;
+    if (target != a.n) {
+      atomicAdd(&a.s_mut[target], 1u);
+      atomicAdd(&a.K_mut[target], x.kv);
+    } else {
+      // Claim an empty id by CAS, probing linearly from the vertex's own id.
+      // Bounded: after 4n probes the kernel records an error and leaves the
+      // vertex where it was (its leave is undone).
+      uint64_t i = x.v;
+      const uint64_t limit = 4ull * a.n + 64;
+      bool got = false;
+      for (uint64_t p = 0; p < limit; ++p) {
+        if (__ldcg(&a.s_mut[i]) == 0u && atomicCAS(&a.s_mut[i], 0u, 1u) == 0u) {
+          got = true;
+          break;
+        }
+        i = (i + 1 == a.n) ? 0 : i + 1;
+      }
+      if (!got) {
+        atomicAdd(&a.s_mut[cur], 1u);
+        atomicAdd(&a.K_mut[cur], x.kv);
+        atomicExch(&a.ctr->error, kErrProbeLimit);
+        return false;
+      }
+      atomicAdd(&a.K_mut[i], x.kv);
+      dest = uint32_t(i);
+    }
+    __stcg(&a.C_mut[x.v], dest);
+    a.moved_cluster_stamp[dest] = a.stamp;
+    a.moved_stamp[x.v] = a.stamp;
+    atomicAdd(&a.ctr->moves, 1ull);
+    return false;
+  }
+  // Sync decision (parallel-correlation-clusterer.cc:142-156): the singleton
+  // rule, then move only on a positive value.
+  uint32_t t2 = target;
+  double v2 = value;
+  if (target < a.n && a.s[target] == 1u && a.s[x.c] == 1u && x.c >= target) {
+    t2 = x.c;
+    v2 = 0;
+  }
+  if (a.out_moves) a.out_moves[x.v] = v2 > 0 ? t2 : kNone;
+  if (v2 > 0) {
+    a.moved_stamp[x.v] = a.stamp;
+    if (t2 != x.c) {
+      a.moves[x.v] = t2;
+      return true;
+    }
+  }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// Hash tables with an occupied-slot list.  The table starts clean (keys
+// kNone, values 0); each insert appends its slot to `used`, and after the
+// vertex only the used slots are read and cleared, so the cost per vertex is
+// proportional to its distinct neighbour clusters, not to the capacity.
+// ---------------------------------------------------------------------------
+template <bool kGlobal>
+__device__ __forceinline__ uint32_t HKey(const uint32_t* keys, uint32_t i) {
+  return kGlobal ? __ldcg(keys + i) : keys[i];
+}
+template <bool kGlobal>
+__device__ __forceinline__ unsigned long long HVal(const unsigned long long* vals, uint32_t i) {
+  return kGlobal ? __ldcg(vals + i) : vals[i];
+}
+
+// Finds or inserts `key`; *inserted is set when this call claimed the slot.
+template <bool kGlobal>
+__device__ __forceinline__ uint32_t FindOrInsertT(uint32_t* keys, uint32_t cap, uint32_t key, bool* inserted) {
+  const uint32_t mask = cap - 1;
+  uint32_t h = HashSlot(key, mask);
+  *inserted = false;
+  for (uint32_t probes = 0; probes < cap; ++probes) {
+    const uint32_t k = HKey<kGlobal>(keys, h);
+    if (k == key) return h;
+    if (k == kNone) {
+      const uint32_t old = atomicCAS(&keys[h], kNone, key);
+      if (old == kNone) {
+        *inserted = true;
+        return h;
+      }
+      if (old == key) return h;
+    }
+    h = (h + 1) & mask;
+  }
+  return kNone;
+}
+
+template <bool kGlobal>
+__device__ __forceinline__ uint32_t FindT(const uint32_t* keys, uint32_t cap, uint32_t key) {
+  const uint32_t mask = cap - 1;
+  uint32_t h = HashSlot(key, mask);
+  for (uint32_t probes = 0; probes < cap; ++probes) {
+    const uint32_t k = HKey<kGlobal>(keys, h);
+    if (k == key) return h;
+    if (k == kNone) return kNone;
+    h = (h + 1) & mask;
+  }
+  return kNone;
+}
+
+template <bool kInt>
+__device__ __forceinline__ double AsDouble(unsigned long long bits) {
+  return kInt ? static_cast<double>(static_cast<long long>(bits))
+              : __longlong_as_double(static_cast<long long>(bits));
+}
+
+}  // namespace
+}  // namespace pcc
