@@ -39,6 +39,30 @@ pcch_graph* pcch_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double
 pcch_graph* pcch_gen_lfr(uint32_t n, double mean_degree, uint32_t dmax, double tau1, uint32_t cmin, uint32_t cmax,
                          double tau2, double mu, double w_lo, double w_hi, uint64_t seed);
 
+/*
+ * Text-format ClustererConfig (clustering/config.proto:94-197) -> pcc_config,
+ * as TextFormat::ParseFromString in cluster-in-memory_main.cc:256-264.
+ * config_case: 0 unset, 1 parameter_string, 4 affinity, 7 correlation.
+ * err (may be NULL) receives the parse error message.  Returns a status code.
+ */
+int32_t pcch_parse_config(const char* text, pcc_config* out, int32_t* config_case, char* err, size_t err_len);
+
+/*
+ * GBBS adjacency text file ("AdjacencyGraph" / "WeightedAdjacencyGraph"),
+ * as gbbs_io::read_(un)weighted_symmetric_graph in cluster-in-memory_main.cc:
+ * 286-306.  Returns NULL and sets *status on error.  All-one weights are
+ * dropped (unit-weight graph).
+ */
+pcch_graph* pcch_read_gbbs(const char* path, int32_t float_weighted, int32_t* status);
+
+/*
+ * CompareCommunities (cluster-in-memory_main.cc:167-222) of a clustering
+ * given as labels[n] (cluster index per node) against a communities file
+ * (tab-separated node ids, one community per line).  out6 = {avg precision,
+ * avg recall, number of clusters, min size, max size, avg size}.
+ */
+int32_t pcch_compare_communities(const char* communities_path, uint32_t n, const uint32_t* labels, double* out6);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -51,6 +51,14 @@ def host_lib():
                                    ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, ctypes.c_uint64]
         L.pcch_gen_lfr.restype = GP
+        L.pcch_parse_config.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                        ctypes.c_char_p, ctypes.c_size_t]
+        L.pcch_parse_config.restype = ctypes.c_int32
+        L.pcch_read_gbbs.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+        L.pcch_read_gbbs.restype = GP
+        L.pcch_compare_communities.argtypes = [ctypes.c_char_p, ctypes.c_uint32, ctypes.c_void_p,
+                                               ctypes.POINTER(ctypes.c_double)]
+        L.pcch_compare_communities.restype = ctypes.c_int32
         _lib = L
     return _lib
 
@@ -96,6 +104,42 @@ def write_gbbs(path: str, g: CsrGraph) -> None:
         np.savetxt(f, g.neighbors.astype(np.uint32), fmt="%d")
         if g.weights is not None:
             np.savetxt(f, g.weights.astype(np.float32), fmt="%.9g")
+
+
+def parse_config(text: str):
+    """Text-format ClustererConfig -> (PccConfig, config_case) via the C++
+    parser (config_case: 0 unset, 1 parameter_string, 4 affinity, 7
+    correlation).  Raises PccError(3) with the parser's message."""
+    from pcc_gb300 import PccConfig
+    cfg = PccConfig()
+    case = ctypes.c_int32(0)
+    err = ctypes.create_string_buffer(512)
+    st = host_lib().pcch_parse_config(text.encode(), ctypes.byref(cfg), ctypes.byref(case), err, 512)
+    if st != 0:
+        raise PccError(st, err.value.decode(errors="replace"))
+    return cfg, case.value
+
+
+def read_gbbs_native(path: str, float_weighted: bool = False) -> CsrGraph:
+    """Reads a GBBS adjacency file with the C++ reader of the CLI."""
+    st = ctypes.c_int32(0)
+    gp = host_lib().pcch_read_gbbs(path.encode(), 1 if float_weighted else 0, ctypes.byref(st))
+    if not gp:
+        raise PccError(st.value, f"cannot read GBBS graph {path}")
+    g, _ = _take(gp)
+    return g
+
+
+def compare_communities(path: str, labels) -> dict:
+    """CompareCommunities of the CLI: average precision / recall of the
+    clustering (labels = cluster index per node) against a communities file."""
+    lab = np.ascontiguousarray(labels, dtype=np.uint32)
+    out = (ctypes.c_double * 6)()
+    st = host_lib().pcch_compare_communities(path.encode(), lab.size, lab.ctypes.data_as(ctypes.c_void_p), out)
+    if st != 0:
+        raise PccError(st, f"cannot score against {path}")
+    keys = ("avg_precision", "avg_recall", "num_clusters", "min_size", "max_size", "avg_size")
+    return dict(zip(keys, list(out)))
 
 
 def read_gbbs(path: str) -> CsrGraph:
