@@ -235,6 +235,43 @@ pcc_status pcc_compress(pcc_context* ctx, const pcc_graph* graph,
 pcc_status pcc_graph_node_weights(pcc_context* ctx, const pcc_graph* graph,
                                   double* out);
 
+/*
+ * No reference counterpart.  EfficientBestMove (target and value, before the
+ * sync decision; the out_targets / out_values of pcc_best_moves) for a list
+ * of vertices, on caller-owned DEVICE arrays, allocating no device memory.
+ * For callers that hold all device memory in their own allocator (a serving
+ * loop with a fixed HBM budget, a framework's caching allocator) and cannot
+ * let a library call cudaMalloc on the request path.
+ *
+ * Scratch is one file-scope device array of 24 MiB (2^21 hash slots); each
+ * listed vertex needs nextpow2(2 * degree + 2) slots, so degrees up to
+ * 1,048,575.  max_degree (>= every listed vertex's degree) above that limit
+ * returns OUT_OF_RANGE before launching; a listed vertex whose degree
+ * exceeds max_degree gets target 0xFFFFFFFF and the call returns
+ * OUT_OF_RANGE.  Vertex or cluster ids >= n return INVALID_ARGUMENT.
+ *
+ *   d_offsets / d_neighbors / d_weights   device CSR (d_weights NULL = 1)
+ *   d_cluster_ids (uint32[n]), d_node_weights (double[n]),
+ *   d_cluster_weights (double[n], per cluster id)
+ *   d_vertices    device uint32[num_vertices], or NULL for all n vertices
+ *   d_out_targets / d_out_values   device arrays of num_vertices
+ *   stream        cudaStream_t (NULL = default stream) of the current device
+ *
+ * Runs on the current device.  The first call on a device resolves the
+ * scratch address and must come before any stream capture.  The call
+ * synchronises `stream` to read its status.  Calls that overlap in time on
+ * one device share the scratch and race: serialise them.  Sums use FP64
+ * atomics: equal to pcc_best_moves on integer weights, within rounding on
+ * real weights.
+ */
+pcc_status pcc_best_moves_static(
+    uint32_t n, const uint64_t* d_offsets, const uint32_t* d_neighbors,
+    const float* d_weights, const uint32_t* d_cluster_ids,
+    const double* d_node_weights, const double* d_cluster_weights,
+    double resolution, double edge_weight_offset, const uint32_t* d_vertices,
+    uint32_t num_vertices, uint32_t max_degree, uint32_t* d_out_targets,
+    double* d_out_values, void* stream);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif
