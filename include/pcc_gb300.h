@@ -129,6 +129,7 @@ uint64_t pcc_device_bytes_in_use(const pcc_context* ctx);
  * GbbsGraph::Import/FinishImport (clustering/gbbs-graph.cc:32-76) and the
  * CLI's CopyGraph injection (clustering/cluster-in-memory_main.cc:231-306).
  * weights == NULL stores a unit-weight graph with no weight array.
+ * n must be at most 2^32 - 32 (INVALID_ARGUMENT otherwise).
  */
 pcc_status pcc_graph_upload(pcc_context* ctx, uint32_t n, uint64_t m,
                             const uint64_t* offsets, const uint32_t* neighbors,

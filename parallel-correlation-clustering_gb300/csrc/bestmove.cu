@@ -22,6 +22,7 @@
 //   FP64 mode: degree <= 1000 adds in adjacency order (the reference's
 //             sequential flat_hash_map path, bit-exact); hubs add in any
 //             order, as the reference's concurrent map does.
+#include "certify.cuh"
 #include "moves.cuh"
 
 namespace pcc {
@@ -64,14 +65,12 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
     }
     const bool cand = has && u != x.v;
     const uint32_t cu = cand ? LdC<kAsync>(a.C + u) : kNone;
-    const unsigned long long key =
-        cand ? ((static_cast<unsigned long long>(g) << 32) | cu) : (0xFFFFFFFF00000000ull | lane);
-    const unsigned peers = __match_any_sync(kFull, key);
+    const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane)) & gmask;
     const bool leader = cand && int(lane) == __ffs(peers) - 1;
     double S;
     if (kInt) {
       const int xi = cand ? (static_cast<int>(wt) - a.ioffset) : 0;
-      S = static_cast<double>(__reduce_add_sync(peers, xi));
+      S = static_cast<double>(GroupSumInt(peers, xi, a.w == nullptr, leader, reinterpret_cast<int*>(stage[warp])));
     } else {
       stage[warp][lane] = cand ? Dsub(static_cast<double>(wt), a.offset) : 0.0;
       __syncwarp();
@@ -186,8 +185,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
       }
       const bool cand = has && u != x.v;
       const uint32_t cu = cand ? LdC<kAsync>(a.C + u) : kNone;
-      const unsigned long long key = cand ? cu : (0x100000000ull | lane);
-      const unsigned peers = __match_any_sync(kFull, key);
+      const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane));
       const bool leader = cand && int(lane) == __ffs(peers) - 1;
       uint32_t slot = kNone;
       bool ins = false;
@@ -205,7 +203,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
       }
       if (kInt) {
         const int xi = cand ? (static_cast<int>(wt) - a.ioffset) : 0;
-        const int S = __reduce_add_sync(peers, xi);
+        const int S = GroupSumInt(peers, xi, a.w == nullptr, leader, reinterpret_cast<int*>(stage));
         if (slot != kNone) vals[slot] += static_cast<unsigned long long>(static_cast<long long>(S));
       } else {
         stage[lane] = cand ? Dsub(static_cast<double>(wt), a.offset) : 0.0;
@@ -302,6 +300,290 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
   }
 }
 
+// ---------------------------------------------------------------------------
+// INT-mode synchronous rounds: certified decisions (certify.cuh).  The FP32
+// pre-filter selects the survivors; when they form one (S, K) class and the
+// FP32 bounds decide the move, no FP64 instruction runs for the vertex.
+// Otherwise -- and always in replay mode, where the exact values are outputs
+// -- the exact FP64 values decide; in replay mode a certified decision that
+// differs from the FP64 one raises kErrCertMismatch (a self-check).
+// ---------------------------------------------------------------------------
+template <int G>
+__global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t* __restrict__ list,
+                                                      const uint32_t* __restrict__ bin_counts,
+                                                      const uint32_t* __restrict__ bin_starts, int bin) {
+  __shared__ int stage[8][32];
+  const uint32_t count = bin_counts[bin];
+  const uint32_t start = bin_starts[bin];
+  const unsigned lane = LaneId(), warp = threadIdx.x >> 5;
+  constexpr unsigned kVpw = 32 / G;
+  const unsigned g = lane / G, gl = lane % G;
+  const unsigned gmask = G == 32 ? kFull : (((1u << G) - 1u) << (g * G));
+  const bool replay = a.out_target != nullptr;
+  const bool unit = a.w == nullptr;
+  const uint64_t stride = uint64_t(gridDim.x) * 8 * kVpw;
+  for (uint64_t base = (uint64_t(blockIdx.x) * 8 + warp) * kVpw; base < count; base += stride) {
+    const uint64_t idx = base + g;
+    bool vvalid = idx < count;
+    VertexCtx x{};
+    if (vvalid) {
+      const uint32_t v = list[start + idx];
+      vvalid = InFront(a, v);
+      if (vvalid) x = LoadVertex<false>(a, v);
+    }
+    if (__ballot_sync(kFull, vvalid) == 0) continue;
+    const bool has = vvalid && gl < x.d;
+    uint32_t u = x.v;
+    float wt = 0.f;
+    if (has) {
+      u = a.nbr[x.b + gl];
+      wt = a.w ? a.w[x.b + gl] : 1.0f;
+    }
+    const bool cand = has && u != x.v;
+    const uint32_t cu = cand ? __ldg(a.C + u) : kNone;
+    const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane)) & gmask;
+    const bool leader = cand && int(lane) == __ffs(peers) - 1;
+    const int xi = cand ? (static_cast<int>(wt) - a.ioffset) : 0;
+    const int S = GroupSumInt(peers, xi, unit, leader, stage[warp]);
+    const unsigned tmask = __ballot_sync(kFull, leader && cu == x.c) & gmask;
+    const int Tsh = __shfl_sync(kFull, S, tmask ? __ffs(tmask) - 1 : int(lane));
+    const long long T = tmask ? Tsh : 0;
+    int smax = leader ? S : INT_MIN;
+#pragma unroll
+    for (int o = G / 2; o >= 1; o >>= 1) smax = max(smax, __shfl_xor_sync(kFull, smax, o));
+    const float k32 = vvalid ? a.kf[x.v] : 0.f;
+    const float Kc32 = vvalid ? a.Kf[x.c] : 0.f;
+    const ChangeApprox ca = ApproxChange(a.res32, a.int_nw != 0, k32, Kc32, T);
+    const float cabs = ChangeAbsBound(ca);
+    // FP32 pre-filter over the group's leaders.
+    FilterVal f{0.f, 0.f, false};
+    float KfD = 0.f;
+    float lo = -CUDART_INF_F;
+    if (leader) {
+      KfD = a.Kf[cu];
+      f = FilterOf(a.res32, k32, KfD, S, smax, cabs);
+      if (f.sane) lo = __fsub_rn(f.Y, f.e);
+    }
+    float U = lo;
+#pragma unroll
+    for (int o = G / 2; o >= 1; o >>= 1) U = fmaxf(U, __shfl_xor_sync(kFull, U, o));
+    const bool contender = leader && (!f.sane || __fadd_rn(f.Y, f.e) >= U);
+    // The leading (S, K) class of the contenders and the trailing one.
+    LexKey lead, tail;
+    double KD = 0.0;
+    if (contender) {
+      KD = a.K[cu];
+      const unsigned long long ko = KOrder(KD);
+      lead.Keep(S, ko, cu);
+      tail.Keep(-static_cast<long long>(S), ~ko, cu);
+    }
+    LexGroupReduce<G>(lead);
+    LexGroupReduce<G>(tail);
+    const bool single = lead.id == kNone || (-tail.S == lead.S && ~tail.K == lead.K);
+    int cres = kUncertain;
+    uint32_t ctarget = kNone;
+    if (vvalid && single) {
+      const float KfA = lead.id != kNone ? a.Kf[lead.id] : 0.f;
+      cres = CertifyDecision(ca, a.res32, k32, lead.id != kNone, lead.S, KfA, lead.id, a.n, &ctarget);
+    }
+    const uint32_t cmove = cres == kUncertain ? kNone : CertifiedMove(a, x, ctarget, cres == kCertMove);
+    const bool fp64 = vvalid && (replay || cres == kUncertain);
+    bool append = false;
+    if (vvalid && !fp64 && gl == 0) append = ApplyCertified(a, x, cmove);
+    if (__ballot_sync(kFull, fp64)) {
+      // Exact path: FP64 change and values of the contenders.
+      double change = 0.0, val = -CUDART_INF;
+      uint32_t id = kNone;
+      if (fp64) {
+        change = ChangeOf(a, x, static_cast<double>(T));
+        if (contender) {
+          val = ValOf(a, x.kv, change, static_cast<double>(S), KD);
+          id = cu;
+        }
+      }
+#pragma unroll
+      for (int o = G / 2; o >= 1; o >>= 1) {
+        const double ov = __shfl_xor_sync(kFull, val, o);
+        const uint32_t oid = __shfl_xor_sync(kFull, id, o);
+        if (Better(ov, oid, val, id)) {
+          val = ov;
+          id = oid;
+        }
+      }
+      if (fp64 && gl == 0) {
+        append = Decide<false>(a, x, val, id, change);
+        if (replay && cres != kUncertain && a.out_moves && a.out_moves[x.v] != cmove)
+          atomicExch(&a.ctr->error, kErrCertMismatch);
+      }
+    }
+    const uint32_t slot = WarpAppendFull(&a.ctr->movers, append);
+    if (append) a.movers[slot] = x.v;
+  }
+}
+
+template <int HC>
+constexpr size_t CertWarpSmem() {
+  // per warp: vals HC*8, keys HC*4, used HC/2 * 2, stage 32*4, count 16
+  return size_t(kWarpKernelWarps) * (size_t(HC) * 13 + 32 * 4 + 16);
+}
+
+template <int HC>
+__global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a, const uint32_t* __restrict__ list,
+                                                                       const uint32_t* __restrict__ bin_counts,
+                                                                       const uint32_t* __restrict__ bin_starts,
+                                                                       int bin) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const uint32_t count = bin_counts[bin];
+  const uint32_t start = bin_starts[bin];
+  const unsigned lane = LaneId(), warp = threadIdx.x >> 5;
+  unsigned char* base = smem + size_t(warp) * (size_t(HC) * 13 + 32 * 4 + 16);
+  long long* vals = reinterpret_cast<long long*>(base);
+  uint32_t* keys = reinterpret_cast<uint32_t*>(base + size_t(HC) * 8);
+  int* stage = reinterpret_cast<int*>(base + size_t(HC) * 12);
+  uint16_t* used = reinterpret_cast<uint16_t*>(base + size_t(HC) * 12 + 32 * 4);
+  uint32_t* used_count = reinterpret_cast<uint32_t*>(base + size_t(HC) * 13 + 32 * 4);
+  const bool replay = a.out_target != nullptr;
+  const bool unit = a.w == nullptr;
+  for (int i = lane; i < HC; i += 32) {
+    keys[i] = kNone;
+    vals[i] = 0;
+  }
+  if (lane == 0) *used_count = 0;
+  __syncwarp();
+  for (uint64_t idx = uint64_t(blockIdx.x) * kWarpKernelWarps + warp; idx < count;
+       idx += uint64_t(gridDim.x) * kWarpKernelWarps) {
+    const uint32_t vid = list[start + idx];
+    if (!InFront(a, vid)) continue;
+    const VertexCtx x = LoadVertex<false>(a, vid);
+    for (uint32_t e0 = 0; e0 < x.d; e0 += 32) {
+      const uint32_t e = e0 + lane;
+      const bool has = e < x.d;
+      uint32_t u = x.v;
+      float wt = 0.f;
+      if (has) {
+        u = a.nbr[x.b + e];
+        wt = a.w ? a.w[x.b + e] : 1.0f;
+      }
+      const bool cand = has && u != x.v;
+      const uint32_t cu = cand ? __ldg(a.C + u) : kNone;
+      const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane));
+      const bool leader = cand && int(lane) == __ffs(peers) - 1;
+      uint32_t slot = kNone;
+      bool ins = false;
+      if (leader) {
+        slot = FindOrInsertT<false>(keys, HC, cu, &ins);
+        if (slot == kNone) atomicExch(&a.ctr->error, kErrHashFull);
+      }
+      const unsigned im = __ballot_sync(kFull, ins);
+      if (im) {
+        uint32_t b0 = 0;
+        const int ld = __ffs(im) - 1;
+        if (int(lane) == ld) b0 = atomicAdd(used_count, uint32_t(__popc(im)));
+        b0 = __shfl_sync(kFull, b0, ld);
+        if (ins) used[b0 + __popc(im & LaneMaskLt())] = static_cast<uint16_t>(slot);
+      }
+      const int xi = cand ? (static_cast<int>(wt) - a.ioffset) : 0;
+      const int Sg = GroupSumInt(peers, xi, unit, leader, stage);
+      if (slot != kNone) vals[slot] += Sg;
+      __syncwarp();
+    }
+    long long T = 0;
+    if (lane == 0) {
+      const uint32_t slot = FindT<false>(keys, HC, x.c);
+      if (slot != kNone) T = vals[slot];
+    }
+    T = __shfl_sync(kFull, T, 0);
+    const uint32_t nused = *used_count;
+    const float k32 = a.kf[x.v];
+    const ChangeApprox ca = ApproxChange(a.res32, a.int_nw != 0, k32, a.Kf[x.c], T);
+    const float cabs = ChangeAbsBound(ca);
+    long long smax = LLONG_MIN;
+    for (uint32_t i = lane; i < nused; i += 32) smax = max(smax, vals[used[i]]);
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) smax = max(smax, __shfl_xor_sync(kFull, smax, o));
+    float U = -CUDART_INF_F;
+    for (uint32_t i = lane; i < nused; i += 32) {
+      const uint32_t slot = used[i];
+      const FilterVal f = FilterOf(a.res32, k32, a.Kf[keys[slot]], vals[slot], smax, cabs);
+      if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) U = fmaxf(U, __shfl_xor_sync(kFull, U, o));
+    LexKey lead, tail;
+    for (uint32_t i = lane; i < nused; i += 32) {
+      const uint32_t slot = used[i];
+      const uint32_t key = keys[slot];
+      const FilterVal f = FilterOf(a.res32, k32, a.Kf[key], vals[slot], smax, cabs);
+      if (f.sane && __fadd_rn(f.Y, f.e) < U) {
+        keys[slot] = kNone;  // not a contender: cleared now, skipped later
+        vals[slot] = 0;
+        used[i] = 0xFFFFu;
+        continue;
+      }
+      const unsigned long long ko = KOrder(a.K[key]);
+      lead.Keep(vals[slot], ko, key);
+      tail.Keep(-vals[slot], ~ko, key);
+    }
+    LexGroupReduce<32>(lead);
+    LexGroupReduce<32>(tail);
+    const bool single = lead.id == kNone || (-tail.S == lead.S && ~tail.K == lead.K);
+    int cres = kUncertain;
+    uint32_t ctarget = kNone;
+    if (single) {
+      const float KfA = lead.id != kNone ? a.Kf[lead.id] : 0.f;
+      cres = CertifyDecision(ca, a.res32, k32, lead.id != kNone, lead.S, KfA, lead.id, a.n, &ctarget);
+    }
+    const uint32_t cmove = cres == kUncertain ? kNone : CertifiedMove(a, x, ctarget, cres == kCertMove);
+    bool append = false;
+    if (replay || cres == kUncertain) {
+      // Exact path over the contenders (warp-uniform branch).
+      const double change = ChangeOf(a, x, static_cast<double>(T));
+      double best = -CUDART_INF;
+      uint32_t bid = kNone;
+      for (uint32_t i = lane; i < nused; i += 32) {
+        const uint32_t slot = used[i];
+        if (slot == 0xFFFFu) continue;
+        const uint32_t key = keys[slot];
+        const double val = ValOf(a, x.kv, change, static_cast<double>(vals[slot]), a.K[key]);
+        if (Better(val, key, best, bid)) {
+          best = val;
+          bid = key;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        const double ov = __shfl_xor_sync(kFull, best, o);
+        const uint32_t oid = __shfl_xor_sync(kFull, bid, o);
+        if (Better(ov, oid, best, bid)) {
+          best = ov;
+          bid = oid;
+        }
+      }
+      if (lane == 0) {
+        append = Decide<false>(a, x, best, bid, change);
+        if (replay && cres != kUncertain && a.out_moves && a.out_moves[x.v] != cmove)
+          atomicExch(&a.ctr->error, kErrCertMismatch);
+      }
+    } else if (lane == 0) {
+      append = ApplyCertified(a, x, cmove);
+    }
+    __syncwarp();
+    // Clear the table through the key list (used[] may hold 0xFFFF marks).
+    for (uint32_t i = lane; i < nused; i += 32) {
+      const uint32_t slot = used[i];
+      if (slot != 0xFFFFu) {
+        keys[slot] = kNone;
+        vals[slot] = 0;
+      }
+    }
+    const uint32_t pos = WarpAppendFull(&a.ctr->movers, append);
+    if (append) a.movers[pos] = x.v;
+    __syncwarp();
+    if (lane == 0) *used_count = 0;
+    __syncwarp();
+  }
+}
+
 template <class K>
 Status SetSmem(K kernel, size_t bytes) {
   PCC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
@@ -318,37 +600,43 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
   };
   auto want = [&](int bin) { return !host_counts || host_counts[bin] > 0; };
   cudaStream_t st = ctx->stream;
-  if (want(kBinG4))
-    BestMoveGroupKernel<4, kInt, kAsync><<<grid(kBinG4, 64, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG4); PCC_COUNT(1);
-  if (want(kBinG8))
-    BestMoveGroupKernel<8, kInt, kAsync><<<grid(kBinG8, 32, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG8); PCC_COUNT(1);
-  if (want(kBinG16))
-    BestMoveGroupKernel<16, kInt, kAsync><<<grid(kBinG16, 16, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG16); PCC_COUNT(1);
-  if (want(kBinG32))
-    BestMoveGroupKernel<32, kInt, kAsync><<<grid(kBinG32, 8, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG32); PCC_COUNT(1);
-  if (want(kBinW128)) {
-    auto k = BestMoveWarpKernel<256, kInt, kAsync>;
-    PCC_RETURN_IF_ERROR(SetSmem(k, WarpKernelSmem<256>()));
-    k<<<grid(kBinW128, kWarpKernelWarps, sms * 16), kWarpKernelWarps * 32, WarpKernelSmem<256>(), st>>>(
-        a, list, counts, starts, kBinW128); PCC_COUNT(1);
+  constexpr bool kCert = kInt && !kAsync;
+  if (kCert) {
+    if (want(kBinG4))
+      CertGroupKernel<4><<<grid(kBinG4, 64, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG4); PCC_COUNT(1);
+    if (want(kBinG8))
+      CertGroupKernel<8><<<grid(kBinG8, 32, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG8); PCC_COUNT(1);
+    if (want(kBinG16))
+      CertGroupKernel<16><<<grid(kBinG16, 16, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG16); PCC_COUNT(1);
+    if (want(kBinG32))
+      CertGroupKernel<32><<<grid(kBinG32, 8, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG32); PCC_COUNT(1);
+  } else {
+    if (want(kBinG4))
+      BestMoveGroupKernel<4, kInt, kAsync><<<grid(kBinG4, 64, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG4); PCC_COUNT(1);
+    if (want(kBinG8))
+      BestMoveGroupKernel<8, kInt, kAsync><<<grid(kBinG8, 32, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG8); PCC_COUNT(1);
+    if (want(kBinG16))
+      BestMoveGroupKernel<16, kInt, kAsync><<<grid(kBinG16, 16, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG16); PCC_COUNT(1);
+    if (want(kBinG32))
+      BestMoveGroupKernel<32, kInt, kAsync><<<grid(kBinG32, 8, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG32); PCC_COUNT(1);
   }
-  if (want(kBinW256)) {
-    auto k = BestMoveWarpKernel<512, kInt, kAsync>;
-    PCC_RETURN_IF_ERROR(SetSmem(k, WarpKernelSmem<512>()));
-    k<<<grid(kBinW256, kWarpKernelWarps, sms * 8), kWarpKernelWarps * 32, WarpKernelSmem<512>(), st>>>(
-        a, list, counts, starts, kBinW256); PCC_COUNT(1);
-  }
-  if (want(kBinW512)) {
-    auto k = BestMoveWarpKernel<1024, kInt, kAsync>;
-    PCC_RETURN_IF_ERROR(SetSmem(k, WarpKernelSmem<1024>()));
-    k<<<grid(kBinW512, kWarpKernelWarps, sms * 4), kWarpKernelWarps * 32, WarpKernelSmem<1024>(), st>>>(
-        a, list, counts, starts, kBinW512); PCC_COUNT(1);
-  }
-  if (want(kBinW1000)) {
-    auto k = BestMoveWarpKernel<2048, kInt, kAsync>;
-    PCC_RETURN_IF_ERROR(SetSmem(k, WarpKernelSmem<2048>()));
-    k<<<grid(kBinW1000, kWarpKernelWarps, sms * 2), kWarpKernelWarps * 32, WarpKernelSmem<2048>(), st>>>(
-        a, list, counts, starts, kBinW1000); PCC_COUNT(1);
+  auto warp_bin = [&](auto k, size_t smem, int bin, unsigned cap) -> Status {
+    if (!want(bin)) return Status::Ok();
+    PCC_RETURN_IF_ERROR(SetSmem(k, smem));
+    k<<<grid(bin, kWarpKernelWarps, cap), kWarpKernelWarps * 32, smem, st>>>(a, list, counts, starts, bin);
+    PCC_COUNT(1);
+    return Status::Ok();
+  };
+  if (kCert) {
+    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<256>, CertWarpSmem<256>(), kBinW128, sms * 16));
+    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<512>, CertWarpSmem<512>(), kBinW256, sms * 8));
+    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<1024>, CertWarpSmem<1024>(), kBinW512, sms * 4));
+    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<2048>, CertWarpSmem<2048>(), kBinW1000, sms * 2));
+  } else {
+    PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<256, kInt, kAsync>, WarpKernelSmem<256>(), kBinW128, sms * 16));
+    PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<512, kInt, kAsync>, WarpKernelSmem<512>(), kBinW256, sms * 8));
+    PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<1024, kInt, kAsync>, WarpKernelSmem<1024>(), kBinW512, sms * 4));
+    PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<2048, kInt, kAsync>, WarpKernelSmem<2048>(), kBinW1000, sms * 2));
   }
   return LaunchCheck();
 }

@@ -9,6 +9,7 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -232,6 +233,26 @@ inline unsigned Blocks(uint64_t items, unsigned per_block, unsigned cap) {
 // ---------------------------------------------------------------------------
 // Device helpers.
 // ---------------------------------------------------------------------------
+// FP32 image of an FP64 quantity for the pre-filter and the certified
+// decision: the nearest float when the value is 0 or within [2^-100, 2^100],
+// NaN otherwise (the relative-error model needs normal floats; a NaN
+// candidate always survives the filter and makes a decision uncertain).
+__host__ __device__ inline float FilterF32(double d) {
+  const double m = d < 0 ? -d : d;
+  if (d == 0.0 || (m >= 7.888609052210118e-31 && m <= 1.2676506002282294e30)) return static_cast<float>(d);
+#ifdef __CUDA_ARCH__
+  return __int_as_float(0x7fc00000);
+#else
+  return std::numeric_limits<float>::quiet_NaN();
+#endif
+}
+
+// A 32-bit match key no cluster id can take: graphs have at most
+// kMaxVertices vertices, so ids stay below 0xFFFFFFE0.  (A 64-bit
+// __match_any_sync key costs far more than a 32-bit one.)
+constexpr uint32_t kMaxVertices = 0xFFFFFFE0u;
+__device__ __forceinline__ uint32_t LaneSentinel(unsigned lane) { return 0xFFFFFFE0u | lane; }
+
 __device__ __forceinline__ unsigned LaneId() {
   unsigned r;
   asm volatile("mov.u32 %0, %%laneid;" : "=r"(r));

@@ -21,8 +21,8 @@ namespace pcc {
 //   d <= 128/256/512     one warp, shared-memory hash of 256/512/1024 slots
 //   d <= 1000            one warp, shared-memory hash of 2048 slots
 //                        (the reference's sequential path ends at 1000)
-//   d <= 4096            one CTA, shared-memory hash of 8192 slots
-//   d >  4096            one CTA, hash in global scratch
+//   d >  1000            hubs: hash-partitioned CTAs (hubs.cuh); the two
+//                        top bins only split the static vertex list
 // ---------------------------------------------------------------------------
 enum Bin : int {
   kBinG4 = 0, kBinG8, kBinG16, kBinG32,
@@ -46,8 +46,6 @@ __host__ __device__ inline int BinOf(uint64_t d) {
   return kBinGlobal;
 }
 
-struct BatchPlan;
-
 // Degree-binned vertex list: bins are contiguous segments of `list`.
 struct BinSet {
   DBuf<uint32_t> list;       // n entries
@@ -55,7 +53,6 @@ struct BinSet {
   uint64_t edges = 0;        // sum of degrees (host copy, static bins only)
   uint32_t size = 0;         // vertices (host copy, static bins only)
   uint32_t host_counts[kNumBins] = {0};
-  mutable std::shared_ptr<BatchPlan> batch_plan;  // built on first use
 };
 
 struct HubPlan;
@@ -107,6 +104,7 @@ struct DevCounters {
 
 constexpr int kErrProbeLimit = 1;   // async new-cluster probe exceeded its bound
 constexpr int kErrHashFull = 2;     // a best-move hash table filled up
+constexpr int kErrCertMismatch = 3; // a certified decision differed from FP64 (replay self-check)
 
 // Best-move kernel arguments.
 struct BMArgs {
@@ -118,9 +116,11 @@ struct BMArgs {
   const uint32_t* s;
   const double* k;
   const double* K;
-  const float* Kf;          // fl32(K), current for the sync round (filter input)
+  const float* Kf;          // FilterF32(K), current for the sync round (filter input)
+  const float* kf;          // FilterF32(k), node weights (certified decisions)
   double res;
-  float res32;
+  float res32;              // FilterF32(res)
+  int int_nw;               // all node weights are integers (certified decisions)
   double offset;
   int32_t ioffset;          // integer offset (INT mode)
   uint32_t stamp;
@@ -152,9 +152,8 @@ Status LaunchBestMoves(Context* ctx, const BMArgs& a, const uint32_t* list, cons
                        const uint32_t* bin_starts, const uint32_t* host_counts, bool int_mode,
                        uint32_t max_deg);
 
-// The hub plan of a graph / the batch plan of a bin set (built on first use).
+// The hub plan of a graph (built on first use).
 Status EnsureHubPlan(Context* ctx, const DevGraph* g);
-Status EnsureBatchPlan(Context* ctx, const DevGraph* g, const BinSet* bins);
 
 }  // namespace pcc
 

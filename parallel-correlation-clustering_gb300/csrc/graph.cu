@@ -7,7 +7,6 @@
 
 #include "graphops.cuh"
 #include "hubs.cuh"
-#include "batch.cuh"
 
 namespace pcc {
 
@@ -94,14 +93,6 @@ Status EnsureHubPlan(Context* ctx, const DevGraph* g) {
   return Status::Ok();
 }
 
-Status EnsureBatchPlan(Context* ctx, const DevGraph* g, const BinSet* bins) {
-  if (bins->batch_plan) return Status::Ok();
-  auto plan = std::make_shared<BatchPlan>();
-  PCC_RETURN_IF_ERROR(BuildBatchPlan(ctx, *g, *bins, plan.get()));
-  bins->batch_plan = std::move(plan);
-  return Status::Ok();
-}
-
 Status EnsureAllBins(Context* ctx, const DevGraph* g) {
   if (g->bins_all.list.p) return Status::Ok();
   return BuildBins(ctx, g, &g->bins_all, true);
@@ -148,7 +139,7 @@ Status Upload(pcc_context* pctx, uint32_t n, uint64_t m, const uint64_t* off, co
   if (!pctx || !out) return MakeError(PCC_INVALID_ARGUMENT, "null context or output");
   if (!off || (m && !nbr)) return MakeError(PCC_INVALID_ARGUMENT, "null offsets or neighbors");
   if (m >= 0xFFFFFFFFull) return MakeError(PCC_INVALID_ARGUMENT, "graphs with 2^32 or more entries are not supported");
-  if (n == 0xFFFFFFFFu) return MakeError(PCC_INVALID_ARGUMENT, "n must be below 2^32 - 1");
+  if (n > kMaxVertices) return MakeError(PCC_INVALID_ARGUMENT, "n must be at most 2^32 - 32");
   Context* ctx = &pctx->c;
   if (!device_src) {
     if (off[0] != 0 || off[n] != m)

@@ -19,7 +19,6 @@
 
 #include "graphops.cuh"
 #include "hubs.cuh"
-#include "batch.cuh"
 
 namespace pcc {
 
@@ -86,7 +85,21 @@ __global__ void AccumulateClustersKernel(uint32_t n, const uint32_t* __restrict_
 __global__ void RefreshKfKernel(uint32_t n, const double* __restrict__ K, float* Kf,
                                 const uint32_t* __restrict__ mod_stamp, uint32_t stamp) {
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
-    if (stamp == 0 || mod_stamp[i] == stamp) Kf[i] = static_cast<float>(K[i]);
+    if (stamp == 0 || mod_stamp[i] == stamp) Kf[i] = FilterF32(K[i]);
+}
+
+// kf = FilterF32(k): node weights for the FP32 pre-filter and certified
+// decisions.
+__global__ void NodeKfKernel(uint32_t n, const double* __restrict__ k, float* kf) {
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    kf[i] = FilterF32(k[i]);
+}
+
+// All node weights are integers of magnitude below 2^53 (host array).
+bool IntegralWeights(const double* w, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i)
+    if (!(w[i] == std::trunc(w[i]) && std::fabs(w[i]) < 9007199254740992.0)) return false;
+  return true;
 }
 
 // cluster_ids[i] = C[cluster_ids[i]] (FlattenClustering).
@@ -331,7 +344,8 @@ struct Level {
   std::unique_ptr<DevGraph> own;
   DBuf<uint32_t> C, s;
   DBuf<double> k, K;
-  DBuf<float> Kf;  // fl32(K)
+  DBuf<float> Kf;  // FilterF32(K)
+  DBuf<float> kf;  // FilterF32(k)
   // Vertices the best-move kernels visit: the degree > 0 bins, or all
   // vertices when isolated ones may sit in shared clusters (level 0 started
   // from given labels).  From singletons an isolated vertex never moves:
@@ -358,7 +372,8 @@ bool IntModeFor(const DevGraph& g, double offset) {
 
 class Engine {
  public:
-  Engine(Context* ctx, const pcc_config& cfg) : ctx_(ctx), cfg_(cfg), timer_(ctx->stream) {}
+  Engine(Context* ctx, const pcc_config& cfg, bool int_nw)
+      : ctx_(ctx), cfg_(cfg), int_nw_(int_nw), timer_(ctx->stream) {}
 
   Status Init(uint32_t n_max, uint32_t max_deg) {
     n_max_ = n_max;
@@ -398,6 +413,7 @@ class Engine {
     PCC_RETURN_IF_ERROR(L->k.Alloc(ctx_, nn));
     PCC_RETURN_IF_ERROR(L->K.Alloc(ctx_, nn));
     PCC_RETURN_IF_ERROR(L->Kf.Alloc(ctx_, nn));
+    PCC_RETURN_IF_ERROR(L->kf.Alloc(ctx_, nn));
     if (n) {
       if (k_is_ones || !d_k) {
         FillF64Kernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, 1.0, L->k.p); PCC_COUNT(1);
@@ -413,6 +429,7 @@ class Engine {
         SingletonsKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->k.p, L->C.p, L->s.p, L->K.p); PCC_COUNT(1);
       }
       RefreshKfKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->K.p, L->Kf.p, nullptr, 0); PCC_COUNT(1);
+      NodeKfKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->k.p, L->kf.p); PCC_COUNT(1);
       PCC_RETURN_IF_ERROR(LaunchCheck());
     }
     L->int_mode = IntModeFor(*g, cfg_.edge_weight_offset);
@@ -457,8 +474,10 @@ class Engine {
     a.k = L->k.p;
     a.K = L->K.p;
     a.Kf = L->Kf.p;
+    a.kf = L->kf.p;
+    a.int_nw = int_nw_ ? 1 : 0;
     a.res = cfg_.resolution;
-    a.res32 = static_cast<float>(cfg_.resolution);
+    a.res32 = FilterF32(cfg_.resolution);
     a.offset = cfg_.edge_weight_offset;
     a.ioffset = static_cast<int32_t>(cfg_.edge_weight_offset);
     a.stamp = stamp_;
@@ -475,13 +494,8 @@ class Engine {
     a.front_val = front_stamp;
     const BinSet& bins = *L->bins;
     timer_.Begin(kPhaseBestMoves);
-    if (L->int_mode && !cfg_.async) {
-      PCC_RETURN_IF_ERROR(EnsureBatchPlan(ctx_, &g, &bins));
-      PCC_RETURN_IF_ERROR(LaunchBatchBestMoves(ctx_, a, *bins.batch_plan));
-    } else {
-      PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx_, a, bins.list.p, bins.counts.p, bins.counts.p + kNumBins,
-                                          bins.host_counts, L->int_mode, g.max_deg));
-    }
+    PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx_, a, bins.list.p, bins.counts.p, bins.counts.p + kNumBins,
+                                        bins.host_counts, L->int_mode, g.max_deg));
     PCC_RETURN_IF_ERROR(LaunchHubBestMoves(ctx_, a, *g.hub_plan, hub_state_, L->int_mode));
     timer_.End(kPhaseBestMoves);
 
@@ -689,6 +703,7 @@ class Engine {
  private:
   Context* ctx_;
   pcc_config cfg_;
+  bool int_nw_ = false;  // integer node weights (certified decisions)
   uint32_t n_max_ = 0;
   uint32_t stamp_ = 0;
   DBuf<uint32_t> moves_, movers_, moved_stamp_, mod_stamp_, next_stamp_, new_stamp_, aux_stamp_;
@@ -847,7 +862,10 @@ Status ClusterImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config* 
     PCC_RETURN_IF_ERROR(dinit.FromHost(initial_labels, n));
   }
   PCC_RETURN_IF_ERROR(dout.Alloc(ctx, nn));
-  Engine eng(ctx, cfg);
+  // Integer node weights: degrees, the default ones, or given integers (sums
+  // of integers stay integers on the compressed levels).
+  const bool int_nw = modularity || !node_weights || IntegralWeights(node_weights, n);
+  Engine eng(ctx, cfg, int_nw);
   uint32_t groups = 0;
   PCC_RETURN_IF_ERROR(eng.Run(g, dk.p, dinit.p, dout.p, &groups));
   double obj = 0;
@@ -979,8 +997,9 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   const uint64_t nn = std::max<uint64_t>(n, 1);
   DBuf<uint32_t> dC, ds, dt, dm, dmoves, dmovers, dstamp;
   DBuf<double> dk, dK, dv;
-  DBuf<float> dKf;
+  DBuf<float> dKf, dkf;
   PCC_RETURN_IF_ERROR(dKf.Alloc(ctx, nn));
+  PCC_RETURN_IF_ERROR(dkf.Alloc(ctx, nn));
   PCC_RETURN_IF_ERROR(dC.Alloc(ctx, nn));
   PCC_RETURN_IF_ERROR(ds.Alloc(ctx, nn));
   PCC_RETURN_IF_ERROR(dk.Alloc(ctx, nn));
@@ -999,6 +1018,8 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   if (n) {
     RefreshKfKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, dK.p, dKf.p, nullptr, 0);
     PCC_COUNT(1);
+    NodeKfKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, dk.p, dkf.p);
+    PCC_COUNT(1);
   }
   DBuf<DevCounters> ctr;
   PCC_RETURN_IF_ERROR(ctr.Alloc(ctx, 1));
@@ -1016,8 +1037,10 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   a.k = dk.p;
   a.K = dK.p;
   a.Kf = dKf.p;
+  a.kf = dkf.p;
+  a.int_nw = IntegralWeights(k, n) ? 1 : 0;
   a.res = config->resolution;
-  a.res32 = static_cast<float>(config->resolution);
+  a.res32 = FilterF32(config->resolution);
   a.offset = config->edge_weight_offset;
   a.ioffset = static_cast<int32_t>(config->edge_weight_offset);
   a.stamp = 1;
@@ -1031,13 +1054,8 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   a.async = 0;
   PCC_RETURN_IF_ERROR(EnsureAllBins(ctx, &g));
   const BinSet& ab = g.bins_all;
-  if (IntModeFor(g, config->edge_weight_offset)) {
-    PCC_RETURN_IF_ERROR(EnsureBatchPlan(ctx, &g, &ab));
-    PCC_RETURN_IF_ERROR(LaunchBatchBestMoves(ctx, a, *ab.batch_plan));
-  } else {
-    PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx, a, ab.list.p, ab.counts.p, ab.counts.p + kNumBins, ab.host_counts,
-                                        false, g.max_deg));
-  }
+  PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx, a, ab.list.p, ab.counts.p, ab.counts.p + kNumBins, ab.host_counts,
+                                      IntModeFor(g, config->edge_weight_offset), g.max_deg));
   PCC_RETURN_IF_ERROR(LaunchHubBestMoves(ctx, a, *g.hub_plan, hs, IntModeFor(g, config->edge_weight_offset)));
   PCC_RETURN_IF_ERROR(dt.ToHost(out_t, n));
   PCC_RETURN_IF_ERROR(dv.ToHost(out_v, n));

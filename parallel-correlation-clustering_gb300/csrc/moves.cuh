@@ -228,6 +228,28 @@ __device__ __forceinline__ uint32_t FindT(const uint32_t* keys, uint32_t cap, ui
   return kNone;
 }
 
+// Sum of the integer weights x over the calling lane's match_any group
+// `peers`; every lane of the warp calls it.  (__reduce_add_sync with a
+// different mask per group executes once per distinct group -- up to 32
+// passes per instruction.)  Unit weights: every lane's x is the same, so the
+// sum is x * |group|.  Other weights: the group's leader adds its peers'
+// values from the warp's 32-int stage row (passes = the largest group).
+__device__ __forceinline__ int GroupSumInt(unsigned peers, int x, bool unit, bool leader, int* stage) {
+  if (unit) return x * __popc(peers);
+  stage[LaneId()] = x;
+  __syncwarp();
+  int s = 0;
+  if (leader) {
+    unsigned mm = peers;
+    while (mm) {
+      s += stage[__ffs(mm) - 1];
+      mm &= mm - 1;
+    }
+  }
+  __syncwarp();
+  return s;
+}
+
 template <bool kInt>
 __device__ __forceinline__ double AsDouble(unsigned long long bits) {
   return kInt ? static_cast<double>(static_cast<long long>(bits))

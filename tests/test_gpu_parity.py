@@ -240,3 +240,30 @@ def test_clusterer_class_dropin(ctx, graphs):
         init[grp] = i
     lab_o2, _ = O.modularity_cluster(og, cfg, initial_labels=init)
     assert refined == P.labels_to_clustering(lab_o2)
+
+
+@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "sbm3k_int"])
+@pytest.mark.parametrize("weights", ["int", "real", "huge"])
+def test_best_moves_certified_paths(ctx, graphs, name, weights):
+    """INT-mode replays over node weights and resolutions that push the FP32
+    certification to both outcomes.  Replay runs the exact FP64 path and
+    raises an error if a certified decision disagrees with it; the result
+    must equal the oracle bit for bit."""
+    g = graphs[name]
+    dg, og = _both(ctx, g)
+    rng = np.random.default_rng(17)
+    if weights == "int":
+        k = rng.integers(1, 6, size=g.n).astype(np.float64)
+    elif weights == "real":
+        k = rng.uniform(0.25, 3.0, size=g.n)
+    else:
+        k = rng.integers(1, 4, size=g.n).astype(np.float64) * 2.0**26   # K beyond 2^24
+    for div in (1, 5, 200):
+        C, s, _, K = rand_state(g.n, max(1, g.n // div), seed=div, node_weights=k)
+        for res in (0.0, 1e-12, 1e-3, 0.37, 5.0):
+            cfg = P.make_config(resolution=res * (2.0**-52 if weights == "huge" else 1.0))
+            t_g, v_g, m_g = P.best_moves(dg, cfg, C, s, k, K)
+            t_o, v_o, m_o = O.best_moves(og, cfg, C, s, k, K)
+            np.testing.assert_array_equal(t_g, t_o)
+            np.testing.assert_array_equal(v_g.view(np.uint64), v_o.view(np.uint64))
+            np.testing.assert_array_equal(m_g, m_o)
