@@ -421,13 +421,19 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
   }
 }
 
-template <int HC>
+// Per-warp shared bytes: vals HC*sizeof(V), keys HC*4, stage 32*4, used
+// HC/2 * 2, count 16.
+template <int HC, typename V>
+__host__ __device__ constexpr size_t CertWarpStride() {
+  return size_t(HC) * (sizeof(V) + 5) + 32 * 4 + 16;
+}
+template <int HC, typename V>
 constexpr size_t CertWarpSmem() {
-  // per warp: vals HC*8, keys HC*4, used HC/2 * 2, stage 32*4, count 16
-  return size_t(kWarpKernelWarps) * (size_t(HC) * 13 + 32 * 4 + 16);
+  return size_t(kWarpKernelWarps) * CertWarpStride<HC, V>();
 }
 
-template <int HC>
+// V: int when every cluster sum fits in 32 bits (narrow), else long long.
+template <int HC, typename V>
 __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a, const uint32_t* __restrict__ list,
                                                                        const uint32_t* __restrict__ bin_counts,
                                                                        const uint32_t* __restrict__ bin_starts,
@@ -436,12 +442,12 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
   const uint32_t count = bin_counts[bin];
   const uint32_t start = bin_starts[bin];
   const unsigned lane = LaneId(), warp = threadIdx.x >> 5;
-  unsigned char* base = smem + size_t(warp) * (size_t(HC) * 13 + 32 * 4 + 16);
-  long long* vals = reinterpret_cast<long long*>(base);
-  uint32_t* keys = reinterpret_cast<uint32_t*>(base + size_t(HC) * 8);
-  int* stage = reinterpret_cast<int*>(base + size_t(HC) * 12);
-  uint16_t* used = reinterpret_cast<uint16_t*>(base + size_t(HC) * 12 + 32 * 4);
-  uint32_t* used_count = reinterpret_cast<uint32_t*>(base + size_t(HC) * 13 + 32 * 4);
+  unsigned char* base = smem + size_t(warp) * CertWarpStride<HC, V>();
+  V* vals = reinterpret_cast<V*>(base);
+  uint32_t* keys = reinterpret_cast<uint32_t*>(base + size_t(HC) * sizeof(V));
+  int* stage = reinterpret_cast<int*>(base + size_t(HC) * (sizeof(V) + 4));
+  uint16_t* used = reinterpret_cast<uint16_t*>(base + size_t(HC) * (sizeof(V) + 4) + 32 * 4);
+  uint32_t* used_count = reinterpret_cast<uint32_t*>(base + size_t(HC) * (sizeof(V) + 5) + 32 * 4);
   const bool replay = a.out_target != nullptr;
   const bool unit = a.w == nullptr;
   for (int i = lane; i < HC; i += 32) {
@@ -484,7 +490,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
       }
       const int xi = cand ? (static_cast<int>(wt) - a.ioffset) : 0;
       const int Sg = GroupSumInt(peers, xi, unit, leader, stage);
-      if (slot != kNone) vals[slot] += Sg;
+      if (slot != kNone) vals[slot] += static_cast<V>(Sg);
       __syncwarp();
     }
     long long T = 0;
@@ -497,10 +503,11 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     const float k32 = a.kf[x.v];
     const ChangeApprox ca = ApproxChange(a.res32, a.int_nw != 0, k32, a.Kf[x.c], T);
     const float cabs = ChangeAbsBound(ca);
-    long long smax = LLONG_MIN;
-    for (uint32_t i = lane; i < nused; i += 32) smax = max(smax, vals[used[i]]);
+    V vmax = sizeof(V) == 4 ? V(INT_MIN) : V(LLONG_MIN);
+    for (uint32_t i = lane; i < nused; i += 32) vmax = max(vmax, vals[used[i]]);
 #pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) smax = max(smax, __shfl_xor_sync(kFull, smax, o));
+    for (int o = 16; o >= 1; o >>= 1) vmax = max(vmax, __shfl_xor_sync(kFull, vmax, o));
+    const long long smax = vmax;
     float U = -CUDART_INF_F;
     for (uint32_t i = lane; i < nused; i += 32) {
       const uint32_t slot = used[i];
@@ -521,8 +528,9 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
         continue;
       }
       const unsigned long long ko = KOrder(a.K[key]);
-      lead.Keep(vals[slot], ko, key);
-      tail.Keep(-vals[slot], ~ko, key);
+      const long long S = vals[slot];
+      lead.Keep(S, ko, key);
+      tail.Keep(-S, ~ko, key);
     }
     LexGroupReduce<32>(lead);
     LexGroupReduce<32>(tail);
@@ -627,11 +635,16 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
     PCC_COUNT(1);
     return Status::Ok();
   };
-  if (kCert) {
-    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<256>, CertWarpSmem<256>(), kBinW128, sms * 16));
-    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<512>, CertWarpSmem<512>(), kBinW256, sms * 8));
-    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<1024>, CertWarpSmem<1024>(), kBinW512, sms * 4));
-    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<2048>, CertWarpSmem<2048>(), kBinW1000, sms * 2));
+  if (kCert && a.narrow) {
+    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<256, int>, CertWarpSmem<256, int>(), kBinW128, sms * 16));
+    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<512, int>, CertWarpSmem<512, int>(), kBinW256, sms * 8));
+    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<1024, int>, CertWarpSmem<1024, int>(), kBinW512, sms * 6));
+    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<2048, int>, CertWarpSmem<2048, int>(), kBinW1000, sms * 3));
+  } else if (kCert) {
+    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<256, long long>, CertWarpSmem<256, long long>(), kBinW128, sms * 16));
+    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<512, long long>, CertWarpSmem<512, long long>(), kBinW256, sms * 8));
+    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<1024, long long>, CertWarpSmem<1024, long long>(), kBinW512, sms * 4));
+    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<2048, long long>, CertWarpSmem<2048, long long>(), kBinW1000, sms * 2));
   } else {
     PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<256, kInt, kAsync>, WarpKernelSmem<256>(), kBinW128, sms * 16));
     PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<512, kInt, kAsync>, WarpKernelSmem<512>(), kBinW256, sms * 8));

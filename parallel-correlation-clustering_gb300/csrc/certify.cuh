@@ -47,6 +47,12 @@ constexpr float kU48 = 3.552713678800501e-15f;  // 2^-48
 constexpr float kU50 = 8.881784197001252e-16f;  // 2^-50
 constexpr float kTwo24 = 16777216.0f;
 
+// int64 -> float through the 32-bit conversion when the value fits (the
+// 64-bit conversion is far slower on this GPU).
+__device__ __forceinline__ float I2F(long long x) {
+  return (x >= INT_MIN && x <= INT_MAX) ? __int2float_rn(static_cast<int>(x)) : __ll2float_rn(x);
+}
+
 __device__ __forceinline__ bool SaneF(float z) {
   const float m = fabsf(z);
   return z == 0.0f || (m >= 7.888609052210118e-31f /* 2^-100 */ && m <= 1.2676506002282294e30f /* 2^100 */);
@@ -102,8 +108,8 @@ __device__ __forceinline__ FilterVal FilterOf(float r32, float k32, float KfD, l
                                               float change32) {
   FilterVal f;
   const float R = __fmul_rn(r32, __fmul_rn(k32, KfD));
-  f.Y = __fsub_rn(static_cast<float>(S - Smax), R);
-  f.e = FilterBound(R, f.Y, static_cast<float>(S), change32);
+  f.Y = __fsub_rn(I2F(S - Smax), R);
+  f.e = FilterBound(R, f.Y, I2F(S), change32);
   f.sane = SaneF(R) && SaneF(KfD) && isfinite(f.Y) && isfinite(f.e);
   return f;
 }
@@ -131,7 +137,7 @@ __device__ __forceinline__ ChangeApprox ApproxChange(float r32, bool int_nw, flo
   const float rk = __fmul_rn(fabsf(r32), fabsf(k32));
   const float M = __fmul_rn(r32, __fmul_rn(k32, diff));
   const float eM = __fadd_rn(__fmul_rn(__fmul_rn(rk, ed), 1.0001f), __fmul_rn(kU21, fabsf(M)));
-  const float T32 = static_cast<float>(T);
+  const float T32 = I2F(T);
   const float eT = fabsf(T32) > kTwo24 ? __fmul_rn(kU23, fabsf(T32)) : 0.0f;
   c.M = M;
   c.eM = eM;
@@ -158,7 +164,7 @@ __device__ __forceinline__ int CertifyDecision(const ChangeApprox& c, float r32,
   if (!c.ok) return kUncertain;
   if (has_cand) {
     const float RA = __fmul_rn(r32, __fmul_rn(k32, KfA));
-    const float SA32 = static_cast<float>(SA);
+    const float SA32 = I2F(SA);
     const float X = __fsub_rn(SA32, RA);
     float eX = __fadd_rn(__fmul_rn(kU21, fabsf(RA)), __fmul_rn(kU23, fabsf(X)));
     if (fabsf(SA32) > kTwo24) eX = __fadd_rn(eX, __fmul_rn(kU23, fabsf(SA32)));
@@ -170,13 +176,13 @@ __device__ __forceinline__ int CertifyDecision(const ChangeApprox& c, float r32,
       // bound carries only the FP32 error of M and R_A (a vertex tied
       // between its own cluster and A has S_A = T and a tiny value).
       const long long I = SA - c.T;
-      const float I32 = static_cast<float>(I);
+      const float I32 = I2F(I);
       const float mr = __fsub_rn(c.M, RA);
       const float vs = __fadd_rn(I32, mr);
       float ev = __fadd_rn(__fadd_rn(c.eM, __fmul_rn(kU21, fabsf(RA))),
                            __fmul_rn(kU23, __fadd_rn(fabsf(mr), fabsf(vs))));
       if (fabsf(I32) > kTwo24) ev = __fadd_rn(ev, __fmul_rn(kU23, fabsf(I32)));
-      ev = __fadd_rn(ev, __fmul_rn(kU48, __fadd_rn(__fadd_rn(fabsf(static_cast<float>(c.T)), SA32 < 0 ? -SA32 : SA32),
+      ev = __fadd_rn(ev, __fmul_rn(kU48, __fadd_rn(__fadd_rn(fabsf(I2F(c.T)), fabsf(SA32)),
                                                     __fadd_rn(fabsf(c.M), fabsf(RA)))));
       *target = idA;
       if (!isfinite(ev)) return kUncertain;

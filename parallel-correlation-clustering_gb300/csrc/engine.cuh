@@ -73,6 +73,7 @@ struct DevGraph {
   uint32_t max_deg = 0;
   bool integral = true;   // every weight is an integer value
   double max_abs_w = 1.0; // max |w| (1 for unit weights)
+  double row_abs_bound = 0; // upper bound of any row's sum of |w|
   const float* wp() const { return w.p; }
 };
 
@@ -121,6 +122,7 @@ struct BMArgs {
   double res;
   float res32;              // FilterF32(res)
   int int_nw;               // all node weights are integers (certified decisions)
+  int narrow;               // INT mode and every cluster sum fits in 32 bits
   double offset;
   int32_t ioffset;          // integer offset (INT mode)
   uint32_t stamp;

@@ -18,9 +18,12 @@ struct DegreeInput {
 };
 
 // Non-integral weight count and max |w| (as float bits of the magnitude).
+// Weight statistics: non-integral count, max |w| and the sum of |w| over
+// integral weights below 2^32 (saturating; it bounds every row's sum).
 struct WeightStats {
   unsigned long long nonint;
   float maxabs;
+  unsigned long long sumabs;
 };
 struct WeightInput {
   const float* w;
@@ -29,6 +32,7 @@ struct WeightInput {
     WeightStats r;
     r.nonint = (x != truncf(x) || isnan(x) || isinf(x)) ? 1ull : 0ull;
     r.maxabs = fabsf(x);
+    r.sumabs = r.maxabs < 4294967296.0f ? __float2uint_rz(r.maxabs) : 0xFFFFFFFFull;
     return r;
   }
 };
@@ -37,6 +41,8 @@ struct WeightOp {
     WeightStats r;
     r.nonint = a.nonint + b.nonint;
     r.maxabs = fmaxf(a.maxabs, b.maxabs);
+    r.sumabs = a.sumabs + b.sumabs;
+    if (r.sumabs < a.sumabs) r.sumabs = ~0ull;
     return r;
   }
 };
@@ -116,11 +122,11 @@ Status ComputeGraphProperties(Context* ctx, DevGraph* g) {
     PCC_RETURN_IF_ERROR(Reduce<uint32_t>(ctx, g->n, DegreeInput{g->off.p}, OpMax{}, 0u, out.p, part));
     PCC_RETURN_IF_ERROR(out.ToHost(&maxd, 1));
   }
-  WeightStats ws{0, 1.0f};
+  WeightStats ws{0, 1.0f, g->m};
   if (g->w.p && g->m) {
     DBuf<WeightStats> wpart, wout;
     PCC_RETURN_IF_ERROR(wout.Alloc(ctx, 1));
-    PCC_RETURN_IF_ERROR(Reduce<WeightStats>(ctx, g->m, WeightInput{g->w.p}, WeightOp{}, WeightStats{0, 0.0f},
+    PCC_RETURN_IF_ERROR(Reduce<WeightStats>(ctx, g->m, WeightInput{g->w.p}, WeightOp{}, WeightStats{0, 0.0f, 0},
                                             wout.p, wpart));
     PCC_RETURN_IF_ERROR(wout.ToHost(&ws, 1));
     PCC_RETURN_IF_ERROR(Sync(ctx));
@@ -129,6 +135,9 @@ Status ComputeGraphProperties(Context* ctx, DevGraph* g) {
   g->max_deg = maxd;
   g->integral = ws.nonint == 0;
   g->max_abs_w = ws.maxabs;
+  // A row's sum of |w| is at most max|w| * degree and at most the total.
+  g->row_abs_bound = std::min(static_cast<double>(ws.maxabs) * static_cast<double>(maxd),
+                              static_cast<double>(ws.sumabs));
   return Status::Ok();
 }
 

@@ -2,40 +2,49 @@
 //
 // The reference gives hubs their own path (EfficientBestMove, degree > 1000:
 // a concurrent sparse_additive_map and a parallel reduce, parallel-
-// correlation-clusterer-internal.cc:516-582).  Here a hub's neighbour
-// clusters are split by a hash of the cluster id into P partitions, each
-// small enough for one CTA's shared-memory table (P = ceil(degree /
-// kHubPartKeys)).  A work item is (hub, partition); its CTA
-//   1. scans the whole row (entries are re-read by the P CTAs of a hub, from
-//      L2 after the first), sums w - offset of the entries whose cluster
-//      falls in its partition into the shared table, and sums the entries of
-//      the hub's own cluster ("together");
-//   2. evaluates its table: FP32 pre-filter, exact FP64 value of the
-//      survivors, argmax (value desc, id asc);
-//   3. writes its partial best; the last CTA of the hub (atomic counter)
-//      combines the P partials and makes the sync / async decision.
-// A partition whose keys overflow the table is split again by further hash
-// bits and rescanned (sub-passes), so correctness does not depend on the
-// hash distribution.  No global hash tables, no spin-waits.
+// correlation-clusterer-internal.cc:516-582).  Here a hub's neighbour-cluster
+// sums live in shared memory only:
+//
+//   small hubs (1000 < degree <= kHubSmallMax): one CTA per hub, a table of
+//     2 * degree slots, so it never fills;
+//   big hubs (degree > kHubSmallMax): one thread-block cluster of
+//     kHubClusterSize CTAs per (hub, partition).  The cluster's tables form
+//     one distributed table: a hash of the cluster id picks the owning CTA,
+//     every CTA scans 1/kHubClusterSize of the row and adds each entry into
+//     its owner's table through distributed shared memory.  Hubs with more
+//     than kHubClusterKeys distinct neighbour clusters are split into P
+//     hash partitions (P = ceil(degree / kHubClusterKeys)), one cluster
+//     each, which re-read the row from L2.  A partition whose keys overflow
+//     the tables is split again by further hash bits and rescanned.
+//
+// Each CTA evaluates its own table (FP32 pre-filter, exact FP64 values of the
+// survivors, argmax by value desc / id asc); for big hubs the CTAs' partial
+// bests are combined by the hub's last CTA (atomic counter).  No global hash
+// tables, no spin-waits.
 #pragma once
 
 #include "engine.cuh"
 
 namespace pcc {
 
-constexpr uint32_t kHubMinDegree = 1000;  // hub = degree > 1000
-constexpr uint32_t kHubSlots = 4096;      // shared table capacity per CTA
-constexpr uint32_t kHubPartKeys = 2048;   // expected distinct keys per partition
+constexpr uint32_t kHubMinDegree = 1000;      // hub = degree > 1000
+constexpr uint32_t kHubSmallMax = 4096;       // one-CTA hubs
+constexpr uint32_t kHubSlots = 8192;          // shared table slots per CTA
+constexpr uint32_t kHubClusterSize = 8;       // CTAs per big-hub cluster
+constexpr uint32_t kHubClusterKeys = kHubSlots / 2 * kHubClusterSize;  // keys per partition
 
 // Static part (depends on the graph only).
 struct HubPlan {
   uint32_t num_hubs = 0;
-  uint32_t num_items = 0;
-  uint64_t num_partials = 0;
-  DBuf<uint32_t> hub_v;       // hub vertex ids
-  DBuf<uint32_t> hub_parts;   // P per hub
-  DBuf<uint32_t> hub_pbase;   // first partial of the hub
-  DBuf<uint32_t> item_hub;    // work items, largest hubs first
+  uint32_t num_small = 0;      // hubs with degree <= kHubSmallMax
+  uint32_t num_big = 0;
+  uint32_t num_items = 0;      // big-hub work items (hub, partition)
+  uint64_t num_partials = 0;   // kHubClusterSize per big-hub item
+  DBuf<uint32_t> small_v;      // small hubs, largest first
+  DBuf<uint32_t> big_v;        // big hubs, largest first
+  DBuf<uint32_t> big_parts;    // P per big hub
+  DBuf<uint32_t> big_pbase;    // first partial of the big hub
+  DBuf<uint32_t> item_hub;     // work items, largest hubs first
   DBuf<uint32_t> item_part;
 };
 
@@ -48,6 +57,9 @@ struct HubState {
 
 Status BuildHubPlan(Context* ctx, const DevGraph& g, const BinSet& bins, HubPlan* plan);
 Status AllocHubState(Context* ctx, const HubPlan& plan, HubState* st);
-Status LaunchHubBestMoves(Context* ctx, const BMArgs& a, const HubPlan& plan, HubState& st, bool int_mode);
+// narrow: INT mode with every neighbour-cluster sum below 2^31 in
+// magnitude, so the tables hold 32-bit sums.
+Status LaunchHubBestMoves(Context* ctx, const BMArgs& a, const HubPlan& plan, HubState& st, bool int_mode,
+                          bool narrow);
 
 }  // namespace pcc

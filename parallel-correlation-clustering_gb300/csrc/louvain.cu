@@ -364,6 +364,12 @@ struct RunResult {
   uint64_t algo_bytes = 0;
 };
 
+// INT mode with every neighbour-cluster sum below 2^31 in magnitude: a
+// cluster sum is at most the row's sum of |w| plus degree * |offset|.
+bool NarrowSums(const DevGraph& g, double offset) {
+  return g.row_abs_bound + std::fabs(offset) * static_cast<double>(g.max_deg) < 2147483647.0;
+}
+
 bool IntModeFor(const DevGraph& g, double offset) {
   if (!g.integral) return false;
   if (offset != std::floor(offset) || std::fabs(offset) > 4194304.0) return false;
@@ -476,6 +482,7 @@ class Engine {
     a.Kf = L->Kf.p;
     a.kf = L->kf.p;
     a.int_nw = int_nw_ ? 1 : 0;
+    a.narrow = (L->int_mode && NarrowSums(g, cfg_.edge_weight_offset)) ? 1 : 0;
     a.res = cfg_.resolution;
     a.res32 = FilterF32(cfg_.resolution);
     a.offset = cfg_.edge_weight_offset;
@@ -496,7 +503,7 @@ class Engine {
     timer_.Begin(kPhaseBestMoves);
     PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx_, a, bins.list.p, bins.counts.p, bins.counts.p + kNumBins,
                                         bins.host_counts, L->int_mode, g.max_deg));
-    PCC_RETURN_IF_ERROR(LaunchHubBestMoves(ctx_, a, *g.hub_plan, hub_state_, L->int_mode));
+    PCC_RETURN_IF_ERROR(LaunchHubBestMoves(ctx_, a, *g.hub_plan, hub_state_, L->int_mode, a.narrow != 0));
     timer_.End(kPhaseBestMoves);
 
     timer_.Begin(kPhaseApply);
@@ -1039,6 +1046,7 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   a.Kf = dKf.p;
   a.kf = dkf.p;
   a.int_nw = IntegralWeights(k, n) ? 1 : 0;
+  a.narrow = (IntModeFor(g, config->edge_weight_offset) && NarrowSums(g, config->edge_weight_offset)) ? 1 : 0;
   a.res = config->resolution;
   a.res32 = FilterF32(config->resolution);
   a.offset = config->edge_weight_offset;
@@ -1056,7 +1064,8 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   const BinSet& ab = g.bins_all;
   PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx, a, ab.list.p, ab.counts.p, ab.counts.p + kNumBins, ab.host_counts,
                                       IntModeFor(g, config->edge_weight_offset), g.max_deg));
-  PCC_RETURN_IF_ERROR(LaunchHubBestMoves(ctx, a, *g.hub_plan, hs, IntModeFor(g, config->edge_weight_offset)));
+  const bool im = IntModeFor(g, config->edge_weight_offset);
+  PCC_RETURN_IF_ERROR(LaunchHubBestMoves(ctx, a, *g.hub_plan, hs, im, im && NarrowSums(g, config->edge_weight_offset)));
   PCC_RETURN_IF_ERROR(dt.ToHost(out_t, n));
   PCC_RETURN_IF_ERROR(dv.ToHost(out_v, n));
   if (out_moves) PCC_RETURN_IF_ERROR(dm.ToHost(out_moves, n));
