@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
     const bool leader = cand && int(lane) == __ffs(peers) - 1;
     double S;
     if (kInt) {
-      const int xi = cand ? (static_cast<int>(wt) - a.ioffset) : 0;
+      const int xi = cand ? (WeightToInt(wt) - a.ioffset) : 0;
       S = static_cast<double>(GroupSumInt(peers, xi, a.w == nullptr, leader, reinterpret_cast<int*>(stage[warp])));
     } else {
       stage[warp][lane] = cand ? Dsub(static_cast<double>(wt), a.offset) : 0.0;
@@ -140,6 +140,7 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
 // which keeps the reference's adjacency-order summation exactly.
 // ---------------------------------------------------------------------------
 constexpr int kWarpKernelWarps = 4;
+constexpr int kCertUnroll = 4;  // chunks of 32 entries loaded together
 
 template <int HC>
 constexpr size_t WarpKernelSmem() {
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
         if (ins) used[base + __popc(im & LaneMaskLt())] = static_cast<uint16_t>(slot);
       }
       if (kInt) {
-        const int xi = cand ? (static_cast<int>(wt) - a.ioffset) : 0;
+        const int xi = cand ? (WeightToInt(wt) - a.ioffset) : 0;
         const int S = GroupSumInt(peers, xi, a.w == nullptr, leader, reinterpret_cast<int*>(stage));
         if (slot != kNone) vals[slot] += static_cast<unsigned long long>(static_cast<long long>(S));
       } else {
@@ -308,6 +309,78 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
 // -- the exact FP64 values decide; in replay mode a certified decision that
 // differs from the FP64 one raises kErrCertMismatch (a self-check).
 // ---------------------------------------------------------------------------
+// Exact FP64 fallbacks of the certified kernels.  They are separate
+// non-inlined functions so that the compiler cannot hoist their FP64
+// arithmetic onto the certified path (an FP64 warp instruction costs ~19
+// SM cycles on this GPU).  Both return whether the vertex must be appended
+// to the movers list; in replay mode they also run the self-check.
+template <int G>
+__device__ __noinline__ bool GroupExact(const BMArgs& a, const VertexCtx& x, bool fp64, bool contender, unsigned gl,
+                                        int T, int S, double KD, uint32_t cu, bool replay, int cres,
+                                        uint32_t cmove) {
+  double change = 0.0, val = -CUDART_INF;
+  uint32_t id = kNone;
+  if (fp64) {
+    change = ChangeOf(a, x, static_cast<double>(T));
+    if (contender) {
+      val = ValOf(a, x.kv, change, static_cast<double>(S), KD);
+      id = cu;
+    }
+  }
+#pragma unroll
+  for (int o = G / 2; o >= 1; o >>= 1) {
+    const double ov = __shfl_xor_sync(kFull, val, o);
+    const uint32_t oid = __shfl_xor_sync(kFull, id, o);
+    if (Better(ov, oid, val, id)) {
+      val = ov;
+      id = oid;
+    }
+  }
+  bool append = false;
+  if (fp64 && gl == 0) {
+    append = Decide<false>(a, x, val, id, change);
+    if (replay && cres != kUncertain && a.out_moves && a.out_moves[x.v] != cmove)
+      atomicExch(&a.ctr->error, kErrCertMismatch);
+  }
+  return append;
+}
+
+template <int HC, typename V>
+__device__ __noinline__ bool WarpExact(const BMArgs& a, const VertexCtx& x, V T, const uint32_t* keys,
+                                       const V* vals, const uint16_t* used, uint32_t nused, bool replay, int cres,
+                                       uint32_t cmove) {
+  const unsigned lane = LaneId();
+  const double change = ChangeOf(a, x, static_cast<double>(T));
+  double best = -CUDART_INF;
+  uint32_t bid = kNone;
+  for (uint32_t i = lane; i < nused; i += 32) {
+    const uint32_t slot = used[i];
+    if (slot == 0xFFFFu) continue;
+    const uint32_t key = keys[slot];
+    const double val = ValOf(a, x.kv, change, static_cast<double>(vals[slot]), a.K[key]);
+    if (Better(val, key, best, bid)) {
+      best = val;
+      bid = key;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const double ov = __shfl_xor_sync(kFull, best, o);
+    const uint32_t oid = __shfl_xor_sync(kFull, bid, o);
+    if (Better(ov, oid, best, bid)) {
+      best = ov;
+      bid = oid;
+    }
+  }
+  bool append = false;
+  if (lane == 0) {
+    append = Decide<false>(a, x, best, bid, change);
+    if (replay && cres != kUncertain && a.out_moves && a.out_moves[x.v] != cmove)
+      atomicExch(&a.ctr->error, kErrCertMismatch);
+  }
+  return append;
+}
+
 template <int G>
 __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t* __restrict__ list,
                                                       const uint32_t* __restrict__ bin_counts,
@@ -322,15 +395,19 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
   const bool replay = a.out_target != nullptr;
   const bool unit = a.w == nullptr;
   const uint64_t stride = uint64_t(gridDim.x) * 8 * kVpw;
-  for (uint64_t base = (uint64_t(blockIdx.x) * 8 + warp) * kVpw; base < count; base += stride) {
+  // Vertex ids are loaded one iteration ahead (latency-bound kernel).
+  uint64_t base = (uint64_t(blockIdx.x) * 8 + warp) * kVpw;
+  uint32_t vid = base + g < count ? list[start + base + g] : 0u;
+  for (; base < count; base += stride) {
     const uint64_t idx = base + g;
+    const uint32_t nvid = base + stride + g < count ? list[start + base + stride + g] : 0u;
     bool vvalid = idx < count;
     VertexCtx x{};
     if (vvalid) {
-      const uint32_t v = list[start + idx];
-      vvalid = InFront(a, v);
-      if (vvalid) x = LoadVertex<false>(a, v);
+      vvalid = InFront(a, vid);
+      if (vvalid) x = LoadVertex<false>(a, vid);
     }
+    vid = nvid;
     if (__ballot_sync(kFull, vvalid) == 0) continue;
     const bool has = vvalid && gl < x.d;
     uint32_t u = x.v;
@@ -343,17 +420,17 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
     const uint32_t cu = cand ? __ldg(a.C + u) : kNone;
     const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane)) & gmask;
     const bool leader = cand && int(lane) == __ffs(peers) - 1;
-    const int xi = cand ? (static_cast<int>(wt) - a.ioffset) : 0;
+    const int xi = cand ? (WeightToInt(wt) - a.ioffset) : 0;
     const int S = GroupSumInt(peers, xi, unit, leader, stage[warp]);
     const unsigned tmask = __ballot_sync(kFull, leader && cu == x.c) & gmask;
     const int Tsh = __shfl_sync(kFull, S, tmask ? __ffs(tmask) - 1 : int(lane));
-    const long long T = tmask ? Tsh : 0;
+    const int T = tmask ? Tsh : 0;  // group sums stay below 2^29 in INT mode
     int smax = leader ? S : INT_MIN;
 #pragma unroll
     for (int o = G / 2; o >= 1; o >>= 1) smax = max(smax, __shfl_xor_sync(kFull, smax, o));
     const float k32 = vvalid ? a.kf[x.v] : 0.f;
     const float Kc32 = vvalid ? a.Kf[x.c] : 0.f;
-    const ChangeApprox ca = ApproxChange(a.res32, a.int_nw != 0, k32, Kc32, T);
+    const ChangeApproxT<int> ca = ApproxChange<int>(a.res32, a.int_nw != 0, k32, Kc32, T);
     const float cabs = ChangeAbsBound(ca);
     // FP32 pre-filter over the group's leaders.
     FilterVal f{0.f, 0.f, false};
@@ -361,7 +438,7 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
     float lo = -CUDART_INF_F;
     if (leader) {
       KfD = a.Kf[cu];
-      f = FilterOf(a.res32, k32, KfD, S, smax, cabs);
+      f = FilterOf<int>(a.res32, k32, KfD, S, smax, cabs);
       if (f.sane) lo = __fsub_rn(f.Y, f.e);
     }
     float U = lo;
@@ -369,13 +446,13 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
     for (int o = G / 2; o >= 1; o >>= 1) U = fmaxf(U, __shfl_xor_sync(kFull, U, o));
     const bool contender = leader && (!f.sane || __fadd_rn(f.Y, f.e) >= U);
     // The leading (S, K) class of the contenders and the trailing one.
-    LexKey lead, tail;
+    LexKeyT<int> lead, tail;
     double KD = 0.0;
     if (contender) {
       KD = a.K[cu];
       const unsigned long long ko = KOrder(KD);
       lead.Keep(S, ko, cu);
-      tail.Keep(-static_cast<long long>(S), ~ko, cu);
+      tail.Keep(-S, ~ko, cu);
     }
     LexGroupReduce<G>(lead);
     LexGroupReduce<G>(tail);
@@ -384,37 +461,15 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
     uint32_t ctarget = kNone;
     if (vvalid && single) {
       const float KfA = lead.id != kNone ? a.Kf[lead.id] : 0.f;
-      cres = CertifyDecision(ca, a.res32, k32, lead.id != kNone, lead.S, KfA, lead.id, a.n, &ctarget);
+      cres = CertifyDecision<int>(ca, a.res32, k32, lead.id != kNone, lead.S, KfA, lead.id, a.n, &ctarget);
     }
     const uint32_t cmove = cres == kUncertain ? kNone : CertifiedMove(a, x, ctarget, cres == kCertMove);
     const bool fp64 = vvalid && (replay || cres == kUncertain);
     bool append = false;
     if (vvalid && !fp64 && gl == 0) append = ApplyCertified(a, x, cmove);
     if (__ballot_sync(kFull, fp64)) {
-      // Exact path: FP64 change and values of the contenders.
-      double change = 0.0, val = -CUDART_INF;
-      uint32_t id = kNone;
-      if (fp64) {
-        change = ChangeOf(a, x, static_cast<double>(T));
-        if (contender) {
-          val = ValOf(a, x.kv, change, static_cast<double>(S), KD);
-          id = cu;
-        }
-      }
-#pragma unroll
-      for (int o = G / 2; o >= 1; o >>= 1) {
-        const double ov = __shfl_xor_sync(kFull, val, o);
-        const uint32_t oid = __shfl_xor_sync(kFull, id, o);
-        if (Better(ov, oid, val, id)) {
-          val = ov;
-          id = oid;
-        }
-      }
-      if (fp64 && gl == 0) {
-        append = Decide<false>(a, x, val, id, change);
-        if (replay && cres != kUncertain && a.out_moves && a.out_moves[x.v] != cmove)
-          atomicExch(&a.ctr->error, kErrCertMismatch);
-      }
+      const bool app = GroupExact<G>(a, x, fp64, contender, gl, T, S, KD, cu, replay, cres, cmove);
+      append = append || app;
     }
     const uint32_t slot = WarpAppendFull(&a.ctr->movers, append);
     if (append) a.movers[slot] = x.v;
@@ -456,22 +511,43 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
   }
   if (lane == 0) *used_count = 0;
   __syncwarp();
-  for (uint64_t idx = uint64_t(blockIdx.x) * kWarpKernelWarps + warp; idx < count;
-       idx += uint64_t(gridDim.x) * kWarpKernelWarps) {
-    const uint32_t vid = list[start + idx];
-    if (!InFront(a, vid)) continue;
+  // The next vertex id is loaded one iteration ahead, and each vertex's
+  // entries are loaded kCertUnroll chunks at a time (up to 128 neighbour ids
+  // and their cluster ids in flight per warp): the kernel is bound by the
+  // latency of the dependent loads list -> offsets -> neighbours -> clusters.
+  const uint64_t wstride = uint64_t(gridDim.x) * kWarpKernelWarps;
+  uint64_t idx = uint64_t(blockIdx.x) * kWarpKernelWarps + warp;
+  uint32_t vid = idx < count ? list[start + idx] : 0u;
+  for (; idx < count; idx += wstride) {
+    const uint64_t nidx = idx + wstride;
+    const uint32_t nvid = nidx < count ? list[start + nidx] : 0u;
+    if (!InFront(a, vid)) {
+      vid = nvid;
+      continue;
+    }
     const VertexCtx x = LoadVertex<false>(a, vid);
-    for (uint32_t e0 = 0; e0 < x.d; e0 += 32) {
-      const uint32_t e = e0 + lane;
-      const bool has = e < x.d;
-      uint32_t u = x.v;
-      float wt = 0.f;
-      if (has) {
-        u = a.nbr[x.b + e];
-        wt = a.w ? a.w[x.b + e] : 1.0f;
+    vid = nvid;
+    for (uint32_t e0 = 0; e0 < x.d; e0 += 32 * kCertUnroll) {
+      uint32_t uu[kCertUnroll], cc[kCertUnroll];
+      float ww[kCertUnroll];
+#pragma unroll
+      for (int k = 0; k < kCertUnroll; ++k) {
+        const uint32_t e = e0 + 32 * k + lane;
+        uu[k] = x.v;
+        ww[k] = 0.f;
+        if (e < x.d) {
+          uu[k] = a.nbr[x.b + e];
+          ww[k] = a.w ? a.w[x.b + e] : 1.0f;
+        }
       }
-      const bool cand = has && u != x.v;
-      const uint32_t cu = cand ? __ldg(a.C + u) : kNone;
+#pragma unroll
+      for (int k = 0; k < kCertUnroll; ++k) cc[k] = uu[k] != x.v ? __ldg(a.C + uu[k]) : kNone;
+#pragma unroll
+      for (int k = 0; k < kCertUnroll; ++k) {
+      if (e0 + 32 * k >= x.d) break;  // warp-uniform
+      const float wt = ww[k];
+      const bool cand = uu[k] != x.v;
+      const uint32_t cu = cc[k];
       const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane));
       const bool leader = cand && int(lane) == __ffs(peers) - 1;
       uint32_t slot = kNone;
@@ -488,12 +564,13 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
         b0 = __shfl_sync(kFull, b0, ld);
         if (ins) used[b0 + __popc(im & LaneMaskLt())] = static_cast<uint16_t>(slot);
       }
-      const int xi = cand ? (static_cast<int>(wt) - a.ioffset) : 0;
+      const int xi = cand ? (WeightToInt(wt) - a.ioffset) : 0;
       const int Sg = GroupSumInt(peers, xi, unit, leader, stage);
       if (slot != kNone) vals[slot] += static_cast<V>(Sg);
       __syncwarp();
+      }
     }
-    long long T = 0;
+    V T = 0;
     if (lane == 0) {
       const uint32_t slot = FindT<false>(keys, HC, x.c);
       if (slot != kNone) T = vals[slot];
@@ -501,26 +578,26 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     T = __shfl_sync(kFull, T, 0);
     const uint32_t nused = *used_count;
     const float k32 = a.kf[x.v];
-    const ChangeApprox ca = ApproxChange(a.res32, a.int_nw != 0, k32, a.Kf[x.c], T);
+    const ChangeApproxT<V> ca = ApproxChange<V>(a.res32, a.int_nw != 0, k32, a.Kf[x.c], T);
     const float cabs = ChangeAbsBound(ca);
     V vmax = sizeof(V) == 4 ? V(INT_MIN) : V(LLONG_MIN);
     for (uint32_t i = lane; i < nused; i += 32) vmax = max(vmax, vals[used[i]]);
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) vmax = max(vmax, __shfl_xor_sync(kFull, vmax, o));
-    const long long smax = vmax;
+    const V smax = vmax;
     float U = -CUDART_INF_F;
     for (uint32_t i = lane; i < nused; i += 32) {
       const uint32_t slot = used[i];
-      const FilterVal f = FilterOf(a.res32, k32, a.Kf[keys[slot]], vals[slot], smax, cabs);
+      const FilterVal f = FilterOf<V>(a.res32, k32, a.Kf[keys[slot]], vals[slot], smax, cabs);
       if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
     }
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) U = fmaxf(U, __shfl_xor_sync(kFull, U, o));
-    LexKey lead, tail;
+    LexKeyT<V> lead, tail;
     for (uint32_t i = lane; i < nused; i += 32) {
       const uint32_t slot = used[i];
       const uint32_t key = keys[slot];
-      const FilterVal f = FilterOf(a.res32, k32, a.Kf[key], vals[slot], smax, cabs);
+      const FilterVal f = FilterOf<V>(a.res32, k32, a.Kf[key], vals[slot], smax, cabs);
       if (f.sane && __fadd_rn(f.Y, f.e) < U) {
         keys[slot] = kNone;  // not a contender: cleared now, skipped later
         vals[slot] = 0;
@@ -528,7 +605,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
         continue;
       }
       const unsigned long long ko = KOrder(a.K[key]);
-      const long long S = vals[slot];
+      const V S = vals[slot];
       lead.Keep(S, ko, key);
       tail.Keep(-S, ~ko, key);
     }
@@ -539,39 +616,12 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     uint32_t ctarget = kNone;
     if (single) {
       const float KfA = lead.id != kNone ? a.Kf[lead.id] : 0.f;
-      cres = CertifyDecision(ca, a.res32, k32, lead.id != kNone, lead.S, KfA, lead.id, a.n, &ctarget);
+      cres = CertifyDecision<V>(ca, a.res32, k32, lead.id != kNone, lead.S, KfA, lead.id, a.n, &ctarget);
     }
     const uint32_t cmove = cres == kUncertain ? kNone : CertifiedMove(a, x, ctarget, cres == kCertMove);
     bool append = false;
     if (replay || cres == kUncertain) {
-      // Exact path over the contenders (warp-uniform branch).
-      const double change = ChangeOf(a, x, static_cast<double>(T));
-      double best = -CUDART_INF;
-      uint32_t bid = kNone;
-      for (uint32_t i = lane; i < nused; i += 32) {
-        const uint32_t slot = used[i];
-        if (slot == 0xFFFFu) continue;
-        const uint32_t key = keys[slot];
-        const double val = ValOf(a, x.kv, change, static_cast<double>(vals[slot]), a.K[key]);
-        if (Better(val, key, best, bid)) {
-          best = val;
-          bid = key;
-        }
-      }
-#pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) {
-        const double ov = __shfl_xor_sync(kFull, best, o);
-        const uint32_t oid = __shfl_xor_sync(kFull, bid, o);
-        if (Better(ov, oid, best, bid)) {
-          best = ov;
-          bid = oid;
-        }
-      }
-      if (lane == 0) {
-        append = Decide<false>(a, x, best, bid, change);
-        if (replay && cres != kUncertain && a.out_moves && a.out_moves[x.v] != cmove)
-          atomicExch(&a.ctr->error, kErrCertMismatch);
-      }
+      append = WarpExact<HC, V>(a, x, T, keys, vals, used, nused, replay, cres, cmove);
     } else if (lane == 0) {
       append = ApplyCertified(a, x, cmove);
     }

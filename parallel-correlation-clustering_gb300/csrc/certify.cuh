@@ -47,11 +47,23 @@ constexpr float kU48 = 3.552713678800501e-15f;  // 2^-48
 constexpr float kU50 = 8.881784197001252e-16f;  // 2^-50
 constexpr float kTwo24 = 16777216.0f;
 
-// int64 -> float through the 32-bit conversion when the value fits (the
-// 64-bit conversion is far slower on this GPU).
-__device__ __forceinline__ float I2F(long long x) {
-  return (x >= INT_MIN && x <= INT_MAX) ? __int2float_rn(static_cast<int>(x)) : __ll2float_rn(x);
+// Integer -> float.  The kernels keep sums in int when they are narrow
+// (every sum and difference below 2^31 in magnitude) and convert them with
+// integer and FP32 arithmetic only: conversion instructions run on this
+// GPU's slow double-precision path.  For |y| < 2^22 the float with bit
+// pattern 0x4B400000 + y is exactly 1.5 * 2^23 + y (the ulp there is 1), so
+// subtracting 1.5 * 2^23 gives y exactly.  x = hi * 2^16 + lo with both
+// halves in that range; hi * 2^16 is exact and the final addition rounds
+// once, so the result is x correctly rounded, like __int2float_rn.
+__device__ __forceinline__ float SmallIntToFloat(int y) {
+  return __fsub_rn(__int_as_float(0x4B400000 + y), 12582912.0f);
 }
+__device__ __forceinline__ float I2F(int x) {
+  const float fh = SmallIntToFloat(x >> 16);
+  const float fl = SmallIntToFloat(x & 0xFFFF);
+  return __fadd_rn(__fmul_rn(fh, 65536.0f), fl);
+}
+__device__ __forceinline__ float I2F(long long x) { return __ll2float_rn(x); }
 
 __device__ __forceinline__ bool SaneF(float z) {
   const float m = fabsf(z);
@@ -68,11 +80,12 @@ __device__ __forceinline__ unsigned long long KOrder(double d) {
 
 // (S desc, K asc, id asc) lexicographic leader of the filter's survivors;
 // id kNone = none.
-struct LexKey {
-  long long S = LLONG_MIN;
+template <typename I>
+struct LexKeyT {
+  I S = sizeof(I) == 4 ? I(INT_MIN) : I(LLONG_MIN);
   unsigned long long K = ~0ull;
   uint32_t id = kNone;
-  __device__ __forceinline__ void Keep(long long s, unsigned long long k, uint32_t i) {
+  __device__ __forceinline__ void Keep(I s, unsigned long long k, uint32_t i) {
     if (i == kNone) return;
     if (id == kNone || s > S || (s == S && (k < K || (k == K && i < id)))) {
       S = s;
@@ -83,11 +96,13 @@ struct LexKey {
 };
 
 // Butterfly over lane groups of G lanes (G = 32: the warp).
-template <int G>
-__device__ __forceinline__ void LexGroupReduce(LexKey& x) {
+using LexKey = LexKeyT<long long>;
+
+template <int G, typename I>
+__device__ __forceinline__ void LexGroupReduce(LexKeyT<I>& x) {
 #pragma unroll
   for (int o = G / 2; o >= 1; o >>= 1) {
-    const long long s = __shfl_xor_sync(kFull, x.S, o);
+    const I s = __shfl_xor_sync(kFull, x.S, o);
     const unsigned long long k = __shfl_xor_sync(kFull, x.K, o);
     const uint32_t i = __shfl_xor_sync(kFull, x.id, o);
     x.Keep(s, k, i);
@@ -104,8 +119,8 @@ struct FilterVal {
   bool sane;
 };
 
-__device__ __forceinline__ FilterVal FilterOf(float r32, float k32, float KfD, long long S, long long Smax,
-                                              float change32) {
+template <typename I>
+__device__ __forceinline__ FilterVal FilterOf(float r32, float k32, float KfD, I S, I Smax, float change32) {
   FilterVal f;
   const float R = __fmul_rn(r32, __fmul_rn(k32, KfD));
   f.Y = __fsub_rn(I2F(S - Smax), R);
@@ -119,15 +134,17 @@ enum CertResult : int { kCertNoMove = 0, kCertMove = 1, kUncertain = 2 };
 
 // FP32 approximation of change = 0 - (T - res*(kv*(K_c - kv))) and its
 // bound; ok = false when the inputs leave the relative-error model.
-struct ChangeApprox {
+template <typename I>
+struct ChangeApproxT {
   float ch, ec;  // change' and its bound
   float M, eM;   // res*kv*(K_c - kv) in FP32 and its bound
-  long long T;
+  I T;
   bool ok;
 };
 
-__device__ __forceinline__ ChangeApprox ApproxChange(float r32, bool int_nw, float k32, float Kc32, long long T) {
-  ChangeApprox c;
+template <typename I>
+__device__ __forceinline__ ChangeApproxT<I> ApproxChange(float r32, bool int_nw, float k32, float Kc32, I T) {
+  ChangeApproxT<I> c;
   const float diff = __fsub_rn(Kc32, k32);
   const bool kc_exact = int_nw && fabsf(Kc32) < kTwo24;
   const bool kv_exact = int_nw && fabsf(k32) < kTwo24;
@@ -151,16 +168,17 @@ __device__ __forceinline__ ChangeApprox ApproxChange(float r32, bool int_nw, flo
 
 // An upper bound of |change| for FilterBound's absolute term (inf when the
 // approximation is not usable, which keeps every candidate).
-__device__ __forceinline__ float ChangeAbsBound(const ChangeApprox& c) {
+template <typename I>
+__device__ __forceinline__ float ChangeAbsBound(const ChangeApproxT<I>& c) {
   return c.ok ? __fmul_rn(__fadd_rn(fabsf(c.ch), c.ec), 1.0001f) : CUDART_INF_F;
 }
 
 // Certifies the decision given the single-class winner A (has_cand) or no
 // candidate at all.  *target receives the target (n = new cluster) when the
 // result is kCertMove.
-__device__ __forceinline__ int CertifyDecision(const ChangeApprox& c, float r32, float k32, bool has_cand,
-                                               long long SA, float KfA, uint32_t idA, uint32_t n,
-                                               uint32_t* target) {
+template <typename I>
+__device__ __forceinline__ int CertifyDecision(const ChangeApproxT<I>& c, float r32, float k32, bool has_cand,
+                                               I SA, float KfA, uint32_t idA, uint32_t n, uint32_t* target) {
   if (!c.ok) return kUncertain;
   if (has_cand) {
     const float RA = __fmul_rn(r32, __fmul_rn(k32, KfA));
@@ -175,8 +193,8 @@ __device__ __forceinline__ int CertifyDecision(const ChangeApprox& c, float r32,
       // is that of (S_A - T) + (M - R_A): the integer part is exact, so the
       // bound carries only the FP32 error of M and R_A (a vertex tied
       // between its own cluster and A has S_A = T and a tiny value).
-      const long long I = SA - c.T;
-      const float I32 = I2F(I);
+      const I dI = SA - c.T;
+      const float I32 = I2F(dI);
       const float mr = __fsub_rn(c.M, RA);
       const float vs = __fadd_rn(I32, mr);
       float ev = __fadd_rn(__fadd_rn(c.eM, __fmul_rn(kU21, fabsf(RA))),

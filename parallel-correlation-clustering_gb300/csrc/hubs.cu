@@ -4,8 +4,6 @@
 // any order (the reference adds concurrently), FP64-mode weights rounded to
 // float after the offset, the argmax by (value desc, id asc), and "no
 // entries" giving the reduce identity (0, 0.0) unless change >= 0.
-#include <cooperative_groups.h>
-
 #include <algorithm>
 #include <numeric>
 #include <type_traits>
@@ -15,16 +13,21 @@
 #include "hubs.cuh"
 #include "moves.cuh"
 
-namespace cg = cooperative_groups;
-
 namespace pcc {
 namespace {
 
-constexpr int kHT = 256;                   // threads per hub CTA
-constexpr int kHW = kHT / 32;
 constexpr int kHubUnroll = 4;              // entries per thread in flight
 constexpr uint32_t kHubMaxSub = 1u << 12;  // sub-partitions before giving up
 constexpr uint32_t kMaxCont = 256;         // contender list per CTA
+
+constexpr int kSmallThreads = 256;         // small hubs: CTA size, table slots
+constexpr uint32_t kSmallSlots = 2 * kHubSmallMax;
+constexpr int kBigThreads = 1024;          // big hubs
+// Big-hub table: ~192 KB of (key, sum) slots.
+template <typename V>
+__host__ __device__ constexpr uint32_t BigSlots() {
+  return sizeof(V) == 4 ? 2 * kHubBigKeys : 16384;
+}
 
 struct HubArgs {
   BMArgs a;
@@ -42,8 +45,9 @@ struct HubArgs {
 };
 
 // MurmurHash3's 32-bit finalizer (a bijection; every output bit depends on
-// every input bit).  Low bits pick the slot, bits 13..15 the owning CTA of a
-// cluster, bits 16.. the sub-partition, the top bits the partition.
+// every input bit).  The product with the capacity's high half picks the
+// slot, bits 8..19 the sub-partition, the top bits (again through a
+// product) the partition.
 __device__ __forceinline__ uint32_t Mix32(uint32_t x) {
   x ^= x >> 16;
   x *= 0x85EBCA6Bu;
@@ -51,6 +55,11 @@ __device__ __forceinline__ uint32_t Mix32(uint32_t x) {
   x *= 0xC2B2AE35u;
   x ^= x >> 16;
   return x;
+}
+
+__device__ __forceinline__ uint32_t SlotHash(uint32_t cu) {
+  // A second mix so that the slot is independent of the partition bits.
+  return Mix32(cu ^ 0x9E3779B9u);
 }
 
 __device__ __forceinline__ void KeepBest(double& bv, uint32_t& bi, double v, uint32_t i) {
@@ -75,12 +84,28 @@ __device__ __forceinline__ V AtomicAddV(V* p, V x) {
   }
 }
 
-template <typename V>
-__device__ __forceinline__ double VToDouble(V x) {
-  return static_cast<double>(x);
-}
+// Shared scratch of a hub CTA of BT threads besides its table.
+template <int BT>
+struct HubShared {
+  static constexpr int kW = BT / 32;
+  long long red_ll[kW];
+  unsigned long long red_k[kW];
+  double red_d[kW];
+  float red_f[kW];
+  uint32_t red_i[kW];
+  int stage_i[kW][32];
+  double stage_d[kW][32];
+  uint32_t cont_key[kMaxCont];
+  long long cont_S[kMaxCont];
+  uint32_t ncont;
+  uint32_t overflow;
+  uint32_t nkeys;
+  double change;
+  float change32;
+};
 
 // Block reductions; every thread receives the result.
+template <int BT>
 __device__ __forceinline__ long long BlockMaxLL(long long x, long long* red) {
 #pragma unroll
   for (int o = 16; o; o >>= 1) x = max(x, __shfl_xor_sync(kFull, x, o));
@@ -88,11 +113,12 @@ __device__ __forceinline__ long long BlockMaxLL(long long x, long long* red) {
   __syncthreads();
   long long r = red[0];
 #pragma unroll
-  for (int w = 1; w < kHW; ++w) r = max(r, red[w]);
+  for (int w = 1; w < BT / 32; ++w) r = max(r, red[w]);
   __syncthreads();
   return r;
 }
 
+template <int BT>
 __device__ __forceinline__ float BlockMaxF(float x, float* red) {
 #pragma unroll
   for (int o = 16; o; o >>= 1) x = fmaxf(x, __shfl_xor_sync(kFull, x, o));
@@ -100,13 +126,13 @@ __device__ __forceinline__ float BlockMaxF(float x, float* red) {
   __syncthreads();
   float r = red[0];
 #pragma unroll
-  for (int w = 1; w < kHW; ++w) r = fmaxf(r, red[w]);
+  for (int w = 1; w < BT / 32; ++w) r = fmaxf(r, red[w]);
   __syncthreads();
   return r;
 }
 
 // Deterministic sum: butterfly inside warps, then the warps in order.
-template <class T>
+template <int BT, class T>
 __device__ __forceinline__ T BlockSum(T x, T* red) {
 #pragma unroll
   for (int o = 16; o; o >>= 1) {
@@ -120,7 +146,7 @@ __device__ __forceinline__ T BlockSum(T x, T* red) {
   __syncthreads();
   T r = red[0];
 #pragma unroll
-  for (int w = 1; w < kHW; ++w) {
+  for (int w = 1; w < BT / 32; ++w) {
     if constexpr (std::is_floating_point<T>::value) {
       r = Dadd(r, red[w]);
     } else {
@@ -131,48 +157,70 @@ __device__ __forceinline__ T BlockSum(T x, T* red) {
   return r;
 }
 
-__device__ __forceinline__ void BlockArgmax(double& v, uint32_t& id, double* redv, uint32_t* redi) {
+// Argmax over (value desc, id asc) with integer compares: the values are
+// mapped to order-preserving 64-bit images (no FP64 instruction; the values
+// here are never -0, the only case where the image order and IEEE equality
+// differ).
+__device__ __forceinline__ unsigned long long ValBits(double d) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(d));
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double BitsVal(unsigned long long k) {
+  const unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+  return __longlong_as_double(static_cast<long long>(b));
+}
+__device__ __forceinline__ void KeepBits(unsigned long long& bo, uint32_t& bi, unsigned long long o, uint32_t i) {
+  if (i == kNone) return;
+  if (bi == kNone || o > bo || (o == bo && i < bi)) {
+    bo = o;
+    bi = i;
+  }
+}
+
+template <int BT>
+__device__ __forceinline__ void BlockArgmax(double& v, uint32_t& id, unsigned long long* redv, uint32_t* redi) {
+  unsigned long long o = ValBits(v);
 #pragma unroll
-  for (int o = 16; o; o >>= 1) {
-    const double ov = __shfl_xor_sync(kFull, v, o);
-    const uint32_t oi = __shfl_xor_sync(kFull, id, o);
-    KeepBest(v, id, ov, oi);
+  for (int off = 16; off; off >>= 1) {
+    const unsigned long long oo = __shfl_xor_sync(kFull, o, off);
+    const uint32_t oi = __shfl_xor_sync(kFull, id, off);
+    KeepBits(o, id, oo, oi);
   }
   if (LaneId() == 0) {
-    redv[threadIdx.x >> 5] = v;
+    redv[threadIdx.x >> 5] = o;
     redi[threadIdx.x >> 5] = id;
   }
   __syncthreads();
-  double rv = redv[0];
+  unsigned long long ro = redv[0];
   uint32_t ri = redi[0];
 #pragma unroll
-  for (int w = 1; w < kHW; ++w) KeepBest(rv, ri, redv[w], redi[w]);
+  for (int w = 1; w < BT / 32; ++w) KeepBits(ro, ri, redv[w], redi[w]);
   __syncthreads();
-  v = rv;
+  v = BitsVal(ro);
   id = ri;
 }
 
-__device__ __forceinline__ LexKey BlockLex(LexKey x, long long* rs, unsigned long long* rk, uint32_t* ri) {
-  LexGroupReduce<32>(x);
+template <int BT, typename I>
+__device__ __forceinline__ LexKeyT<I> BlockLex(LexKeyT<I> x, long long* rs, unsigned long long* rk, uint32_t* ri) {
+  LexGroupReduce<32, I>(x);
   if (LaneId() == 0) {
     rs[threadIdx.x >> 5] = x.S;
     rk[threadIdx.x >> 5] = x.K;
     ri[threadIdx.x >> 5] = x.id;
   }
   __syncthreads();
-  LexKey r;
+  LexKeyT<I> r;
 #pragma unroll
-  for (int w = 0; w < kHW; ++w) r.Keep(rs[w], rk[w], ri[w]);
+  for (int w = 0; w < BT / 32; ++w) r.Keep(static_cast<I>(rs[w]), rk[w], ri[w]);
   __syncthreads();
   return r;
 }
 
-// Finds or inserts `key` (local or distributed shared memory), probing from
-// `start`; kNone when the table is full.
-__device__ __forceinline__ uint32_t HubInsert(uint32_t* keys, uint32_t cap, uint32_t start, uint32_t key,
+// Finds or inserts `key` in a table of `cap` slots (any capacity), probing
+// linearly from the slot the hash picks; kNone when the table is full.
+__device__ __forceinline__ uint32_t HubInsert(uint32_t* keys, uint32_t cap, uint32_t hsh, uint32_t key,
                                               bool* ins) {
-  const uint32_t mask = cap - 1;
-  uint32_t s = start & mask;
+  uint32_t s = __umulhi(hsh, cap);
   *ins = false;
   for (uint32_t pr = 0; pr < cap; ++pr) {
     const uint32_t k = *reinterpret_cast<volatile uint32_t*>(keys + s);
@@ -185,122 +233,26 @@ __device__ __forceinline__ uint32_t HubInsert(uint32_t* keys, uint32_t cap, uint
       }
       if (old == key) return s;
     }
-    s = (s + 1) & mask;
+    s = s + 1 == cap ? 0 : s + 1;
   }
   return kNone;
 }
-
-// Shared scratch of a hub CTA besides its table.
-struct HubShared {
-  long long red_ll[kHW];
-  unsigned long long red_k[kHW];
-  double red_d[kHW];
-  float red_f[kHW];
-  uint32_t red_i[kHW];
-  int stage_i[kHW][32];
-  double stage_d[kHW][32];
-  uint32_t cont_key[kMaxCont];
-  long long cont_S[kMaxCont];
-  uint32_t ncont;
-  double change;
-  float change32;
-  // Cluster exchange (big hubs); flags and key counts double-buffered by
-  // sub-pass parity.
-  long long xT;
-  double xTd;
-  long long xsmax;
-  uint32_t flags[2];
-  uint32_t nkeys[2];
-};
 
 // Entry contribution w - offset: integer in INT mode, the reference hub
 // path's float-rounded value in FP64 mode.
 template <bool kInt>
 __device__ __forceinline__ void EntryWeight(const BMArgs& a, float wt, int* xi, double* xd) {
   if (kInt) {
-    *xi = static_cast<int>(wt) - a.ioffset;
+    *xi = WeightToInt(wt) - a.ioffset;
   } else {
     *xd = static_cast<double>(static_cast<float>(Dsub(static_cast<double>(wt), a.offset)));
   }
 }
 
-// Evaluates this CTA's table: returns (to every thread) the best (exact FP64
-// value, id) of its keys and clears the table.  INT sync mode: FP32
-// pre-filter, then FP64 only for the survivors outside the leading (S, K)
-// class, whose members share one FP64 value (evaluated once).
-template <bool kInt, bool kAsync, typename V>
-__device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double change, long long smax,
-                          uint32_t* skeys, V* svals, uint32_t cap, HubShared& sh, double* out_v, uint32_t* out_id) {
-  const unsigned tid = threadIdx.x;
-  constexpr bool kFilter = kInt && !kAsync;
-  double lv = 0.0;
-  uint32_t lid = kNone;
-  if (kFilter) {
-    const float c32 = sh.change32;
-    float U = -CUDART_INF_F;
-    for (uint32_t s = tid; s < cap; s += kHT) {
-      const uint32_t key = skeys[s];
-      if (key == kNone) continue;
-      const FilterVal f = FilterOf(a.res32, k32, a.Kf[key], static_cast<long long>(svals[s]), smax, c32);
-      if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
-    }
-    if (tid == 0) sh.ncont = 0;
-    U = BlockMaxF(U, sh.red_f);
-    LexKey lead, tail;
-    for (uint32_t s = tid; s < cap; s += kHT) {
-      const uint32_t key = skeys[s];
-      if (key == kNone) continue;
-      const long long S = static_cast<long long>(svals[s]);
-      skeys[s] = kNone;
-      svals[s] = V(0);
-      const FilterVal f = FilterOf(a.res32, k32, a.Kf[key], S, smax, c32);
-      if (f.sane && __fadd_rn(f.Y, f.e) < U) continue;
-      const double KD = a.K[key];
-      const unsigned long long ko = KOrder(KD);
-      lead.Keep(S, ko, key);
-      tail.Keep(-S, ~ko, key);
-      const uint32_t pos = atomicAdd(&sh.ncont, 1u);
-      if (pos < kMaxCont) {
-        sh.cont_key[pos] = key;
-        sh.cont_S[pos] = S;
-      } else {
-        KeepBest(lv, lid, ValOf(a, x.kv, change, static_cast<double>(S), KD), key);  // list full: now
-      }
-    }
-    lead = BlockLex(lead, sh.red_ll, sh.red_k, sh.red_i);
-    tail = BlockLex(tail, sh.red_ll, sh.red_k, sh.red_i);
-    const uint32_t nc = min(sh.ncont, kMaxCont);
-    const bool single = lead.id == kNone || (-tail.S == lead.S && ~tail.K == lead.K);
-    if (!single) {
-      for (uint32_t i = tid; i < nc; i += kHT) {
-        const uint32_t key = sh.cont_key[i];
-        const long long S = sh.cont_S[i];
-        const double KD = a.K[key];
-        if (S == lead.S && KOrder(KD) == lead.K) continue;  // the leading class
-        KeepBest(lv, lid, ValOf(a, x.kv, change, static_cast<double>(S), KD), key);
-      }
-    }
-    if (tid == 0 && lead.id != kNone)
-      KeepBest(lv, lid, ValOf(a, x.kv, change, static_cast<double>(lead.S), a.K[lead.id]), lead.id);
-  } else {
-    for (uint32_t s = tid; s < cap; s += kHT) {
-      const uint32_t key = skeys[s];
-      if (key == kNone) continue;
-      const V sv = svals[s];
-      skeys[s] = kNone;
-      svals[s] = V(0);
-      KeepBest(lv, lid, ValOf(a, x.kv, change, VToDouble(sv), LdK<kAsync>(a.K + key)), key);
-    }
-  }
-  BlockArgmax(lv, lid, sh.red_d, sh.red_i);
-  *out_v = lv;
-  *out_id = lid;
-}
-
 // Warp-aggregated sum of the entry weights of each match group.
-template <bool kInt>
+template <int BT, bool kInt>
 __device__ __forceinline__ void GroupWeights(const BMArgs& a, unsigned peers, bool leader, int xi, double xd,
-                                             HubShared& sh, int* Si, double* Sd) {
+                                             HubShared<BT>& sh, int* Si, double* Sd) {
   const unsigned warp = threadIdx.x >> 5, lane = LaneId();
   if (kInt) {
     *Si = GroupSumInt(peers, xi, a.w == nullptr, leader, sh.stage_i[warp]);
@@ -320,6 +272,83 @@ __device__ __forceinline__ void GroupWeights(const BMArgs& a, unsigned peers, bo
   }
 }
 
+// Evaluates the CTA's table: returns (to every thread) the best (exact FP64
+// value, id) of its keys and clears the table.  INT sync mode: FP32
+// pre-filter, then FP64 only for the survivors outside the leading (S, K)
+// class, whose members share one FP64 value (evaluated once).
+template <int BT, bool kInt, bool kAsync, typename V>
+__device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double change, long long smax_ll,
+                          uint32_t* skeys, V* svals, uint32_t cap, HubShared<BT>& sh, double* out_v,
+                          uint32_t* out_id) {
+  // Integer type of the sums: int for narrow tables (32-bit conversions).
+  using I = typename std::conditional<std::is_same<V, int>::value, int, long long>::type;
+  const unsigned tid = threadIdx.x;
+  constexpr bool kFilter = kInt && !kAsync;
+  double lv = 0.0;
+  uint32_t lid = kNone;
+  if (kFilter) {
+    const I smax = static_cast<I>(smax_ll);
+    const float c32 = sh.change32;
+    float U = -CUDART_INF_F;
+    for (uint32_t s = tid; s < cap; s += BT) {
+      const uint32_t key = skeys[s];
+      if (key == kNone) continue;
+      const FilterVal f = FilterOf<I>(a.res32, k32, a.Kf[key], static_cast<I>(svals[s]), smax, c32);
+      if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
+    }
+    if (tid == 0) sh.ncont = 0;
+    U = BlockMaxF<BT>(U, sh.red_f);
+    LexKeyT<I> lead, tail;
+    for (uint32_t s = tid; s < cap; s += BT) {
+      const uint32_t key = skeys[s];
+      if (key == kNone) continue;
+      const I S = static_cast<I>(svals[s]);
+      skeys[s] = kNone;
+      svals[s] = V(0);
+      const FilterVal f = FilterOf<I>(a.res32, k32, a.Kf[key], S, smax, c32);
+      if (f.sane && __fadd_rn(f.Y, f.e) < U) continue;
+      const double KD = a.K[key];
+      const unsigned long long ko = KOrder(KD);
+      lead.Keep(S, ko, key);
+      tail.Keep(-S, ~ko, key);
+      const uint32_t pos = atomicAdd(&sh.ncont, 1u);
+      if (pos < kMaxCont) {
+        sh.cont_key[pos] = key;
+        sh.cont_S[pos] = S;
+      } else {
+        KeepBest(lv, lid, ValOf(a, x.kv, change, static_cast<double>(S), KD), key);  // list full: now
+      }
+    }
+    lead = BlockLex<BT, I>(lead, sh.red_ll, sh.red_k, sh.red_i);
+    tail = BlockLex<BT, I>(tail, sh.red_ll, sh.red_k, sh.red_i);
+    const uint32_t nc = min(sh.ncont, kMaxCont);
+    const bool single = lead.id == kNone || (-tail.S == lead.S && ~tail.K == lead.K);
+    if (!single) {
+      for (uint32_t i = tid; i < nc; i += BT) {
+        const uint32_t key = sh.cont_key[i];
+        const I S = static_cast<I>(sh.cont_S[i]);
+        const double KD = a.K[key];
+        if (S == lead.S && KOrder(KD) == lead.K) continue;  // the leading class
+        KeepBest(lv, lid, ValOf(a, x.kv, change, static_cast<double>(S), KD), key);
+      }
+    }
+    if (tid == 0 && lead.id != kNone)
+      KeepBest(lv, lid, ValOf(a, x.kv, change, static_cast<double>(lead.S), a.K[lead.id]), lead.id);
+  } else {
+    for (uint32_t s = tid; s < cap; s += BT) {
+      const uint32_t key = skeys[s];
+      if (key == kNone) continue;
+      const V sv = svals[s];
+      skeys[s] = kNone;
+      svals[s] = V(0);
+      KeepBest(lv, lid, ValOf(a, x.kv, change, static_cast<double>(sv), LdK<kAsync>(a.K + key)), key);
+    }
+  }
+  BlockArgmax<BT>(lv, lid, sh.red_k, sh.red_i);
+  *out_v = lv;
+  *out_id = lid;
+}
+
 template <bool kAsync>
 __device__ __forceinline__ void HubDecide(const BMArgs& a, const VertexCtx& x, double bv, uint32_t bi,
                                           double change) {
@@ -331,159 +360,167 @@ __device__ __forceinline__ void HubDecide(const BMArgs& a, const VertexCtx& x, d
   if (!kAsync && append) a.movers[atomicAdd(&a.ctr->movers, 1u)] = x.v;
 }
 
-// ---------------------------------------------------------------------------
-// Small hubs: one CTA per hub, a table of nextpow2(2 * degree + 2) slots.
-// ---------------------------------------------------------------------------
-template <bool kInt, bool kAsync, typename V>
-__global__ void __launch_bounds__(kHT) HubSmallKernel(HubArgs h) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  V* svals = reinterpret_cast<V*>(smem);
-  uint32_t* skeys = reinterpret_cast<uint32_t*>(smem + size_t(kHubSlots) * sizeof(V));
-  __shared__ HubShared sh;
-  const BMArgs& a = h.a;
+// One CTA's scan of a hub row: the entries whose cluster falls in partition
+// p / sub-partition q are added into the CTA's table; "together" (the hub's
+// own cluster) accumulates when want_T.  Returns the largest sum seen
+// (INT mode) through *smax.
+template <int BT, bool kInt, bool kAsync, typename V>
+__device__ __forceinline__ void ScanRow(const BMArgs& a, const VertexCtx& x, uint32_t P, uint32_t p, uint32_t Q,
+                                        uint32_t q, bool want_T, uint32_t* skeys, V* svals, uint32_t cap,
+                                        uint32_t maxkeys, HubShared<BT>& sh, long long* t_int, double* t_dbl,
+                                        long long* smax) {
   const unsigned tid = threadIdx.x, lane = LaneId();
-  for (uint32_t i = tid; i < kHubSlots; i += kHT) {
-    skeys[i] = kNone;
-    svals[i] = V(0);
-  }
-  __syncthreads();
-  for (uint32_t item = blockIdx.x; item < h.num_small; item += gridDim.x) {
-    const uint32_t v = h.small_v[item];
-    if (!InFront(a, v)) continue;  // uniform over the CTA
-    const VertexCtx x = LoadVertex<kAsync>(a, v);
-    uint32_t cap = 256;
-    while (cap < 2 * x.d + 2 && cap < kHubSlots) cap <<= 1;
-    long long t_int = 0, smax = LLONG_MIN;
-    double t_dbl = 0.0;
-    for (uint32_t e0 = 0; e0 < x.d; e0 += kHT * kHubUnroll) {
-      uint32_t uu[kHubUnroll], cc[kHubUnroll];
-      float ww[kHubUnroll];
+  const uint32_t v = x.v;
+  for (uint32_t e0 = 0; e0 < x.d; e0 += BT * kHubUnroll) {
+    uint32_t uu[kHubUnroll], cc[kHubUnroll];
+    float ww[kHubUnroll];
 #pragma unroll
-      for (int k = 0; k < kHubUnroll; ++k) {
-        const uint32_t e = e0 + k * kHT + tid;
-        uu[k] = v;
-        ww[k] = 0.f;
-        if (e < x.d) {
-          uu[k] = a.nbr[x.b + e];
-          ww[k] = a.w ? a.w[x.b + e] : 1.0f;
-        }
+    for (int k = 0; k < kHubUnroll; ++k) {
+      const uint32_t e = e0 + k * BT + tid;
+      uu[k] = v;
+      ww[k] = 0.f;
+      if (e < x.d) {
+        uu[k] = a.nbr[x.b + e];
+        ww[k] = a.w ? a.w[x.b + e] : 1.0f;
       }
+    }
 #pragma unroll
-      for (int k = 0; k < kHubUnroll; ++k) cc[k] = uu[k] != v ? LdC<kAsync>(a.C + uu[k]) : kNone;
+    for (int k = 0; k < kHubUnroll; ++k) cc[k] = uu[k] != v ? LdC<kAsync>(a.C + uu[k]) : kNone;
 #pragma unroll
-      for (int k = 0; k < kHubUnroll; ++k) {
-        const bool cand = uu[k] != v;
-        const uint32_t cu = cc[k];
-        int xi = 0;
-        double xd = 0.0;
-        if (cand) EntryWeight<kInt>(a, ww[k], &xi, &xd);
-        if (cand && cu == x.c) {
-          if (kInt)
-            t_int += xi;
-          else
-            t_dbl = Dadd(t_dbl, xd);
-        }
-        const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane));
-        const bool leader = cand && int(lane) == __ffs(peers) - 1;
-        int Si = 0;
-        double Sd = 0.0;
-        GroupWeights<kInt>(a, peers, leader, xi, xd, sh, &Si, &Sd);
-        if (leader) {
-          bool ins;
-          const uint32_t slot = HubInsert(skeys, cap, Mix32(cu), cu, &ins);
-          if (slot == kNone) {
-            atomicExch(&a.ctr->error, kErrHashFull);
-          } else if (kInt) {
+    for (int k = 0; k < kHubUnroll; ++k) {
+      if (e0 + k * BT >= x.d) break;  // uniform over the CTA
+      const bool cand = uu[k] != v;
+      const uint32_t cu = cc[k];
+      int xi = 0;
+      double xd = 0.0;
+      if (cand) EntryWeight<kInt>(a, ww[k], &xi, &xd);
+      if (want_T && cand && cu == x.c) {
+        if (kInt)
+          *t_int += xi;
+        else
+          *t_dbl = Dadd(*t_dbl, xd);
+      }
+      bool mine = cand;
+      if (P > 1 || Q > 1) {
+        const uint32_t hp = Mix32(cu);
+        mine = mine && __umulhi(hp, P) == p && ((hp >> 8) & (Q - 1)) == q;
+      }
+      const unsigned peers = __match_any_sync(kFull, mine ? cu : LaneSentinel(lane));
+      const bool leader = mine && int(lane) == __ffs(peers) - 1;
+      int Si = 0;
+      double Sd = 0.0;
+      GroupWeights<BT, kInt>(a, peers, leader, xi, xd, sh, &Si, &Sd);
+      if (leader && *reinterpret_cast<volatile uint32_t*>(&sh.overflow) == 0) {
+        bool ins;
+        const uint32_t slot = HubInsert(skeys, cap, SlotHash(cu), cu, &ins);
+        if (slot == kNone) {
+          sh.overflow = 1;
+        } else {
+          if (ins && atomicAdd(&sh.nkeys, 1u) + 1 > maxkeys) sh.overflow = 1;
+          if (kInt) {
             const V old = AtomicAddV<V>(svals + slot, static_cast<V>(Si));
-            smax = max(smax, static_cast<long long>(old) + Si);
+            *smax = max(*smax, static_cast<long long>(old) + Si);
           } else {
             AtomicAddV<V>(svals + slot, static_cast<V>(Sd));
           }
         }
       }
     }
+  }
+}
+
+// The hub's "together" and change, once per item (FP64 by one thread).
+template <int BT, bool kInt>
+__device__ __forceinline__ double HubChange(const BMArgs& a, const VertexCtx& x, long long t_int, double t_dbl,
+                                            HubShared<BT>& sh) {
+  double T;
+  if (kInt)
+    T = static_cast<double>(BlockSum<BT, long long>(t_int, sh.red_ll));
+  else
+    T = BlockSum<BT, double>(t_dbl, sh.red_d);
+  if (threadIdx.x == 0) {
+    sh.change = ChangeOf(a, x, T);
+    sh.change32 = static_cast<float>(sh.change);
+  }
+  __syncthreads();
+  return sh.change;
+}
+
+// ---------------------------------------------------------------------------
+// Small hubs: one CTA per hub, a table of 2 * degree slots (never full).
+// ---------------------------------------------------------------------------
+template <bool kInt, bool kAsync, typename V>
+__global__ void __launch_bounds__(kSmallThreads) HubSmallKernel(HubArgs h) {
+  constexpr int BT = kSmallThreads;
+  extern __shared__ __align__(16) unsigned char smem[];
+  V* svals = reinterpret_cast<V*>(smem);
+  uint32_t* skeys = reinterpret_cast<uint32_t*>(smem + size_t(kSmallSlots) * sizeof(V));
+  __shared__ HubShared<BT> sh;
+  const BMArgs& a = h.a;
+  const unsigned tid = threadIdx.x;
+  for (uint32_t i = tid; i < kSmallSlots; i += BT) {
+    skeys[i] = kNone;
+    svals[i] = V(0);
+  }
+  if (tid == 0) {
+    sh.overflow = 0;
+    sh.nkeys = 0;
+  }
+  __syncthreads();
+  for (uint32_t item = blockIdx.x; item < h.num_small; item += gridDim.x) {
+    const uint32_t v = h.small_v[item];
+    if (!InFront(a, v)) continue;  // uniform over the CTA
+    const VertexCtx x = LoadVertex<kAsync>(a, v);
+    const uint32_t cap = min(kSmallSlots, 2 * x.d + 2);
+    long long t_int = 0, smax = LLONG_MIN;
+    double t_dbl = 0.0;
+    ScanRow<BT, kInt, kAsync, V>(a, x, 1, 0, 1, 0, true, skeys, svals, cap, cap, sh, &t_int, &t_dbl, &smax);
     __syncthreads();
-    double T;
-    if (kInt) {
-      T = static_cast<double>(BlockSum<long long>(t_int, sh.red_ll));
-      smax = BlockMaxLL(smax, sh.red_ll);
-    } else {
-      T = BlockSum<double>(t_dbl, sh.red_d);
-    }
+    const double change = HubChange<BT, kInt>(a, x, t_int, t_dbl, sh);
+    if (kInt) smax = BlockMaxLL<BT>(smax, sh.red_ll);
     if (tid == 0) {
-      sh.change = ChangeOf(a, x, T);  // FP64 once per CTA
-      sh.change32 = static_cast<float>(sh.change);
+      if (sh.overflow) atomicExch(&a.ctr->error, kErrHashFull);  // cannot happen: 2d + 2 slots
+      sh.nkeys = 0;
     }
-    __syncthreads();
-    const double change = sh.change;
     double bv;
     uint32_t bi;
-    EvalTable<kInt, kAsync, V>(a, x, a.kf[v], change, smax, skeys, svals, cap, sh, &bv, &bi);
+    EvalTable<BT, kInt, kAsync, V>(a, x, a.kf[v], change, smax, skeys, svals, cap, sh, &bv, &bi);
     if (tid == 0) HubDecide<kAsync>(a, x, bv, bi, change);
     __syncthreads();
   }
 }
 
 // ---------------------------------------------------------------------------
-// Big hubs: a cluster of kCS CTAs per (hub, partition) sharing one
-// distributed table.  All control flow between cluster barriers is uniform
-// over the cluster (it depends on the item and on values every CTA reads
-// after a barrier), so every CTA reaches every cluster.sync().  kCS = 1 (no
-// distributed shared memory) serves the 64-bit and FP64 sums, which keep
-// their atomics local; the overflow sub-passes then split the partitions.
+// Big hubs: one CTA per (hub, partition), sub-passes on overflow.
 // ---------------------------------------------------------------------------
-template <unsigned kCS, typename T>
-__device__ __forceinline__ T* Owner(cg::cluster_group& cluster, T* p, unsigned r) {
-  if constexpr (kCS == 1) {
-    return p;
-  } else {
-    return cluster.map_shared_rank(p, r);
-  }
-}
-
-template <unsigned kCS>
-__device__ __forceinline__ void ClusterSync(cg::cluster_group& cluster) {
-  if constexpr (kCS == 1) {
-    __syncthreads();
-  } else {
-    cluster.sync();
-  }
-}
-
-template <bool kInt, bool kAsync, typename V, unsigned kCS>
-__global__ void __cluster_dims__(kCS, 1, 1) __launch_bounds__(kHT) HubClusterKernel(HubArgs h) {
+template <bool kInt, bool kAsync, typename V>
+__global__ void __launch_bounds__(kBigThreads) HubBigKernel(HubArgs h) {
+  constexpr int BT = kBigThreads;
+  constexpr uint32_t kSlots = BigSlots<V>();
   extern __shared__ __align__(16) unsigned char smem[];
   V* svals = reinterpret_cast<V*>(smem);
-  uint32_t* skeys = reinterpret_cast<uint32_t*>(smem + size_t(kHubSlots) * sizeof(V));
-  __shared__ HubShared sh;
-  cg::cluster_group cluster = cg::this_cluster();
-  const unsigned rank = kCS == 1 ? 0u : cluster.block_rank();
+  uint32_t* skeys = reinterpret_cast<uint32_t*>(smem + size_t(kSlots) * sizeof(V));
+  __shared__ HubShared<BT> sh;
   const BMArgs& a = h.a;
-  const unsigned tid = threadIdx.x, lane = LaneId();
-  for (uint32_t i = tid; i < kHubSlots; i += kHT) {
+  const unsigned tid = threadIdx.x;
+  for (uint32_t i = tid; i < kSlots; i += BT) {
     skeys[i] = kNone;
     svals[i] = V(0);
   }
   if (tid == 0) {
-    sh.flags[0] = sh.flags[1] = 0;
-    sh.nkeys[0] = sh.nkeys[1] = 0;
+    sh.overflow = 0;
+    sh.nkeys = 0;
   }
-  ClusterSync<kCS>(cluster);  // every table is initialised before any remote insert
-  const uint32_t cid = blockIdx.x / kCS, ncl = gridDim.x / kCS;
-  unsigned parity = 0;
-  for (uint32_t item = cid; item < h.num_items; item += ncl) {
+  __syncthreads();
+  for (uint32_t item = blockIdx.x; item < h.num_items; item += gridDim.x) {
     const uint32_t hb = h.item_hub[item];
     const uint32_t p = h.item_part[item];
     const uint32_t v = h.big_v[hb];
-    if (!InFront(a, v)) continue;  // uniform over the cluster
+    if (!InFront(a, v)) continue;  // uniform over the CTA
     const VertexCtx x = LoadVertex<kAsync>(a, v);
     const uint32_t P = h.big_parts[hb];
-    const uint32_t per_cta = (x.d + P * kCS - 1) / (P * kCS);
-    uint32_t cap = 256;
-    while (cap < 2 * per_cta + 2 && cap < kHubSlots) cap <<= 1;
+    const uint32_t cap = min(kSlots, 2 * ((x.d + P - 1) / P) + 2);
     const uint32_t maxkeys = cap - cap / 4;
-    const uint32_t seg = (x.d + kCS - 1) / kCS;
-    const uint32_t e_lo = min(x.d, rank * seg), e_hi = min(x.d, e_lo + seg);
     uint32_t Q = 1, q = 0;
     bool have_T = false;
     double change = 0.0;
@@ -492,120 +529,31 @@ __global__ void __cluster_dims__(kCS, 1, 1) __launch_bounds__(kHT) HubClusterKer
     while (true) {
       long long t_int = 0, smax = LLONG_MIN;
       double t_dbl = 0.0;
-      for (uint32_t e0 = e_lo; e0 < e_hi; e0 += kHT * kHubUnroll) {
-        uint32_t uu[kHubUnroll], cc[kHubUnroll];
-        float ww[kHubUnroll];
-#pragma unroll
-        for (int k = 0; k < kHubUnroll; ++k) {
-          const uint32_t e = e0 + k * kHT + tid;
-          uu[k] = v;
-          ww[k] = 0.f;
-          if (e < e_hi) {
-            uu[k] = a.nbr[x.b + e];
-            ww[k] = a.w ? a.w[x.b + e] : 1.0f;
-          }
-        }
-#pragma unroll
-        for (int k = 0; k < kHubUnroll; ++k) cc[k] = uu[k] != v ? LdC<kAsync>(a.C + uu[k]) : kNone;
-#pragma unroll
-        for (int k = 0; k < kHubUnroll; ++k) {
-          const bool cand = uu[k] != v;
-          const uint32_t cu = cc[k];
-          int xi = 0;
-          double xd = 0.0;
-          if (cand) EntryWeight<kInt>(a, ww[k], &xi, &xd);
-          if (!have_T && cand && cu == x.c) {
-            if (kInt)
-              t_int += xi;
-            else
-              t_dbl = Dadd(t_dbl, xd);
-          }
-          const uint32_t hsh = Mix32(cu);
-          const bool mine = cand && __umulhi(hsh, P) == p && ((hsh >> 16) & (Q - 1)) == q;
-          const unsigned peers = __match_any_sync(kFull, mine ? cu : LaneSentinel(lane));
-          const bool leader = mine && int(lane) == __ffs(peers) - 1;
-          int Si = 0;
-          double Sd = 0.0;
-          GroupWeights<kInt>(a, peers, leader, xi, xd, sh, &Si, &Sd);
-          if (leader) {
-            const unsigned owner = (hsh >> 13) & (kCS - 1);
-            uint32_t* rkeys = Owner<kCS>(cluster, skeys, owner);
-            V* rvals = Owner<kCS>(cluster, svals, owner);
-            HubShared* rsh = Owner<kCS>(cluster, &sh, owner);
-            bool ins;
-            const uint32_t slot = HubInsert(rkeys, cap, hsh, cu, &ins);
-            if (slot == kNone) {
-              atomicExch(&rsh->flags[parity], 1u);
-            } else {
-              if (ins && atomicAdd(&rsh->nkeys[parity], 1u) + 1 > maxkeys) atomicExch(&rsh->flags[parity], 1u);
-              if (kInt) {
-                const V old = AtomicAddV<V>(rvals + slot, static_cast<V>(Si));
-                smax = max(smax, static_cast<long long>(old) + Si);
-              } else {
-                AtomicAddV<V>(rvals + slot, static_cast<V>(Sd));
-              }
-            }
-          }
-        }
-      }
-      // Per-CTA partials of "together" and of the largest sum, then the
-      // cluster barrier that also publishes every remote insert.
+      ScanRow<BT, kInt, kAsync, V>(a, x, P, p, Q, q, !have_T, skeys, svals, cap, maxkeys, sh, &t_int, &t_dbl,
+                                   &smax);
+      __syncthreads();
       if (!have_T) {
-        if (kInt) {
-          const long long t = BlockSum<long long>(t_int, sh.red_ll);
-          if (tid == 0) sh.xT = t;
-        } else {
-          const double t = BlockSum<double>(t_dbl, sh.red_d);
-          if (tid == 0) sh.xTd = t;
-        }
-      }
-      if (kInt) {
-        const long long m = BlockMaxLL(smax, sh.red_ll);
-        if (tid == 0) sh.xsmax = m;
-      }
-      ClusterSync<kCS>(cluster);  // (1) tables, partials and flags complete
-      bool overflow = false;
-      long long csmax = LLONG_MIN;
-      for (unsigned r = 0; r < kCS; ++r) {
-        const HubShared* rsh = Owner<kCS>(cluster, &sh, r);
-        overflow = overflow || (*reinterpret_cast<const volatile uint32_t*>(&rsh->flags[parity]) != 0);
-        if (kInt) csmax = max(csmax, rsh->xsmax);
-      }
-      if (!have_T) {
-        double T;
-        if (kInt) {
-          long long t = 0;
-          for (unsigned r = 0; r < kCS; ++r) t += Owner<kCS>(cluster, &sh, r)->xT;
-          T = static_cast<double>(t);
-        } else {
-          T = 0.0;
-          for (unsigned r = 0; r < kCS; ++r) T = Dadd(T, Owner<kCS>(cluster, &sh, r)->xTd);
-        }
-        if (tid == 0) {
-          sh.change = ChangeOf(a, x, T);  // FP64 once per CTA
-          sh.change32 = static_cast<float>(sh.change);
-        }
-        __syncthreads();
-        change = sh.change;
+        change = HubChange<BT, kInt>(a, x, t_int, t_dbl, sh);
         have_T = true;
       }
-      // The next sub-pass uses the other parity; reset it here (it was last
-      // read before the previous cluster barrier).
+      if (kInt) smax = BlockMaxLL<BT>(smax, sh.red_ll);  // also orders the reads of sh.overflow
+      const bool overflow = sh.overflow != 0;
+      __syncthreads();
       if (tid == 0) {
-        sh.flags[parity ^ 1] = 0;
-        sh.nkeys[parity ^ 1] = 0;
+        sh.overflow = 0;
+        sh.nkeys = 0;
       }
       if (overflow) {
-        for (uint32_t s = tid; s < cap; s += kHT) {
+        // Split the partition further and rescan from the first sub-pass.
+        for (uint32_t s = tid; s < cap; s += BT) {
           skeys[s] = kNone;
           svals[s] = V(0);
         }
+        __syncthreads();
         Q *= 2;
         q = 0;
         bestv = 0.0;
         bestid = kNone;
-        ClusterSync<kCS>(cluster);  // (2) cleared before the rescan's inserts
-        parity ^= 1;
         if (Q > kHubMaxSub) {
           if (tid == 0) atomicExch(&a.ctr->error, kErrHashFull);
           break;
@@ -614,31 +562,28 @@ __global__ void __cluster_dims__(kCS, 1, 1) __launch_bounds__(kHT) HubClusterKer
       }
       double lv;
       uint32_t lid;
-      EvalTable<kInt, kAsync, V>(a, x, a.kf[v], change, csmax, skeys, svals, cap, sh, &lv, &lid);
+      EvalTable<BT, kInt, kAsync, V>(a, x, a.kf[v], change, smax, skeys, svals, cap, sh, &lv, &lid);
       KeepBest(bestv, bestid, lv, lid);
-      ClusterSync<kCS>(cluster);  // (2) every table cleared before the next inserts
-      parity ^= 1;
+      __syncthreads();
       if (++q == Q) break;
     }
     // Partial result; the hub's last CTA combines and decides.
     if (tid == 0) {
-      const uint32_t pb = h.big_pbase[hb] + p * kCS + rank;
-      h.part_val[pb] = bestv;
-      h.part_id[pb] = bestid;
+      const uint32_t pb = h.big_pbase[hb];
+      h.part_val[pb + p] = bestv;
+      h.part_id[pb + p] = bestid;
       __threadfence();
-      const uint32_t total = P * kCS;
-      if (atomicAdd(&h.done[hb], 1u) == total - 1) {
+      if (atomicAdd(&h.done[hb], 1u) == P - 1) {
         __threadfence();
         double bv = 0.0;
         uint32_t bi = kNone;
-        const uint32_t b0 = h.big_pbase[hb];
-        for (uint32_t j = 0; j < total; ++j) KeepBest(bv, bi, __ldcg(h.part_val + b0 + j), __ldcg(h.part_id + b0 + j));
+        for (uint32_t j = 0; j < P; ++j) KeepBest(bv, bi, __ldcg(h.part_val + pb + j), __ldcg(h.part_id + pb + j));
         h.done[hb] = 0;
         HubDecide<kAsync>(a, x, bv, bi, change);
       }
     }
+    __syncthreads();
   }
-  ClusterSync<kCS>(cluster);  // no CTA leaves while its table may still be read
 }
 
 __global__ void HubDegreesKernel(const uint32_t* list, uint32_t count, const uint64_t* off, uint32_t* deg) {
@@ -648,41 +593,25 @@ __global__ void HubDegreesKernel(const uint32_t* list, uint32_t count, const uin
 
 template <bool kInt, bool kAsync, typename V>
 Status LaunchHubT(Context* ctx, const HubArgs& h) {
-  constexpr size_t smem = size_t(kHubSlots) * (sizeof(V) + sizeof(uint32_t));
-  // Distributed tables only with 32-bit sums (32-bit remote atomics).
-  constexpr unsigned kCS = std::is_same<V, int>::value ? kHubClusterSize : 1u;
   const unsigned sms = unsigned(ctx->num_sms);
   if (h.num_small) {
+    constexpr size_t smem = size_t(kSmallSlots) * (sizeof(V) + sizeof(uint32_t));
     auto k = HubSmallKernel<kInt, kAsync, V>;
     PCC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int per_sm = 0;
-    PCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kHT, smem));
+    PCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kSmallThreads, smem));
     const unsigned grid = Blocks(h.num_small, 1, sms * unsigned(std::max(per_sm, 1)));
-    k<<<grid, kHT, smem, ctx->stream>>>(h);
+    k<<<grid, kSmallThreads, smem, ctx->stream>>>(h);
     PCC_COUNT(1);
   }
   if (h.num_items) {
-    auto k = HubClusterKernel<kInt, kAsync, V, kCS>;
+    constexpr size_t smem = size_t(BigSlots<V>()) * (sizeof(V) + sizeof(uint32_t));
+    auto k = HubBigKernel<kInt, kAsync, V>;
     PCC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    int max_clusters = 0;
-    if (kCS > 1) {
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(kCS * sms, 1, 1);
-      cfg.blockDim = dim3(kHT, 1, 1);
-      cfg.dynamicSmemBytes = smem;
-      cfg.stream = ctx->stream;
-      if (cudaOccupancyMaxActiveClusters(&max_clusters, k, &cfg) != cudaSuccess) {
-        cudaGetLastError();
-        max_clusters = 0;
-      }
-      if (max_clusters < 1) max_clusters = int(sms / kCS);
-    } else {
-      int per_sm = 0;
-      PCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kHT, smem));
-      max_clusters = int(sms) * std::max(per_sm, 1);
-    }
-    const unsigned clusters = std::min<unsigned>(h.num_items, unsigned(std::max(max_clusters, 1)));
-    k<<<clusters * kCS, kHT, smem, ctx->stream>>>(h);
+    int per_sm = 0;
+    PCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kBigThreads, smem));
+    const unsigned grid = Blocks(h.num_items, 1, sms * unsigned(std::max(per_sm, 1)));
+    k<<<grid, kBigThreads, smem, ctx->stream>>>(h);
     PCC_COUNT(1);
   }
   return LaunchCheck();
@@ -720,12 +649,12 @@ Status BuildHubPlan(Context* ctx, const DevGraph& g, const BinSet& bins, HubPlan
       small_v.push_back(hv[i]);
       continue;
     }
-    const uint32_t P = std::max<uint32_t>(1, (hd[i] + kHubClusterKeys - 1) / kHubClusterKeys);
+    const uint32_t P = std::max<uint32_t>(1, (hd[i] + kHubBigKeys - 1) / kHubBigKeys);
     const uint32_t hb = static_cast<uint32_t>(big_v.size());
     big_v.push_back(hv[i]);
     parts.push_back(P);
     pbase.push_back(static_cast<uint32_t>(total));
-    total += uint64_t(P) * kHubClusterSize;
+    total += P;
     for (uint32_t p = 0; p < P; ++p) {
       item_hub.push_back(hb);
       item_part.push_back(p);

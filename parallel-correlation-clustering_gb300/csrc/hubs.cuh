@@ -5,20 +5,18 @@
 // correlation-clusterer-internal.cc:516-582).  Here a hub's neighbour-cluster
 // sums live in shared memory only:
 //
-//   small hubs (1000 < degree <= kHubSmallMax): one CTA per hub, a table of
-//     2 * degree slots, so it never fills;
-//   big hubs (degree > kHubSmallMax): one thread-block cluster of
-//     kHubClusterSize CTAs per (hub, partition).  The cluster's tables form
-//     one distributed table: a hash of the cluster id picks the owning CTA,
-//     every CTA scans 1/kHubClusterSize of the row and adds each entry into
-//     its owner's table through distributed shared memory.  Hubs with more
-//     than kHubClusterKeys distinct neighbour clusters are split into P
-//     hash partitions (P = ceil(degree / kHubClusterKeys)), one cluster
-//     each, which re-read the row from L2.  A partition whose keys overflow
-//     the tables is split again by further hash bits and rescanned.
+//   small hubs (1000 < degree <= kHubSmallMax): one 256-thread CTA per hub,
+//     a table of 2 * degree slots, so it never fills;
+//   big hubs (degree > kHubSmallMax): one 1024-thread CTA per (hub,
+//     partition) with a ~192 KB table.  Hubs with more than kHubBigKeys
+//     distinct neighbour clusters are split into P hash partitions (P =
+//     ceil(degree / kHubBigKeys)), whose CTAs re-read the row from L2.  A
+//     partition whose keys overflow its table is split again by further hash
+//     bits and rescanned (sub-passes), so correctness does not depend on the
+//     hash distribution.
 //
-// Each CTA evaluates its own table (FP32 pre-filter, exact FP64 values of the
-// survivors, argmax by value desc / id asc); for big hubs the CTAs' partial
+// Each CTA evaluates its table (FP32 pre-filter, exact FP64 values of the
+// survivors, argmax by value desc / id asc); for big hubs the partitions'
 // bests are combined by the hub's last CTA (atomic counter).  No global hash
 // tables, no spin-waits.
 #pragma once
@@ -27,11 +25,9 @@
 
 namespace pcc {
 
-constexpr uint32_t kHubMinDegree = 1000;      // hub = degree > 1000
-constexpr uint32_t kHubSmallMax = 4096;       // one-CTA hubs
-constexpr uint32_t kHubSlots = 8192;          // shared table slots per CTA
-constexpr uint32_t kHubClusterSize = 8;       // CTAs per big-hub cluster
-constexpr uint32_t kHubClusterKeys = kHubSlots / 2 * kHubClusterSize;  // keys per partition
+constexpr uint32_t kHubMinDegree = 1000;  // hub = degree > 1000
+constexpr uint32_t kHubSmallMax = 4096;   // one-partition hubs
+constexpr uint32_t kHubBigKeys = 12288;   // expected distinct keys per big-hub partition
 
 // Static part (depends on the graph only).
 struct HubPlan {
@@ -39,7 +35,7 @@ struct HubPlan {
   uint32_t num_small = 0;      // hubs with degree <= kHubSmallMax
   uint32_t num_big = 0;
   uint32_t num_items = 0;      // big-hub work items (hub, partition)
-  uint64_t num_partials = 0;   // kHubClusterSize per big-hub item
+  uint64_t num_partials = 0;   // one per big-hub item
   DBuf<uint32_t> small_v;      // small hubs, largest first
   DBuf<uint32_t> big_v;        // big hubs, largest first
   DBuf<uint32_t> big_parts;    // P per big hub

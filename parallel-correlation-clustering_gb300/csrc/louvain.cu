@@ -364,10 +364,11 @@ struct RunResult {
   uint64_t algo_bytes = 0;
 };
 
-// INT mode with every neighbour-cluster sum below 2^31 in magnitude: a
-// cluster sum is at most the row's sum of |w| plus degree * |offset|.
+// INT mode with every neighbour-cluster sum below 2^30 in magnitude (so
+// sums and their differences fit in int): a cluster sum is at most the
+// row's sum of |w| plus degree * |offset|.
 bool NarrowSums(const DevGraph& g, double offset) {
-  return g.row_abs_bound + std::fabs(offset) * static_cast<double>(g.max_deg) < 2147483647.0;
+  return g.row_abs_bound + std::fabs(offset) * static_cast<double>(g.max_deg) < 1073741824.0;
 }
 
 bool IntModeFor(const DevGraph& g, double offset) {

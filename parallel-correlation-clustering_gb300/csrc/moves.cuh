@@ -228,6 +228,13 @@ __device__ __forceinline__ uint32_t FindT(const uint32_t* keys, uint32_t cap, ui
   return kNone;
 }
 
+// An integral weight |w| <= 2^22 (INT mode) as an int, with integer and FP32
+// arithmetic (no conversion instruction): w + 1.5 * 2^23 is exact and its
+// bit pattern minus 0x4B400000 is w.
+__device__ __forceinline__ int WeightToInt(float w) {
+  return __float_as_int(__fadd_rn(w, 12582912.0f)) - 0x4B400000;
+}
+
 // Sum of the integer weights x over the calling lane's match_any group
 // `peers`; every lane of the warp calls it.  (__reduce_add_sync with a
 // different mask per group executes once per distinct group -- up to 32
