@@ -129,6 +129,11 @@ struct BMArgs {
   // frontier: vertices v with front_stamp[v] == front_val (all when null)
   const uint32_t* front_stamp;
   uint32_t front_val;
+  // async waves: with waves > 1 only the frontier vertices of wave `wave`
+  // (a salted hash of the id) are evaluated by this launch
+  uint32_t waves;
+  uint32_t wave;
+  uint32_t wave_salt;
   // sync outputs
   uint32_t* moves;          // decided target per vertex (read for movers)
   uint32_t* moved_stamp;    // moved_vertex: = stamp when value > 0

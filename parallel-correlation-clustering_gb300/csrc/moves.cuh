@@ -52,7 +52,20 @@ __device__ __forceinline__ bool Better(double va, uint32_t ia, double vb, uint32
   return va > vb || (va == vb && ia < ib);
 }
 
+// Wave of vertex v in an async round: a salted MurmurHash3 finalizer of the
+// id, scaled to [0, waves).
+__device__ __forceinline__ uint32_t WaveOf(uint32_t v, uint32_t salt, uint32_t waves) {
+  uint32_t x = v ^ salt;
+  x ^= x >> 16;
+  x *= 0x85EBCA6Bu;
+  x ^= x >> 13;
+  x *= 0xC2B2AE35u;
+  x ^= x >> 16;
+  return __umulhi(x, waves);
+}
+
 __device__ __forceinline__ bool InFront(const BMArgs& a, uint32_t v) {
+  if (a.waves > 1 && WaveOf(v, a.wave_salt, a.waves) != a.wave) return false;
   return a.front_stamp == nullptr || a.front_stamp[v] == a.front_val;
 }
 
