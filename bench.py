@@ -42,6 +42,13 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 METRIC = "best-move edge-visits/s"
 UNIT = "edge-visits/s"
 
+# DRAM bytes (read + write) per evaluated entry of each best-move kernel
+# family, from ncu captures of RMAT scale 20, level 0, round 1 (the whole
+# frontier); the summary and command are in profiles/.  Traffic scales with
+# the entries evaluated, so the per-launch figure at the bench's size is this
+# times the entries of a launch.
+TRAFFIC_BYTES_PER_ENTRY = {"groups": 51.9, "warps": 8.84, "small_hubs": 5.38, "big_hubs": 7.64}
+
 
 def parse_args():
     ap = argparse.ArgumentParser()
@@ -237,6 +244,7 @@ def main():
 
     for _ in range(max(args.warmup, 0)):
         P.modularity_cluster(dg, cfg)
+    bpe = 12 if g.weights is not None else 8   # algorithmic bytes per entry evaluated
 
     # Timed region: K full clusterings on the resident graph.
     sampler = ClockSampler(local)
@@ -252,6 +260,10 @@ def main():
     front_ms = 0.0
     algo_bytes = 0
     launches = 0
+    fam_ms = [0.0] * 4
+    fam_launch = [0] * 4
+    fam_e = [0] * 4
+    fam_v = [0] * 4
     quality = {}
     for _ in range(args.steps):
         labels, st = P.modularity_cluster(dg, cfg)
@@ -264,6 +276,11 @@ def main():
         front_ms += st["ms_frontier"]
         launches += st["kernel_launches"]
         algo_bytes += st["algo_bytes_best_moves"]
+        for f in range(4):
+            fam_ms[f] += st["family_ms"][f]
+            fam_launch[f] += st["family_launches"][f]
+            fam_e[f] += st["family_entries"][f]
+            fam_v[f] += st["family_vertices"][f]
         quality = {"modularity": st["modularity"], "objective": st["objective"],
                    "num_clusters": st["num_clusters"], "levels": st["levels"], "rounds": st["rounds"]}
     barrier()
@@ -285,6 +302,17 @@ def main():
         e2e_ev += st["edge_visits"]
     barrier()
 
+    # The same configuration in async mode (reported beside the sync line).
+    acfg = P.make_config(resolution=1.0, refine=True, move_method=P.NBHR_MOVE, async_=True, random_seed=1)
+    P.modularity_cluster(dg, acfg)
+    a_ev, a_ms, a_mod = 0, 0.0, []
+    for _ in range(args.steps):
+        _, st = P.modularity_cluster(dg, acfg)
+        a_ev += st["edge_visits"]
+        a_ms += st["ms_total"]
+        a_mod.append(st["modularity"])
+    barrier()
+
     # Max time over ranks; edge visits summed over ranks.
     dev_s = dev_ms / 1000.0
     if dist is not None:
@@ -299,7 +327,24 @@ def main():
 
     if rank == 0:
         peak, peak_kind = measured_peak()
-        achieved = (algo_bytes / (bm_ms / 1000.0)) / 1e9 if bm_ms > 0 else None
+        names = P.PccStats.FAMILIES
+        families = {}
+        for f in range(4):
+            if fam_ms[f] <= 0 or fam_launch[f] == 0:
+                continue
+            byts = bpe * fam_e[f] + 40 * fam_v[f]
+            gbs = byts / (fam_ms[f] / 1000.0) / 1e9
+            families[names[f]] = {
+                "ms_per_step": fam_ms[f] / args.steps, "launches_per_step": fam_launch[f] / args.steps,
+                "entries_per_step": fam_e[f] / args.steps, "achieved_gbs": gbs, "frac": gbs / peak}
+        top = max(range(4), key=lambda f: fam_ms[f])
+        top_bytes_per_launch = (bpe * fam_e[top] + 40 * fam_v[top]) / max(fam_launch[top], 1)
+        top_ms_per_launch = fam_ms[top] / max(fam_launch[top], 1)
+        achieved = top_bytes_per_launch / (top_ms_per_launch / 1000.0) / 1e9 if top_ms_per_launch > 0 else None
+        # DRAM bytes per evaluated entry of the family's kernels, from the ncu
+        # capture summarised in profiles/ (RMAT scale 20, level 0, round 1).
+        traffic_per_entry = TRAFFIC_BYTES_PER_ENTRY.get(names[top])
+        traffic = (traffic_per_entry * fam_e[top] / max(fam_launch[top], 1)) if traffic_per_entry else None
         cpu = None
         if not args.no_cpu_baseline:
             try:
@@ -315,10 +360,12 @@ def main():
                     "h2d_bytes_per_step": int(g.offsets.nbytes + g.neighbors.nbytes),
                     "d2h_bytes_per_step": int(4 * g.n)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None, "traffic": None,
-                         "kernel": "best-move kernels (degree bins), algorithmic bytes "
-                                   "8 or 12 B per edge visit + 40 B per vertex visit",
-                         "peak_kind": f"{peak_kind} hbm_gbs"},
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "kernel": f"best-move family '{names[top]}' (largest device time): "
+                                   f"{bpe} B per entry + 40 B per vertex evaluated, per launch",
+                         "peak_kind": f"{peak_kind} hbm_gbs",
+                         "best_move_phase_gbs": (algo_bytes / (bm_ms / 1000.0)) / 1e9 if bm_ms > 0 else None},
+            "kernel_families": families,
             "cpu_baseline": cpu,
             "clocks": clocks,
             "gpu_launches": launches,
@@ -327,6 +374,9 @@ def main():
                                    "frontier": front_ms / args.steps},
             "wall_s": wall,
             "quality": quality,
+            "modes": {"async": {"value": a_ev / (a_ms / 1000.0) if a_ms > 0 else None, "unit": UNIT,
+                                "ms_per_step": a_ms / args.steps, "modularity_mean": sum(a_mod) / len(a_mod),
+                                "note": "same graph and config with async=true, 16 waves per round"}},
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -103,6 +103,15 @@ typedef struct pcc_stats {
   uint64_t algo_bytes_best_moves; /* algorithmic bytes of the best-move kernels:
                                      (8 or 12) per edge visit + 40 per vertex
                                      visit (8 when the graph has no weights) */
+  /* Best-move kernel families: [0] lane groups (degree <= 32), [1] warps
+     (degree <= 1000), [2] small hubs (<= 4096), [3] big hubs.  Device time
+     (CUDA events around the family's launches), launches, and the entries
+     and vertices evaluated (a big hub counts once however many partitions
+     it is split into). */
+  double family_ms[4];
+  uint64_t family_launches[4];
+  uint64_t family_entries[4];
+  uint64_t family_vertices[4];
 } pcc_stats;
 
 void pcc_config_default(pcc_config* config);

@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
   constexpr unsigned kVpw = 32 / G;
   const unsigned g = lane / G, gl = lane % G;
   const unsigned gmask = G == 32 ? kFull : (((1u << G) - 1u) << (g * G));
+  unsigned long long fam_e = 0, fam_v = 0;
   const uint64_t stride = uint64_t(gridDim.x) * 8 * kVpw;
   for (uint64_t base = (uint64_t(blockIdx.x) * 8 + warp) * kVpw; base < count; base += stride) {
     const uint64_t idx = base + g;
@@ -55,7 +56,11 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
       vvalid = InFront(a, v);
       if (vvalid) x = LoadVertex<kAsync>(a, v);
     }
-    if (__ballot_sync(kFull, vvalid) == 0) continue;  // no frontier vertex in this warp
+    if (__ballot_sync(kFull, vvalid) == 0) continue;
+    if (vvalid && gl == 0) {
+      fam_e += x.d;
+      fam_v += 1;
+    }  // no frontier vertex in this warp
     const bool has = vvalid && gl < x.d;
     uint32_t u = x.v;
     float wt = 0.f;
@@ -131,6 +136,7 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
       if (append) a.movers[slot] = x.v;
     }
   }
+  FlushFamily(a, kFamGroup, fam_e, fam_v);
 }
 
 // ---------------------------------------------------------------------------
@@ -164,6 +170,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
   double* stage = reinterpret_cast<double*>(base + size_t(HC) * 12);
   uint16_t* used = reinterpret_cast<uint16_t*>(base + size_t(HC) * 12 + 32 * 8);
   uint32_t* used_count = reinterpret_cast<uint32_t*>(base + size_t(HC) * 13 + 32 * 8);
+  unsigned long long fam_e = 0, fam_v = 0;
   for (int i = lane; i < HC; i += 32) {
     keys[i] = kNone;
     vals[i] = 0ull;
@@ -175,6 +182,10 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
     const uint32_t vid = list[start + idx];
     if (!InFront(a, vid)) continue;
     const VertexCtx x = LoadVertex<kAsync>(a, vid);
+    if (lane == 0) {
+      fam_e += x.d;
+      fam_v += 1;
+    }
     for (uint32_t e0 = 0; e0 < x.d; e0 += 32) {
       const uint32_t e = e0 + lane;
       const bool has = e < x.d;
@@ -299,6 +310,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
     if (lane == 0) *used_count = 0;
     __syncwarp();
   }
+  FlushFamily(a, kFamWarp, fam_e, fam_v);
 }
 
 // ---------------------------------------------------------------------------
@@ -392,6 +404,7 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
   constexpr unsigned kVpw = 32 / G;
   const unsigned g = lane / G, gl = lane % G;
   const unsigned gmask = G == 32 ? kFull : (((1u << G) - 1u) << (g * G));
+  unsigned long long fam_e = 0, fam_v = 0;
   const bool replay = a.out_target != nullptr;
   const bool unit = a.w == nullptr;
   const uint64_t stride = uint64_t(gridDim.x) * 8 * kVpw;
@@ -409,6 +422,10 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
     }
     vid = nvid;
     if (__ballot_sync(kFull, vvalid) == 0) continue;
+    if (vvalid && gl == 0) {
+      fam_e += x.d;
+      fam_v += 1;
+    }
     const bool has = vvalid && gl < x.d;
     uint32_t u = x.v;
     float wt = 0.f;
@@ -474,6 +491,7 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
     const uint32_t slot = WarpAppendFull(&a.ctr->movers, append);
     if (append) a.movers[slot] = x.v;
   }
+  FlushFamily(a, kFamGroup, fam_e, fam_v);
 }
 
 // Per-warp shared bytes: vals HC*sizeof(V), keys HC*4, stage 32*4, used
@@ -503,6 +521,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
   int* stage = reinterpret_cast<int*>(base + size_t(HC) * (sizeof(V) + 4));
   uint16_t* used = reinterpret_cast<uint16_t*>(base + size_t(HC) * (sizeof(V) + 4) + 32 * 4);
   uint32_t* used_count = reinterpret_cast<uint32_t*>(base + size_t(HC) * (sizeof(V) + 5) + 32 * 4);
+  unsigned long long fam_e = 0, fam_v = 0;
   const bool replay = a.out_target != nullptr;
   const bool unit = a.w == nullptr;
   for (int i = lane; i < HC; i += 32) {
@@ -527,6 +546,10 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     }
     const VertexCtx x = LoadVertex<false>(a, vid);
     vid = nvid;
+    if (lane == 0) {
+      fam_e += x.d;
+      fam_v += 1;
+    }
     for (uint32_t e0 = 0; e0 < x.d; e0 += 32 * kCertUnroll) {
       uint32_t uu[kCertUnroll], cc[kCertUnroll];
       float ww[kCertUnroll];
@@ -640,6 +663,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     if (lane == 0) *used_count = 0;
     __syncwarp();
   }
+  FlushFamily(a, kFamWarp, fam_e, fam_v);
 }
 
 template <class K>
@@ -659,6 +683,9 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
   auto want = [&](int bin) { return !host_counts || host_counts[bin] > 0; };
   cudaStream_t st = ctx->stream;
   constexpr bool kCert = kInt && !kAsync;
+  int ng = 0;
+  for (int b = kBinG4; b <= kBinG32; ++b) ng += want(b) ? 1 : 0;
+  FamBegin(ctx, kFamGroup);
   if (kCert) {
     if (want(kBinG4))
       CertGroupKernel<4><<<grid(kBinG4, 64, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG4); PCC_COUNT(1);
@@ -678,6 +705,10 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
     if (want(kBinG32))
       BestMoveGroupKernel<32, kInt, kAsync><<<grid(kBinG32, 8, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG32); PCC_COUNT(1);
   }
+  FamEnd(ctx, kFamGroup, ng);
+  int nw = 0;
+  for (int b = kBinW128; b <= kBinW1000; ++b) nw += want(b) ? 1 : 0;
+  FamBegin(ctx, kFamWarp);
   auto warp_bin = [&](auto k, size_t smem, int bin, unsigned cap) -> Status {
     if (!want(bin)) return Status::Ok();
     PCC_RETURN_IF_ERROR(SetSmem(k, smem));
@@ -701,6 +732,7 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
     PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<1024, kInt, kAsync>, WarpKernelSmem<1024>(), kBinW512, sms * 4));
     PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<2048, kInt, kAsync>, WarpKernelSmem<2048>(), kBinW1000, sms * 2));
   }
+  FamEnd(ctx, kFamWarp, nw);
   return LaunchCheck();
 }
 

@@ -57,6 +57,17 @@ inline Status MakeError(pcc_status code, std::string msg) {
 // Context: one device, one stream, one stream-ordered pool with an optional
 // HBM budget.  All kernels of a call run on `stream`.
 // ---------------------------------------------------------------------------
+struct PhaseTimer;
+
+// Best-move kernel families, timed and counted separately (roofline of the
+// dominant kernel): lane groups (degree <= 32), warps (<= 1000), small hubs,
+// big hubs.
+constexpr int kFamGroup = 0;
+constexpr int kFamWarp = 1;
+constexpr int kFamHubSmall = 2;
+constexpr int kFamHubBig = 3;
+constexpr int kNumFamilies = 4;
+
 struct Context {
   int device = 0;
   int num_sms = 0;
@@ -67,6 +78,9 @@ struct Context {
   std::mutex mu;
   std::unordered_map<void*, uint64_t> sizes;
   std::string last_error;
+  // Kernel-family timing of the running call (null when not requested).
+  PhaseTimer* fam_timer = nullptr;
+  uint64_t fam_launches[kNumFamilies] = {0, 0, 0, 0};
 
   Status Alloc(void** p, uint64_t bytes) {
     *p = nullptr;
@@ -218,6 +232,14 @@ struct PhaseTimer {
       if (e) cudaEventDestroy(e);
   }
 };
+inline void FamBegin(Context* ctx, int f) {
+  if (ctx->fam_timer) ctx->fam_timer->Begin(f);
+}
+inline void FamEnd(Context* ctx, int f, int launches) {
+  if (ctx->fam_timer) ctx->fam_timer->End(f);
+  ctx->fam_launches[f] += uint64_t(launches);
+}
+
 constexpr int kPhaseBestMoves = 0;
 constexpr int kPhaseCompress = 1;
 constexpr int kPhaseApply = 2;

@@ -101,6 +101,10 @@ struct DevCounters {
   unsigned long long moves;          // real moves (sync) / moves (async)
   int error;                // nonzero: a bounded wait gave up (see kErr*)
   int pad;
+  // Per kernel family (kFam*): entries and vertices evaluated (algorithmic
+  // bytes of the roofline); accumulated over the call.
+  unsigned long long fam_entries[kNumFamilies];
+  unsigned long long fam_vertices[kNumFamilies];
 };
 
 constexpr int kErrProbeLimit = 1;   // async new-cluster probe exceeded its bound

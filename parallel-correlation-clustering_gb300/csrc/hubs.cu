@@ -458,6 +458,7 @@ __global__ void __launch_bounds__(kSmallThreads) HubSmallKernel(HubArgs h) {
   __shared__ HubShared<BT> sh;
   const BMArgs& a = h.a;
   const unsigned tid = threadIdx.x;
+  unsigned long long fam_e = 0, fam_v = 0;  // entries and vertices evaluated (tid 0)
   for (uint32_t i = tid; i < kSmallSlots; i += BT) {
     skeys[i] = kNone;
     svals[i] = V(0);
@@ -472,6 +473,10 @@ __global__ void __launch_bounds__(kSmallThreads) HubSmallKernel(HubArgs h) {
     if (!InFront(a, v)) continue;  // uniform over the CTA
     const VertexCtx x = LoadVertex<kAsync>(a, v);
     const uint32_t cap = min(kSmallSlots, 2 * x.d + 2);
+    if (tid == 0) {
+      fam_e += x.d;
+      fam_v += 1;
+    }
     long long t_int = 0, smax = LLONG_MIN;
     double t_dbl = 0.0;
     ScanRow<BT, kInt, kAsync, V>(a, x, 1, 0, 1, 0, true, skeys, svals, cap, cap, sh, &t_int, &t_dbl, &smax);
@@ -488,6 +493,10 @@ __global__ void __launch_bounds__(kSmallThreads) HubSmallKernel(HubArgs h) {
     if (tid == 0) HubDecide<kAsync>(a, x, bv, bi, change);
     __syncthreads();
   }
+  if (tid == 0 && fam_v) {
+    atomicAdd(&a.ctr->fam_entries[kFamHubSmall], fam_e);
+    atomicAdd(&a.ctr->fam_vertices[kFamHubSmall], fam_v);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -503,6 +512,7 @@ __global__ void __launch_bounds__(kBigThreads) HubBigKernel(HubArgs h) {
   __shared__ HubShared<BT> sh;
   const BMArgs& a = h.a;
   const unsigned tid = threadIdx.x;
+  unsigned long long fam_e = 0, fam_v = 0;  // entries and vertices evaluated once per hub (tid 0)
   for (uint32_t i = tid; i < kSlots; i += BT) {
     skeys[i] = kNone;
     svals[i] = V(0);
@@ -519,6 +529,10 @@ __global__ void __launch_bounds__(kBigThreads) HubBigKernel(HubArgs h) {
     if (!InFront(a, v)) continue;  // uniform over the CTA
     const VertexCtx x = LoadVertex<kAsync>(a, v);
     const uint32_t P = h.big_parts[hb];
+    if (tid == 0 && p == 0) {
+      fam_e += x.d;
+      fam_v += 1;
+    }
     const uint32_t cap = min(kSlots, 2 * ((x.d + P - 1) / P) + 2);
     const uint32_t maxkeys = cap - cap / 4;
     uint32_t Q = 1, q = 0;
@@ -584,6 +598,10 @@ __global__ void __launch_bounds__(kBigThreads) HubBigKernel(HubArgs h) {
     }
     __syncthreads();
   }
+  if (tid == 0 && fam_v) {
+    atomicAdd(&a.ctr->fam_entries[kFamHubBig], fam_e);
+    atomicAdd(&a.ctr->fam_vertices[kFamHubBig], fam_v);
+  }
 }
 
 __global__ void HubDegreesKernel(const uint32_t* list, uint32_t count, const uint64_t* off, uint32_t* deg) {
@@ -601,7 +619,9 @@ Status LaunchHubT(Context* ctx, const HubArgs& h) {
     int per_sm = 0;
     PCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kSmallThreads, smem));
     const unsigned grid = Blocks(h.num_small, 1, sms * unsigned(std::max(per_sm, 1)));
+    FamBegin(ctx, kFamHubSmall);
     k<<<grid, kSmallThreads, smem, ctx->stream>>>(h);
+    FamEnd(ctx, kFamHubSmall, 1);
     PCC_COUNT(1);
   }
   if (h.num_items) {
@@ -611,7 +631,9 @@ Status LaunchHubT(Context* ctx, const HubArgs& h) {
     int per_sm = 0;
     PCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kBigThreads, smem));
     const unsigned grid = Blocks(h.num_items, 1, sms * unsigned(std::max(per_sm, 1)));
+    FamBegin(ctx, kFamHubBig);
     k<<<grid, kBigThreads, smem, ctx->stream>>>(h);
+    FamEnd(ctx, kFamHubBig, 1);
     PCC_COUNT(1);
   }
   return LaunchCheck();

@@ -385,7 +385,13 @@ bool IntModeFor(const DevGraph& g, double offset) {
 class Engine {
  public:
   Engine(Context* ctx, const pcc_config& cfg, bool int_nw)
-      : ctx_(ctx), cfg_(cfg), int_nw_(int_nw), timer_(ctx->stream) {}
+      : ctx_(ctx), cfg_(cfg), int_nw_(int_nw), timer_(ctx->stream), fam_timer_(ctx->stream) {
+    ctx_->fam_timer = &fam_timer_;
+    for (int f = 0; f < kNumFamilies; ++f) ctx_->fam_launches[f] = 0;
+  }
+  ~Engine() { ctx_->fam_timer = nullptr; }
+  Engine(const Engine&) = delete;
+  Engine& operator=(const Engine&) = delete;
 
   Status Init(uint32_t n_max, uint32_t max_deg) {
     n_max_ = n_max;
@@ -721,6 +727,18 @@ class Engine {
 
   const RunResult& result() const { return res_; }
   double PhaseMs(int k) const { return timer_.TotalMs(k); }
+  double FamilyMs(int f) const { return fam_timer_.TotalMs(f); }
+  // Family counters of the call (reads the device counters).
+  Status FamilyCounts(uint64_t* entries, uint64_t* vertices) {
+    DevCounters hc;
+    PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
+    PCC_RETURN_IF_ERROR(Sync(ctx_));
+    for (int f = 0; f < kNumFamilies; ++f) {
+      entries[f] = hc.fam_entries[f];
+      vertices[f] = hc.fam_vertices[f];
+    }
+    return Status::Ok();
+  }
   DevCounters* ctr() { return ctr_.p; }
 
  private:
@@ -736,6 +754,7 @@ class Engine {
   DBuf<DevCounters> ctr_;
   RunResult res_;
   PhaseTimer timer_;
+  PhaseTimer fam_timer_;  // best-move kernel families (kFam*)
 };
 
 // Objective of dense labels L (< n) with node weights k (device, or null).
@@ -917,6 +936,14 @@ Status ClusterImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config* 
     stats->ms_frontier = eng.PhaseMs(kPhaseFrontier);
     stats->kernel_launches = LaunchCounter().load() - launches0;
     stats->algo_bytes_best_moves = eng.result().algo_bytes;
+    uint64_t fe[kNumFamilies], fv[kNumFamilies];
+    PCC_RETURN_IF_ERROR(eng.FamilyCounts(fe, fv));
+    for (int f = 0; f < kNumFamilies; ++f) {
+      stats->family_ms[f] = eng.FamilyMs(f);
+      stats->family_launches[f] = ctx->fam_launches[f];
+      stats->family_entries[f] = fe[f];
+      stats->family_vertices[f] = fv[f];
+    }
   }
   return Status::Ok();
 }

@@ -52,6 +52,20 @@ __device__ __forceinline__ bool Better(double va, uint32_t ia, double vb, uint32
   return va > vb || (va == vb && ia < ib);
 }
 
+// Adds a warp's per-lane counts of evaluated entries and vertices to the
+// kernel family's counters (one atomic per warp; every lane calls).
+__device__ __forceinline__ void FlushFamily(const BMArgs& a, int fam, unsigned long long e, unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    e += __shfl_xor_sync(kFull, e, o);
+    v += __shfl_xor_sync(kFull, v, o);
+  }
+  if (LaneId() == 0 && v) {
+    atomicAdd(&a.ctr->fam_entries[fam], e);
+    atomicAdd(&a.ctr->fam_vertices[fam], v);
+  }
+}
+
 // Wave of vertex v in an async round: a salted MurmurHash3 finalizer of the
 // id, scaled to [0, waves).
 __device__ __forceinline__ uint32_t WaveOf(uint32_t v, uint32_t salt, uint32_t waves) {

@@ -87,10 +87,20 @@ class PccStats(ctypes.Structure):
         ("ms_frontier", ctypes.c_double),
         ("kernel_launches", ctypes.c_uint64),
         ("algo_bytes_best_moves", ctypes.c_uint64),
+        ("family_ms", ctypes.c_double * 4),
+        ("family_launches", ctypes.c_uint64 * 4),
+        ("family_entries", ctypes.c_uint64 * 4),
+        ("family_vertices", ctypes.c_uint64 * 4),
     ]
 
+    FAMILIES = ("groups", "warps", "small_hubs", "big_hubs")
+
     def as_dict(self) -> dict:
-        return {name: getattr(self, name) for name, _ in self._fields_}
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if isinstance(v, ctypes.Array) else v
+        return out
 
 
 def make_config(resolution: float = 0.0, edge_weight_offset: float = 0.0,
