@@ -132,6 +132,9 @@ const char* pcc_last_error(const pcc_context* ctx);
 const char* pcc_version(void);
 /* Bytes of device memory currently held by the context. */
 uint64_t pcc_device_bytes_in_use(const pcc_context* ctx);
+/* High-water mark of the context's device memory since creation or the last
+ * reset (reset != 0 restarts it from the current use). */
+uint64_t pcc_device_peak_bytes(pcc_context* ctx, int32_t reset);
 
 /*
  * Graph upload.  Copies a host CSR graph into HBM.  Replaces
@@ -244,6 +247,74 @@ pcc_status pcc_compress(pcc_context* ctx, const pcc_graph* graph,
 /* Node weights attached to a compressed graph (host double[n]). */
 pcc_status pcc_graph_node_weights(pcc_context* ctx, const pcc_graph* graph,
                                   double* out);
+
+/* ------------------------------------------------------------------------
+ * Batched clustering and the serving loop (no reference counterpart; the
+ * reference clusters one graph per process).  Many independent graphs run
+ * concurrently on one GPU: `concurrency` worker threads each own a context
+ * (its own CUDA stream and memory pool share), so the kernels of different
+ * graphs overlap on the device.  Every result is identical to a call of
+ * pcc_cluster_host_csr on that graph alone.
+ * ---------------------------------------------------------------------- */
+typedef struct pcc_batch_graph {
+  uint32_t n;
+  uint64_t m;
+  const uint64_t* offsets;      /* host CSR, as pcc_graph_upload */
+  const uint32_t* neighbors;
+  const float* weights;         /* NULL = unit weights */
+  const double* node_weights;   /* correlation only; NULL = all 1 */
+} pcc_batch_graph;
+
+/*
+ * Clusters graphs[0..num_graphs).  configs: one config for all graphs
+ * (num_configs == 1) or one per graph; objectives: NULL (all correlation) or
+ * one per graph (0 correlation, 1 modularity).  out_labels[i]: host
+ * uint32[n_i].  stats: NULL or one per graph.  hbm_budget: 0 = none, else
+ * the limit on the device memory all workers hold together.  *wall_ms (may
+ * be NULL) receives the batch's wall time.  The first failing graph's
+ * status is returned; the others stop taking new work.
+ */
+pcc_status pcc_cluster_batch(int device, uint32_t num_graphs, const pcc_batch_graph* graphs,
+                             const pcc_config* configs, uint32_t num_configs,
+                             const int32_t* objectives, uint32_t concurrency,
+                             uint64_t hbm_budget, uint32_t* const* out_labels,
+                             pcc_stats* stats, double* wall_ms);
+
+/*
+ * Serving loop with continuous batching: requests are queued by
+ * pcc_server_submit and admitted, first come first served, as soon as a
+ * worker slot is free and the request's device-memory estimate fits the HBM
+ * budget next to the requests already running; admitted requests run
+ * concurrently.  Each result is identical to a standalone
+ * pcc_cluster_host_csr call.
+ */
+typedef struct pcc_server pcc_server;
+
+pcc_status pcc_server_create(pcc_server** out, int device, uint32_t slots,
+                             uint64_t hbm_budget);
+/* Copies the graph; returns a ticket.  RESOURCE_EXHAUSTED when the request
+ * alone exceeds the budget. */
+pcc_status pcc_server_submit(pcc_server* server, uint32_t n, uint64_t m,
+                             const uint64_t* offsets, const uint32_t* neighbors,
+                             const float* weights, const double* node_weights,
+                             const pcc_config* config, int32_t objective,
+                             uint64_t* ticket);
+/*
+ * Waits up to wait_ms (< 0: no limit) for a request.  When it has finished,
+ * copies its labels (host uint32[n]) and stats (may be NULL), sets
+ * *latency_ms (submit to completion) and *queue_ms (submit to admission),
+ * releases the ticket and returns the request's status.  Returns
+ * DEADLINE_EXCEEDED (ticket kept) while it is still queued or running, and
+ * NOT_FOUND for an unknown ticket.
+ */
+pcc_status pcc_server_wait(pcc_server* server, uint64_t ticket, int32_t wait_ms,
+                           uint32_t* out_labels, pcc_stats* stats,
+                           double* latency_ms, double* queue_ms);
+/* Device-memory estimate the admission control uses for a request. */
+uint64_t pcc_request_bytes_estimate(uint32_t n, uint64_t m, int32_t has_weights);
+/* Finishes the running requests, fails the queued ones (CANCELLED) and
+ * frees the server. */
+void pcc_server_destroy(pcc_server* server);
 
 /*
  * No reference counterpart.  EfficientBestMove (target and value, before the

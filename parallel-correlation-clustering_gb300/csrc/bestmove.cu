@@ -666,9 +666,17 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
   FlushFamily(a, kFamWarp, fam_e, fam_v);
 }
 
+// Sets the kernel's dynamic shared-memory limit once per process (the
+// runtime call takes a lock that serialises concurrent contexts).
 template <class K>
 Status SetSmem(K kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, size_t> done;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = done.find(reinterpret_cast<const void*>(kernel));
+  if (it != done.end() && it->second >= bytes) return Status::Ok();
   PCC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+  done[reinterpret_cast<const void*>(kernel)] = bytes;
   return Status::Ok();
 }
 

@@ -75,12 +75,32 @@ struct Context {
   cudaStream_t stream = nullptr;
   uint64_t budget = 0;             // 0 = device capacity
   std::atomic<uint64_t> in_use{0};
+  std::atomic<uint64_t> peak{0};   // high-water mark of in_use
   std::mutex mu;
   std::unordered_map<void*, uint64_t> sizes;
   std::string last_error;
   // Kernel-family timing of the running call (null when not requested).
   PhaseTimer* fam_timer = nullptr;
   uint64_t fam_launches[kNumFamilies] = {0, 0, 0, 0};
+  // CUDA events reused across calls (event creation takes a runtime lock
+  // that serialises concurrent contexts).
+  std::vector<cudaEvent_t> event_pool;
+  cudaEvent_t GetEvent() {
+    if (event_pool.empty()) {
+      cudaEvent_t e = nullptr;
+      cudaEventCreate(&e);
+      return e;
+    }
+    cudaEvent_t e = event_pool.back();
+    event_pool.pop_back();
+    return e;
+  }
+  void PutEvent(cudaEvent_t e) {
+    if (e) event_pool.push_back(e);
+  }
+  ~Context() {
+    for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
+  }
 
   Status Alloc(void** p, uint64_t bytes) {
     *p = nullptr;
@@ -99,7 +119,10 @@ struct Context {
                            std::to_string(bytes) + " bytes failed: " +
                            cudaGetErrorString(e));
     }
-    in_use += bytes;
+    const uint64_t now = in_use += bytes;
+    uint64_t pk = peak.load();
+    while (now > pk && !peak.compare_exchange_weak(pk, now)) {
+    }
     std::lock_guard<std::mutex> lk(mu);
     sizes[*p] = bytes;
     return Status::Ok();
@@ -186,31 +209,32 @@ inline Status LaunchCheck() {
   return Status::Ok();
 }
 
-// Process-wide count of kernel launches issued by this library; a call
-// reports the difference across its own duration.
-inline std::atomic<uint64_t>& LaunchCounter() {
-  static std::atomic<uint64_t> c{0};
+// Count of kernel launches issued by this library on the calling host
+// thread (a call runs on one thread and reports the difference across its
+// own duration; concurrent calls on other threads do not disturb it).
+inline uint64_t& LaunchCounter() {
+  thread_local uint64_t c = 0;
   return c;
 }
 #define PCC_COUNT(k) (::pcc::LaunchCounter() += (k))
 
 // CUDA-event spans of named phases on the context stream; totals are read
-// after the stream has been synchronised.
+// after the stream has been synchronised.  Events come from the context's
+// pool and go back to it.
 struct PhaseTimer {
-  cudaStream_t stream = nullptr;
+  Context* ctx;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> spans[4];
   cudaEvent_t open[4] = {nullptr, nullptr, nullptr, nullptr};
-  explicit PhaseTimer(cudaStream_t s) : stream(s) {}
+  explicit PhaseTimer(Context* c) : ctx(c) {}
   PhaseTimer(const PhaseTimer&) = delete;
   PhaseTimer& operator=(const PhaseTimer&) = delete;
   void Begin(int k) {
-    cudaEventCreate(&open[k]);
-    cudaEventRecord(open[k], stream);
+    open[k] = ctx->GetEvent();
+    cudaEventRecord(open[k], ctx->stream);
   }
   void End(int k) {
-    cudaEvent_t e;
-    cudaEventCreate(&e);
-    cudaEventRecord(e, stream);
+    cudaEvent_t e = ctx->GetEvent();
+    cudaEventRecord(e, ctx->stream);
     spans[k].emplace_back(open[k], e);
     open[k] = nullptr;
   }
@@ -225,11 +249,10 @@ struct PhaseTimer {
   ~PhaseTimer() {
     for (auto& v : spans)
       for (auto& sp : v) {
-        cudaEventDestroy(sp.first);
-        cudaEventDestroy(sp.second);
+        ctx->PutEvent(sp.first);
+        ctx->PutEvent(sp.second);
       }
-    for (auto e : open)
-      if (e) cudaEventDestroy(e);
+    for (auto e : open) ctx->PutEvent(e);
   }
 };
 inline void FamBegin(Context* ctx, int f) {

@@ -249,6 +249,13 @@ const char* pcc_last_error(const pcc_context* ctx) { return ctx ? ctx->c.last_er
 
 uint64_t pcc_device_bytes_in_use(const pcc_context* ctx) { return ctx ? ctx->c.in_use.load() : 0; }
 
+uint64_t pcc_device_peak_bytes(pcc_context* ctx, int32_t reset) {
+  if (!ctx) return 0;
+  const uint64_t p = ctx->c.peak.load();
+  if (reset) ctx->c.peak.store(ctx->c.in_use.load());
+  return p;
+}
+
 pcc_status pcc_graph_upload(pcc_context* ctx, uint32_t n, uint64_t m, const uint64_t* offsets,
                             const uint32_t* neighbors, const float* weights, pcc_graph** out) {
   try {

@@ -5,7 +5,9 @@
 // float after the offset, the argmax by (value desc, id asc), and "no
 // entries" giving the reduce identity (0, 0.0) unless change >= 0.
 #include <algorithm>
+#include <mutex>
 #include <numeric>
+#include <unordered_map>
 #include <type_traits>
 #include <vector>
 
@@ -609,15 +611,34 @@ __global__ void HubDegreesKernel(const uint32_t* list, uint32_t count, const uin
     deg[i] = static_cast<uint32_t>(off[list[i] + 1] - off[list[i]]);
 }
 
+// Dynamic shared-memory limit and resident CTAs per SM of a kernel, set up
+// and queried once per process (the runtime calls take a lock that
+// serialises concurrent contexts).  Returns 0 on failure.
+template <class K>
+int PrepareOnce(K kernel, int threads, size_t smem) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, int> per_sm_of;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = per_sm_of.find(reinterpret_cast<const void*>(kernel));
+  if (it != per_sm_of.end()) return it->second;
+  int per_sm = 0;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  per_sm_of[reinterpret_cast<const void*>(kernel)] = per_sm;
+  return per_sm;
+}
+
 template <bool kInt, bool kAsync, typename V>
 Status LaunchHubT(Context* ctx, const HubArgs& h) {
   const unsigned sms = unsigned(ctx->num_sms);
   if (h.num_small) {
     constexpr size_t smem = size_t(kSmallSlots) * (sizeof(V) + sizeof(uint32_t));
     auto k = HubSmallKernel<kInt, kAsync, V>;
-    PCC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    int per_sm = 0;
-    PCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kSmallThreads, smem));
+    const int per_sm = PrepareOnce(k, kSmallThreads, smem);
+    if (per_sm <= 0) return MakeError(PCC_INTERNAL, "small-hub kernel cannot be configured");
     const unsigned grid = Blocks(h.num_small, 1, sms * unsigned(std::max(per_sm, 1)));
     FamBegin(ctx, kFamHubSmall);
     k<<<grid, kSmallThreads, smem, ctx->stream>>>(h);
@@ -627,9 +648,8 @@ Status LaunchHubT(Context* ctx, const HubArgs& h) {
   if (h.num_items) {
     constexpr size_t smem = size_t(BigSlots<V>()) * (sizeof(V) + sizeof(uint32_t));
     auto k = HubBigKernel<kInt, kAsync, V>;
-    PCC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    int per_sm = 0;
-    PCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kBigThreads, smem));
+    const int per_sm = PrepareOnce(k, kBigThreads, smem);
+    if (per_sm <= 0) return MakeError(PCC_INTERNAL, "big-hub kernel cannot be configured");
     const unsigned grid = Blocks(h.num_items, 1, sms * unsigned(std::max(per_sm, 1)));
     FamBegin(ctx, kFamHubBig);
     k<<<grid, kBigThreads, smem, ctx->stream>>>(h);

@@ -385,7 +385,7 @@ bool IntModeFor(const DevGraph& g, double offset) {
 class Engine {
  public:
   Engine(Context* ctx, const pcc_config& cfg, bool int_nw)
-      : ctx_(ctx), cfg_(cfg), int_nw_(int_nw), timer_(ctx->stream), fam_timer_(ctx->stream) {
+      : ctx_(ctx), cfg_(cfg), int_nw_(int_nw), timer_(ctx), fam_timer_(ctx) {
     ctx_->fam_timer = &fam_timer_;
     for (int f = 0; f < kNumFamilies; ++f) ctx_->fam_launches[f] = 0;
   }
@@ -830,6 +830,8 @@ Status ComputeModularityDevice(Context* ctx, const DevGraph& g, const uint32_t* 
 
 Status ValidateGraphArgs(pcc_context* ctx, const pcc_graph* graph, const pcc_config* cfg) {
   if (!ctx) return MakeError(PCC_INVALID_ARGUMENT, "null context");
+  // The calling thread may have another device current (worker threads).
+  if (cudaSetDevice(ctx->c.device) != cudaSuccess) return MakeError(PCC_UNAVAILABLE, "cannot select the device");
   if (!graph) return MakeError(PCC_INVALID_ARGUMENT, "null graph");
   if (!cfg) return MakeError(PCC_INVALID_ARGUMENT, "null config");
   if (cfg->move_method < 0 || cfg->move_method > 2)
@@ -883,7 +885,7 @@ Status ClusterImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config* 
   const uint32_t n = g.n;
   PCC_RETURN_IF_ERROR(CheckLabels(initial_labels, n));
   EventTimer timer(ctx->stream);
-  const uint64_t launches0 = LaunchCounter().load();
+  const uint64_t launches0 = LaunchCounter();
   pcc_config cfg = *config;
   DBuf<double> dk;
   DBuf<uint32_t> dinit, dout;
@@ -934,7 +936,7 @@ Status ClusterImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config* 
     stats->ms_compress = eng.PhaseMs(kPhaseCompress);
     stats->ms_apply = eng.PhaseMs(kPhaseApply);
     stats->ms_frontier = eng.PhaseMs(kPhaseFrontier);
-    stats->kernel_launches = LaunchCounter().load() - launches0;
+    stats->kernel_launches = LaunchCounter() - launches0;
     stats->algo_bytes_best_moves = eng.result().algo_bytes;
     uint64_t fe[kNumFamilies], fv[kNumFamilies];
     PCC_RETURN_IF_ERROR(eng.FamilyCounts(fe, fv));

@@ -1,0 +1,328 @@
+// serve.cu -- batched clustering and the serving loop (host code).
+//
+// Many independent graphs run concurrently on one GPU: a pool of worker
+// threads, each owning a context (its own non-blocking CUDA stream), takes
+// requests from a FIFO queue and runs the single-graph path
+// (pcc_cluster_host_csr) on them, so the kernels of different graphs overlap
+// on the device while every result stays identical to a standalone call.
+// Admission is continuous: a queued request starts as soon as a worker is
+// free and its device-memory estimate fits the HBM budget beside the
+// requests already running.  pcc_cluster_batch drives the same pool with
+// requests that point at the caller's arrays; the server copies them.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "common.cuh"
+
+namespace pcc {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double MsBetween(Clock::time_point a, Clock::time_point b) {
+  return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+struct Request {
+  uint64_t ticket = 0;
+  uint32_t n = 0;
+  uint64_t m = 0;
+  // Graph arrays: the owned copies (server) or the caller's arrays (batch).
+  std::vector<uint64_t> off_own;
+  std::vector<uint32_t> nbr_own;
+  std::vector<float> w_own;
+  std::vector<double> k_own;
+  const uint64_t* off = nullptr;
+  const uint32_t* nbr = nullptr;
+  const float* w = nullptr;
+  const double* k = nullptr;
+  pcc_config cfg{};
+  int32_t objective = 0;
+  uint64_t est_bytes = 0;
+  // Results.
+  uint32_t* labels_out = nullptr;       // batch: the caller's array
+  std::vector<uint32_t> labels;         // server: kept until waited for
+  pcc_stats stats{};
+  pcc_stats* stats_out = nullptr;       // batch: the caller's slot
+  pcc_status status = PCC_OK;
+  bool done = false;
+  Clock::time_point t_submit, t_start, t_end;
+};
+
+class Pool {
+ public:
+  Pool(int device, uint32_t slots, uint64_t budget) : device_(device), budget_(budget) {
+    slots_ = std::max<uint32_t>(1, slots);
+  }
+
+  pcc_status Start() {
+    for (uint32_t i = 0; i < slots_; ++i) {
+      pcc_context* c = nullptr;
+      const pcc_status s = pcc_create(&c, device_, 0);
+      if (s != PCC_OK) {
+        Stop();
+        return s;
+      }
+      ctxs_.push_back(c);
+    }
+    for (uint32_t i = 0; i < slots_; ++i) workers_.emplace_back([this, i] { Work(i); });
+    return PCC_OK;
+  }
+
+  // Finishes running requests, cancels queued ones, joins the workers.
+  void Stop() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+      for (Request* r : queue_) Finish(r, PCC_CANCELLED);
+      queue_.clear();
+    }
+    cv_work_.notify_all();
+    for (auto& t : workers_) t.join();
+    workers_.clear();
+    for (pcc_context* c : ctxs_) pcc_destroy(c);
+    ctxs_.clear();
+  }
+
+  ~Pool() { Stop(); }
+
+  pcc_status Submit(Request* r) {
+    r->t_submit = Clock::now();
+    if (budget_ && r->est_bytes > budget_) return PCC_RESOURCE_EXHAUSTED;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (stop_) return PCC_CANCELLED;
+      queue_.push_back(r);
+    }
+    cv_work_.notify_all();
+    return PCC_OK;
+  }
+
+  // Waits until r is done or the deadline passes; true when done.
+  bool Wait(Request* r, int32_t wait_ms) {
+    std::unique_lock<std::mutex> lk(mu_);
+    if (wait_ms < 0) {
+      cv_done_.wait(lk, [&] { return r->done; });
+      return true;
+    }
+    return cv_done_.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return r->done; });
+  }
+
+  std::mutex& mu() { return mu_; }
+
+ private:
+  void Finish(Request* r, pcc_status s) {  // mu_ held
+    r->status = s;
+    r->t_end = Clock::now();
+    r->done = true;
+    cv_done_.notify_all();
+  }
+
+  void Work(uint32_t slot) {
+    pcc_context* ctx = ctxs_[slot];
+    cudaSetDevice(device_);
+    for (;;) {
+      Request* r = nullptr;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        // First come, first served: the head of the queue runs when its
+        // estimate fits beside the admitted requests.
+        cv_work_.wait(lk, [&] {
+          return stop_ || (!queue_.empty() && (!budget_ || reserved_ + queue_.front()->est_bytes <= budget_));
+        });
+        if (stop_) return;
+        r = queue_.front();
+        queue_.pop_front();
+        reserved_ += r->est_bytes;
+        r->t_start = Clock::now();
+      }
+      uint32_t* out = r->labels_out;
+      if (!out) {
+        r->labels.resize(std::max<uint32_t>(r->n, 1));
+        out = r->labels.data();
+      }
+      const pcc_status s = pcc_cluster_host_csr(ctx, r->n, r->m, r->off, r->nbr, r->w, &r->cfg, r->objective,
+                                                r->objective == 1 ? nullptr : r->k, out, &r->stats);
+      if (r->stats_out) *r->stats_out = r->stats;
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        reserved_ -= r->est_bytes;
+        Finish(r, s);
+      }
+      cv_work_.notify_all();  // memory was released: the queue head may fit now
+    }
+  }
+
+  int device_;
+  uint32_t slots_;
+  uint64_t budget_;
+  uint64_t reserved_ = 0;
+  bool stop_ = false;
+  std::vector<pcc_context*> ctxs_;
+  std::vector<std::thread> workers_;
+  std::deque<Request*> queue_;
+  std::mutex mu_;
+  std::condition_variable cv_work_, cv_done_;
+};
+
+}  // namespace
+}  // namespace pcc
+
+using pcc::Clock;
+using pcc::Pool;
+using pcc::Request;
+
+struct pcc_server {
+  std::unique_ptr<Pool> pool;
+  std::mutex mu;
+  uint64_t next_ticket = 1;
+  std::unordered_map<uint64_t, std::unique_ptr<Request>> requests;
+};
+
+extern "C" {
+
+// Device memory of one clustering call: the uploaded CSR and per-level
+// state, the engine's per-round arrays, and the contraction of level 0
+// (sort keys and values with their double buffers) -- the peak -- plus a
+// fixed allowance for pools and small tables.
+uint64_t pcc_request_bytes_estimate(uint32_t n, uint64_t m, int32_t has_weights) {
+  const uint64_t per_entry = 52 + (has_weights ? 8 : 0);
+  return per_entry * m + 192ull * n + (64ull << 20);
+}
+
+pcc_status pcc_cluster_batch(int device, uint32_t num_graphs, const pcc_batch_graph* graphs,
+                             const pcc_config* configs, uint32_t num_configs, const int32_t* objectives,
+                             uint32_t concurrency, uint64_t hbm_budget, uint32_t* const* out_labels,
+                             pcc_stats* stats, double* wall_ms) {
+  if (num_graphs == 0) {
+    if (wall_ms) *wall_ms = 0;
+    return PCC_OK;
+  }
+  if (!graphs || !configs || !out_labels || (num_configs != 1 && num_configs != num_graphs))
+    return PCC_INVALID_ARGUMENT;
+  for (uint32_t i = 0; i < num_graphs; ++i) {
+    if (!out_labels[i] || !graphs[i].offsets || (graphs[i].m && !graphs[i].neighbors)) return PCC_INVALID_ARGUMENT;
+    if (objectives && objectives[i] != 0 && objectives[i] != 1) return PCC_INVALID_ARGUMENT;
+  }
+  const auto t0 = Clock::now();
+  Pool pool(device, std::min(std::max<uint32_t>(concurrency, 1), num_graphs), hbm_budget);
+  pcc_status s = pool.Start();
+  if (s != PCC_OK) return s;
+  std::vector<Request> reqs(num_graphs);
+  for (uint32_t i = 0; i < num_graphs; ++i) {
+    Request& r = reqs[i];
+    const pcc_batch_graph& g = graphs[i];
+    r.ticket = i;
+    r.n = g.n;
+    r.m = g.m;
+    r.off = g.offsets;
+    r.nbr = g.neighbors;
+    r.w = g.weights;
+    r.k = g.node_weights;
+    r.cfg = configs[num_configs == 1 ? 0 : i];
+    r.objective = objectives ? objectives[i] : 0;
+    r.est_bytes = pcc_request_bytes_estimate(g.n, g.m, g.weights != nullptr);
+    r.labels_out = out_labels[i];
+    r.stats_out = stats ? stats + i : nullptr;
+  }
+  pcc_status first = PCC_OK;
+  uint32_t submitted = 0;
+  for (; submitted < num_graphs; ++submitted) {
+    const pcc_status ss = pool.Submit(&reqs[submitted]);
+    if (ss != PCC_OK) {
+      first = ss;
+      break;
+    }
+  }
+  for (uint32_t i = 0; i < submitted; ++i) {
+    pool.Wait(&reqs[i], -1);
+    if (first == PCC_OK && reqs[i].status != PCC_OK) first = reqs[i].status;
+  }
+  pool.Stop();
+  if (wall_ms) *wall_ms = pcc::MsBetween(t0, Clock::now());
+  return first;
+}
+
+pcc_status pcc_server_create(pcc_server** out, int device, uint32_t slots, uint64_t hbm_budget) {
+  if (!out) return PCC_INVALID_ARGUMENT;
+  *out = nullptr;
+  auto s = std::make_unique<pcc_server>();
+  s->pool = std::make_unique<Pool>(device, slots, hbm_budget);
+  const pcc_status st = s->pool->Start();
+  if (st != PCC_OK) return st;
+  *out = s.release();
+  return PCC_OK;
+}
+
+pcc_status pcc_server_submit(pcc_server* server, uint32_t n, uint64_t m, const uint64_t* offsets,
+                             const uint32_t* neighbors, const float* weights, const double* node_weights,
+                             const pcc_config* config, int32_t objective, uint64_t* ticket) {
+  if (!server || !offsets || (m && !neighbors) || !config || !ticket || (objective != 0 && objective != 1))
+    return PCC_INVALID_ARGUMENT;
+  auto r = std::make_unique<Request>();
+  r->n = n;
+  r->m = m;
+  r->off_own.assign(offsets, offsets + uint64_t(n) + 1);
+  r->nbr_own.assign(neighbors, neighbors + m);
+  if (weights) r->w_own.assign(weights, weights + m);
+  if (node_weights) r->k_own.assign(node_weights, node_weights + n);
+  r->off = r->off_own.data();
+  r->nbr = r->nbr_own.data();
+  r->w = weights ? r->w_own.data() : nullptr;
+  r->k = node_weights ? r->k_own.data() : nullptr;
+  r->cfg = *config;
+  r->objective = objective;
+  r->est_bytes = pcc_request_bytes_estimate(n, m, weights != nullptr);
+  Request* raw = r.get();
+  {
+    std::lock_guard<std::mutex> lk(server->mu);
+    r->ticket = server->next_ticket++;
+    *ticket = r->ticket;
+    server->requests[r->ticket] = std::move(r);
+  }
+  const pcc_status s = server->pool->Submit(raw);
+  if (s != PCC_OK) {
+    std::lock_guard<std::mutex> lk(server->mu);
+    server->requests.erase(*ticket);
+    *ticket = 0;
+  }
+  return s;
+}
+
+pcc_status pcc_server_wait(pcc_server* server, uint64_t ticket, int32_t wait_ms, uint32_t* out_labels,
+                           pcc_stats* stats, double* latency_ms, double* queue_ms) {
+  if (!server) return PCC_INVALID_ARGUMENT;
+  Request* r = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(server->mu);
+    auto it = server->requests.find(ticket);
+    if (it == server->requests.end()) return PCC_NOT_FOUND;
+    r = it->second.get();
+  }
+  if (!server->pool->Wait(r, wait_ms)) return PCC_DEADLINE_EXCEEDED;
+  const pcc_status s = r->status;
+  if (s == PCC_OK && out_labels && r->n) std::memcpy(out_labels, r->labels.data(), sizeof(uint32_t) * r->n);
+  if (stats) *stats = r->stats;
+  if (latency_ms) *latency_ms = pcc::MsBetween(r->t_submit, r->t_end);
+  if (queue_ms) *queue_ms = r->t_start.time_since_epoch().count() ? pcc::MsBetween(r->t_submit, r->t_start) : 0.0;
+  std::lock_guard<std::mutex> lk(server->mu);
+  server->requests.erase(ticket);
+  return s;
+}
+
+void pcc_server_destroy(pcc_server* server) {
+  if (!server) return;
+  server->pool->Stop();
+  delete server;
+}
+
+}  // extern "C"

@@ -212,6 +212,24 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.pcc_version.restype = ctypes.c_char_p
     lib.pcc_device_bytes_in_use.argtypes = [vp]
     lib.pcc_device_bytes_in_use.restype = ctypes.c_uint64
+    lib.pcc_device_peak_bytes.argtypes = [vp, ctypes.c_int32]
+    lib.pcc_device_peak_bytes.restype = ctypes.c_uint64
+    lib.pcc_cluster_batch.argtypes = [ctypes.c_int, ctypes.c_uint32, vp, P(PccConfig), ctypes.c_uint32,
+                                      vp, ctypes.c_uint32, ctypes.c_uint64, vp, vp, P(ctypes.c_double)]
+    lib.pcc_cluster_batch.restype = ctypes.c_int
+    lib.pcc_server_create.argtypes = [P(vp), ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64]
+    lib.pcc_server_create.restype = ctypes.c_int
+    lib.pcc_server_submit.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint64, P(ctypes.c_uint64),
+                                      P(ctypes.c_uint32), P(ctypes.c_float), P(ctypes.c_double),
+                                      P(PccConfig), ctypes.c_int32, P(ctypes.c_uint64)]
+    lib.pcc_server_submit.restype = ctypes.c_int
+    lib.pcc_server_wait.argtypes = [vp, ctypes.c_uint64, ctypes.c_int32, P(ctypes.c_uint32), P(PccStats),
+                                    P(ctypes.c_double), P(ctypes.c_double)]
+    lib.pcc_server_wait.restype = ctypes.c_int
+    lib.pcc_server_destroy.argtypes = [vp]
+    lib.pcc_server_destroy.restype = None
+    lib.pcc_request_bytes_estimate.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32]
+    lib.pcc_request_bytes_estimate.restype = ctypes.c_uint64
     lib.pcc_config_default.argtypes = [P(PccConfig)]
     lib.pcc_config_default.restype = None
     lib.pcc_graph_upload.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint64,
@@ -451,6 +469,113 @@ def compress(g: DeviceGraph, cluster_ids, node_weights=None) -> DeviceGraph:
     g.ctx.check(g.ctx.lib.pcc_compress(g.ctx.handle, g.handle, _ptr(C, ctypes.c_uint32),
                                        _ptr(k, ctypes.c_double), ctypes.byref(h)))
     return DeviceGraph(g.ctx, h)
+
+
+class _BatchGraph(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint32), ("m", ctypes.c_uint64), ("offsets", ctypes.c_void_p),
+                ("neighbors", ctypes.c_void_p), ("weights", ctypes.c_void_p), ("node_weights", ctypes.c_void_p)]
+
+
+def cluster_batch(graphs: Sequence[CsrGraph], configs, objectives=None, node_weights=None, concurrency: int = 16,
+                  hbm_budget: int = 0, device: int = 0):
+    """pcc_cluster_batch: clusters independent graphs concurrently on one GPU.
+    configs: one PccConfig or one per graph; objectives: None (correlation)
+    or 0/1 per graph.  Returns (list of label arrays, list of stats dicts,
+    wall ms)."""
+    lib = load_library()
+    ng = len(graphs)
+    keep = []
+    arr = (_BatchGraph * max(ng, 1))()
+    labels = []
+    for i, g in enumerate(graphs):
+        off = np.ascontiguousarray(g.offsets, dtype=np.uint64)
+        nbr = np.ascontiguousarray(g.neighbors, dtype=np.uint32)
+        w = None if g.weights is None else np.ascontiguousarray(g.weights, dtype=np.float32)
+        k = None if node_weights is None or node_weights[i] is None else \
+            np.ascontiguousarray(node_weights[i], dtype=np.float64)
+        keep.append((off, nbr, w, k))
+        arr[i].n = g.n
+        arr[i].m = g.m
+        arr[i].offsets = off.ctypes.data
+        arr[i].neighbors = nbr.ctypes.data if g.m else None
+        arr[i].weights = None if w is None else w.ctypes.data
+        arr[i].node_weights = None if k is None else k.ctypes.data
+        labels.append(np.empty(max(g.n, 1), dtype=np.uint32))
+    if isinstance(configs, PccConfig):
+        cfgs = (PccConfig * 1)(configs)
+        ncfg = 1
+    else:
+        cfgs = (PccConfig * ng)(*configs)
+        ncfg = ng
+    objs = None if objectives is None else np.ascontiguousarray(objectives, dtype=np.int32)
+    outs = (ctypes.c_void_p * max(ng, 1))(*[lab.ctypes.data for lab in labels])
+    stats = (PccStats * max(ng, 1))()
+    wall = ctypes.c_double(0)
+    st = lib.pcc_cluster_batch(device, ng, ctypes.cast(arr, ctypes.c_void_p), cfgs, ncfg,
+                               None if objs is None else objs.ctypes.data, concurrency, hbm_budget,
+                               ctypes.cast(outs, ctypes.c_void_p), ctypes.cast(stats, ctypes.c_void_p),
+                               ctypes.byref(wall))
+    if st != 0:
+        raise PccError(st, "pcc_cluster_batch failed")
+    return [labels[i][:graphs[i].n] for i in range(ng)], [stats[i].as_dict() for i in range(ng)], wall.value
+
+
+class Server:
+    """The serving loop (pcc_server_*): submit requests, wait for results."""
+
+    def __init__(self, slots: int = 8, hbm_budget: int = 0, device: int = 0):
+        self.lib = load_library()
+        self.handle = ctypes.c_void_p()
+        st = self.lib.pcc_server_create(ctypes.byref(self.handle), device, slots, hbm_budget)
+        if st != 0:
+            raise PccError(st, "pcc_server_create failed")
+        self.sizes = {}
+
+    def submit(self, g: CsrGraph, config: PccConfig, objective: int = 0, node_weights=None) -> int:
+        off = np.ascontiguousarray(g.offsets, dtype=np.uint64)
+        nbr = np.ascontiguousarray(g.neighbors, dtype=np.uint32)
+        w = None if g.weights is None else np.ascontiguousarray(g.weights, dtype=np.float32)
+        k = None if node_weights is None else np.ascontiguousarray(node_weights, dtype=np.float64)
+        t = ctypes.c_uint64(0)
+        st = self.lib.pcc_server_submit(self.handle, g.n, g.m, _ptr(off, ctypes.c_uint64),
+                                        _ptr(nbr, ctypes.c_uint32), _ptr(w, ctypes.c_float),
+                                        _ptr(k, ctypes.c_double), ctypes.byref(config), objective, ctypes.byref(t))
+        if st != 0:
+            raise PccError(st, "pcc_server_submit failed")
+        self.sizes[t.value] = g.n
+        return t.value
+
+    def wait(self, ticket: int, wait_ms: int = -1):
+        """Returns (labels, stats dict, latency ms, queue ms), or None while
+        the request is still queued or running (wait_ms >= 0)."""
+        n = self.sizes[ticket]
+        lab = np.empty(max(n, 1), dtype=np.uint32)
+        stt = PccStats()
+        lat = ctypes.c_double(0)
+        qms = ctypes.c_double(0)
+        st = self.lib.pcc_server_wait(self.handle, ticket, wait_ms, _ptr(lab, ctypes.c_uint32), ctypes.byref(stt),
+                                      ctypes.byref(lat), ctypes.byref(qms))
+        if st == 4:  # DEADLINE_EXCEEDED
+            return None
+        del self.sizes[ticket]
+        if st != 0:
+            raise PccError(st, "request failed")
+        return lab[:n], stt.as_dict(), lat.value, qms.value
+
+    def close(self):
+        if self.handle:
+            self.lib.pcc_server_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def request_bytes_estimate(n: int, m: int, weighted: bool) -> int:
+    return int(load_library().pcc_request_bytes_estimate(n, m, 1 if weighted else 0))
 
 
 def labels_to_clustering(labels: Sequence[int]) -> List[List[int]]:

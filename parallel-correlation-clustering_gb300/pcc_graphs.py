@@ -159,3 +159,48 @@ def read_gbbs(path: str) -> CsrGraph:
     nbr = data[2 + n:2 + n + m].astype(np.uint32)
     w = data[2 + n + m:2 + n + 2 * m].astype(np.float32) if header.startswith("Weighted") else None
     return CsrGraph(off, nbr, w)
+
+
+def batch_sbm_spec(count: int, seed: int = 7, n_lo: int = 200, n_hi: int = 50000):
+    """Parameters of the batched SBM workload: n log-uniform in [n_lo, n_hi],
+    blocks uniform in [2, 200] (at most n / 2), mean degree uniform in
+    [8, 32], p_out / p_in = 0.02.  Returns a list of (n, blocks, p_in, p_out,
+    seed) tuples; p_in solves
+    mean degree = p_in * (n / B - 1) + p_out * (n - n / B)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi)))))
+        blocks = int(min(rng.integers(2, 201), max(2, n // 2)))
+        deg = rng.uniform(8.0, 32.0)
+        size = n / blocks
+        p_in = deg / max((size - 1.0) + 0.02 * (n - size), 1e-9)
+        p_in = float(min(p_in, 1.0))
+        out.append((n, blocks, p_in, 0.02 * p_in, int(rng.integers(1, 2**62))))
+    return out
+
+
+def batch_sbm_graphs(count: int, seed: int = 7, n_lo: int = 200, n_hi: int = 50000):
+    """The batched SBM workload's graphs (unit weights)."""
+    return [sbm(n, b, pi, po, s)[0] for (n, b, pi, po, s) in batch_sbm_spec(count, seed, n_lo, n_hi)]
+
+
+def serving_requests(count: int, seed: int = 11, rmat_scale: int = 20, n_hi: int = 50000):
+    """Serving workload: 95% graphs of the batched SBM distribution, 5% RMAT
+    (edge factor 16); resolution from {0.01, 0.1, 0.5}; objective modularity
+    (1) or correlation (0) with equal probability.  Returns a list of dicts
+    (graph, resolution, objective, kind)."""
+    rng = np.random.default_rng(seed)
+    spec = batch_sbm_spec(count, seed + 1, n_hi=n_hi)
+    out = []
+    for i in range(count):
+        if rng.random() < 0.05:
+            g = rmat(rmat_scale, 16, seed=int(rng.integers(1, 2**62)))
+            kind = f"rmat{rmat_scale}"
+        else:
+            n, b, pi, po, s = spec[i]
+            g = sbm(n, b, pi, po, s)[0]
+            kind = "sbm"
+        out.append({"graph": g, "resolution": float(rng.choice([0.01, 0.1, 0.5])),
+                    "objective": int(rng.integers(0, 2)), "kind": kind})
+    return out
