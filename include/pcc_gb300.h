@@ -273,12 +273,44 @@ typedef struct pcc_batch_graph {
  * the limit on the device memory all workers hold together.  *wall_ms (may
  * be NULL) receives the batch's wall time.  The first failing graph's
  * status is returned; the others stop taking new work.
+ *
+ * When num_configs == 1, every objective is correlation and the config is
+ * LOUVAIN, synchronous and without subclustering, the batch runs as disjoint
+ * unions (pcc_cluster_union on one context; stats as documented there).
+ * Otherwise each graph runs on the worker pool and its stats equal a
+ * standalone call's.
  */
 pcc_status pcc_cluster_batch(int device, uint32_t num_graphs, const pcc_batch_graph* graphs,
                              const pcc_config* configs, uint32_t num_configs,
                              const int32_t* objectives, uint32_t concurrency,
                              uint64_t hbm_budget, uint32_t* const* out_labels,
                              pcc_stats* stats, double* wall_ms);
+
+/*
+ * Batched clustering as a disjoint-union graph: graphs that share one
+ * correlation config run as one engine run, and each kernel launch of a
+ * round covers all of them.  Each graph keeps the control flow of
+ * RefineClusters_subroutine
+ * (clustering/clusterers/parallel-correlation-clusterer.cc:476-629) for itself:
+ *   - its own level count;
+ *   - its own inner-loop exit;
+ *   - its own refinement levels;
+ *   - new-cluster ids from its own empty ids.
+ * So its labels and objective equal those of a standalone
+ * pcc_correlation_cluster call (bit for bit with integer weights and node
+ * weights, else within FP64 summation order for the objective).
+ * config: LOUVAIN, synchronous, NONE_SUBCLUSTERING.  Graphs are packed in
+ * order into unions of at most max_union_entries adjacency entries (0:
+ * 2^31) and 2^31 vertices.  out_labels[i]: host uint32[n_i] (may be NULL
+ * when n_i == 0).  stats (NULL or one per graph) carries objective,
+ * num_clusters, levels, rounds, refine_passes and edge_visits of each graph
+ * (the other fields are 0).  batch_stats (may be NULL) receives the totals,
+ * phase times and kernel launches of the whole call.
+ */
+pcc_status pcc_cluster_union(pcc_context* ctx, uint32_t num_graphs, const pcc_batch_graph* graphs,
+                             const pcc_config* config, uint64_t max_union_entries,
+                             uint32_t* const* out_labels, pcc_stats* stats,
+                             pcc_stats* batch_stats);
 
 /*
  * Serving loop with continuous batching: requests are queued by

@@ -83,6 +83,40 @@ Status ComputeGraphProperties(Context* ctx, DevGraph* g);
 // Builds g->bins_all (degree bins including isolated vertices) if absent.
 Status EnsureAllBins(Context* ctx, const DevGraph* g);
 
+// ---------------------------------------------------------------------------
+// Disjoint union of independent graphs (batched clustering).  Graph j owns
+// the vertex ids [vbase[j], vbase[j+1]) at every level: contraction keeps
+// cluster ids as vertex ids (1 + max C vertices), and new-cluster ids and
+// refinement relabels are drawn inside each graph's range, so every graph
+// runs exactly as it would alone, with its ids shifted by vbase[j].
+// ---------------------------------------------------------------------------
+struct UnionLayout {
+  uint32_t B = 0;               // graphs (each with n > 0)
+  std::vector<uint32_t> vbase;  // B + 1 (host)
+  std::vector<uint64_t> ebase;  // B + 1 (host)
+  DBuf<uint32_t> d_vbase;       // B + 1
+};
+
+// Index j < B of the last base[j] <= x (bases ascending): the graph owning
+// vertex id (or entry index) x.
+template <class T>
+__device__ __forceinline__ uint32_t GraphOf(const T* __restrict__ base, uint32_t B, T x) {
+  uint32_t lo = 0, hi = B;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (base[mid] <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Uploads graphs[0..B) (host CSR, each n > 0) as one union graph with
+// shifted offsets and neighbour ids, validating every graph's CSR.  Node
+// weights: *k receives the union's node weights when any graph has them
+// (1 for the graphs without); *int_nw = every node weight is an integer.
+Status UploadUnion(Context* ctx, uint32_t B, const pcc_batch_graph* const* graphs, DevGraph* g, UnionLayout* u,
+                   DBuf<double>* k, bool* int_nw);
+
 // Device counters of one call (all in one allocation).
 struct DevCounters {
   uint32_t bin_count[kNumBins];
@@ -110,6 +144,7 @@ struct DevCounters {
 constexpr int kErrProbeLimit = 1;   // async new-cluster probe exceeded its bound
 constexpr int kErrHashFull = 2;     // a best-move hash table filled up
 constexpr int kErrCertMismatch = 3; // a certified decision differed from FP64 (replay self-check)
+constexpr int kErrUnionRange = 4;   // a union graph's new-cluster id fell outside its range
 
 // Best-move kernel arguments.
 struct BMArgs {

@@ -143,6 +143,125 @@ Status ComputeGraphProperties(Context* ctx, DevGraph* g) {
 
 namespace {
 
+// Union fix-up, vertices: offsets of graph j are shifted by ebase[j] (index
+// vbase[j+1] belongs to graph j+1, whose copy wrote 0 there last); node
+// weights of graphs without them are 1.
+__global__ void UnionVertexFixKernel(uint32_t n, const uint32_t* __restrict__ vbase,
+                                     const uint64_t* __restrict__ ebase, uint32_t B, uint64_t* off, double* k,
+                                     const uint8_t* __restrict__ has_k) {
+  for (uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; v <= n; v += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t j = GraphOf(vbase, B, static_cast<uint32_t>(v));
+    off[v] += ebase[j];
+    if (k && v < n && !has_k[j]) k[v] = 1.0;
+  }
+}
+
+// Union fix-up, entries: local neighbour ids are checked against the
+// graph's own n and shifted by vbase[j]; unweighted graphs get weight 1.
+__global__ void UnionEntryFixKernel(uint64_t m, const uint32_t* __restrict__ vbase,
+                                    const uint64_t* __restrict__ ebase, uint32_t B, uint32_t* nbr, float* w,
+                                    const uint8_t* __restrict__ has_w, int* bad) {
+  for (uint64_t e = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t j = GraphOf(ebase, B, e);
+    const uint32_t x = nbr[e];
+    if (x >= vbase[j + 1] - vbase[j]) {
+      atomicExch(bad, 4);
+      continue;
+    }
+    nbr[e] = x + vbase[j];
+    if (w && !has_w[j]) w[e] = 1.0f;
+  }
+}
+
+}  // namespace
+
+Status UploadUnion(Context* ctx, uint32_t B, const pcc_batch_graph* const* graphs, DevGraph* g, UnionLayout* u,
+                   DBuf<double>* k, bool* int_nw) {
+  if (B == 0) return MakeError(PCC_INVALID_ARGUMENT, "empty union");
+  u->B = B;
+  u->vbase.assign(B + 1, 0);
+  u->ebase.assign(B + 1, 0);
+  bool any_w = false, any_k = false;
+  *int_nw = true;
+  std::vector<uint8_t> has_w(B), has_k(B);
+  for (uint32_t j = 0; j < B; ++j) {
+    const pcc_batch_graph& x = *graphs[j];
+    if (x.n == 0) return MakeError(PCC_INVALID_ARGUMENT, "union graphs must have n > 0");
+    if (!x.offsets || (x.m && !x.neighbors)) return MakeError(PCC_INVALID_ARGUMENT, "null offsets or neighbors");
+    if (x.offsets[0] != 0 || x.offsets[x.n] != x.m)
+      return MakeError(PCC_INVALID_ARGUMENT, "offsets must start at 0 and end at m");
+    const uint64_t nv = uint64_t(u->vbase[j]) + x.n;
+    const uint64_t ne = u->ebase[j] + x.m;
+    if (nv > kMaxVertices) return MakeError(PCC_INVALID_ARGUMENT, "union has more than 2^32 - 32 vertices");
+    if (ne >= 0xFFFFFFFFull) return MakeError(PCC_INVALID_ARGUMENT, "union has 2^32 or more entries");
+    u->vbase[j + 1] = static_cast<uint32_t>(nv);
+    u->ebase[j + 1] = ne;
+    has_w[j] = x.weights != nullptr;
+    has_k[j] = x.node_weights != nullptr;
+    any_w |= has_w[j] != 0;
+    any_k |= has_k[j] != 0;
+    if (x.node_weights)
+      for (uint32_t v = 0; v < x.n && *int_nw; ++v)
+        if (x.node_weights[v] != std::floor(x.node_weights[v])) *int_nw = false;
+  }
+  const uint32_t n = u->vbase[B];
+  const uint64_t m = u->ebase[B];
+  g->n = n;
+  g->m = m;
+  PCC_RETURN_IF_ERROR(g->off.Alloc(ctx, uint64_t(n) + 1));
+  PCC_RETURN_IF_ERROR(g->nbr.Alloc(ctx, m ? m : 1));
+  if (any_w) PCC_RETURN_IF_ERROR(g->w.Alloc(ctx, m ? m : 1));
+  if (any_k) PCC_RETURN_IF_ERROR(k->Alloc(ctx, n));
+  // Stream order matters for the offsets: graph j+1's copy overwrites the
+  // shared index vbase[j+1] (graph j's value m_j) with 0.
+  for (uint32_t j = 0; j < B; ++j) {
+    const pcc_batch_graph& x = *graphs[j];
+    PCC_CUDA(cudaMemcpyAsync(g->off.p + u->vbase[j], x.offsets, sizeof(uint64_t) * (uint64_t(x.n) + 1),
+                             cudaMemcpyHostToDevice, ctx->stream));
+    if (x.m) {
+      PCC_CUDA(cudaMemcpyAsync(g->nbr.p + u->ebase[j], x.neighbors, sizeof(uint32_t) * x.m, cudaMemcpyHostToDevice,
+                               ctx->stream));
+      if (x.weights)
+        PCC_CUDA(cudaMemcpyAsync(g->w.p + u->ebase[j], x.weights, sizeof(float) * x.m, cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    }
+    if (x.node_weights)
+      PCC_CUDA(cudaMemcpyAsync(k->p + u->vbase[j], x.node_weights, sizeof(double) * x.n, cudaMemcpyHostToDevice,
+                               ctx->stream));
+  }
+  DBuf<uint64_t> d_ebase;
+  DBuf<uint8_t> d_has_w, d_has_k;
+  PCC_RETURN_IF_ERROR(u->d_vbase.Alloc(ctx, B + 1));
+  PCC_RETURN_IF_ERROR(d_ebase.Alloc(ctx, B + 1));
+  PCC_RETURN_IF_ERROR(d_has_w.Alloc(ctx, B));
+  PCC_RETURN_IF_ERROR(d_has_k.Alloc(ctx, B));
+  PCC_RETURN_IF_ERROR(u->d_vbase.FromHost(u->vbase.data(), B + 1));
+  PCC_RETURN_IF_ERROR(d_ebase.FromHost(u->ebase.data(), B + 1));
+  PCC_RETURN_IF_ERROR(d_has_w.FromHost(has_w.data(), B));
+  PCC_RETURN_IF_ERROR(d_has_k.FromHost(has_k.data(), B));
+  DBuf<int> bad;
+  PCC_RETURN_IF_ERROR(bad.Alloc(ctx, 1));
+  PCC_RETURN_IF_ERROR(bad.Zero());
+  const unsigned cap = unsigned(ctx->num_sms) * 8;
+  UnionVertexFixKernel<<<Blocks(uint64_t(n) + 1, 256, cap), 256, 0, ctx->stream>>>(
+      n, u->d_vbase.p, d_ebase.p, B, g->off.p, any_k ? k->p : nullptr, d_has_k.p); PCC_COUNT(1);
+  if (m) {
+    UnionEntryFixKernel<<<Blocks(m, 256, cap), 256, 0, ctx->stream>>>(m, u->d_vbase.p, d_ebase.p, B, g->nbr.p,
+                                                                       g->w.p, d_has_w.p, bad.p); PCC_COUNT(1);
+  }
+  CheckCsrKernel<<<Blocks(std::max<uint64_t>(m, uint64_t(n) + 1), 256, cap), 256, 0, ctx->stream>>>(
+      n, m, g->off.p, g->nbr.p, bad.p); PCC_COUNT(1);
+  int hbad = 0;
+  PCC_RETURN_IF_ERROR(bad.ToHost(&hbad, 1));
+  PCC_RETURN_IF_ERROR(Sync(ctx));
+  if (hbad)
+    return MakeError(PCC_INVALID_ARGUMENT,
+                     hbad == 4 ? "neighbor id out of range" : "offsets are not a valid CSR row index");
+  return ComputeGraphProperties(ctx, g);
+}
+
+namespace {
+
 Status Upload(pcc_context* pctx, uint32_t n, uint64_t m, const uint64_t* off, const uint32_t* nbr, const float* w,
               bool device_src, pcc_graph** out) {
   if (!pctx || !out) return MakeError(PCC_INVALID_ARGUMENT, "null context or output");

@@ -240,6 +240,141 @@ __global__ void __launch_bounds__(kT) AssignNewKernel(ApplyArgs a, const uint32_
   }
 }
 
+// ---------------------------------------------------------------------------
+// Disjoint-union kernels (batched graphs; vbase: B + 1 vertex bases).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t LowerBound(const uint32_t* __restrict__ a, uint32_t len, uint32_t x) {
+  uint32_t lo = 0, hi = len;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// New clusters of a union: graph j's i-th new mover (ascending id) takes
+// graph j's i-th empty id (ascending), as it would alone.  Graph j always
+// has at least as many empty ids as new movers (its other clusters hold the
+// rest of its vertices); an index outside graph j's range is reported as
+// kErrUnionRange and skipped.
+__global__ void __launch_bounds__(kT) AssignNewUnionKernel(ApplyArgs a, const uint32_t* __restrict__ zero_ids,
+                                                           const uint32_t* __restrict__ zcount,
+                                                           const uint32_t* __restrict__ new_list,
+                                                           const uint32_t* __restrict__ vbase, uint32_t B) {
+  const uint32_t count = a.ctr->new_movers;
+  const uint32_t zc = *zcount;
+  for (uint64_t i = uint64_t(blockIdx.x) * kT + threadIdx.x; i < count; i += uint64_t(gridDim.x) * kT) {
+    const uint32_t v = new_list[i];
+    const uint32_t j = GraphOf(vbase, B, v);
+    const uint32_t lo = vbase[j];
+    const uint32_t nb = LowerBound(new_list, count, lo);
+    const uint32_t zb = LowerBound(zero_ids, zc, lo);
+    const uint64_t zi = uint64_t(zb) + (i - nb);
+    if (zi >= zc || zero_ids[zi] >= vbase[j + 1]) {
+      atomicExch(&a.ctr->error, kErrUnionRange);
+      continue;
+    }
+    const uint32_t cid = zero_ids[zi];
+    a.C[v] = cid;
+    a.s[cid] = 1u;
+    a.K[cid] = a.k[v];
+    a.mod_stamp[cid] = a.stamp;
+  }
+}
+
+// Per graph: flags[j] = stamp when the frontier (st == stamp) holds a vertex
+// of graph j, and edges[j] += the degrees of those vertices.
+__global__ void __launch_bounds__(kT) GraphFrontierKernel(uint32_t n, const uint64_t* __restrict__ off,
+                                                          const uint32_t* __restrict__ st, uint32_t stamp,
+                                                          const uint32_t* __restrict__ vbase, uint32_t B,
+                                                          uint32_t* flags, unsigned long long* edges) {
+  const uint64_t limit = (uint64_t(n) + 31) & ~uint64_t(31);
+  for (uint64_t v = uint64_t(blockIdx.x) * kT + threadIdx.x; v < limit; v += uint64_t(gridDim.x) * kT) {
+    const bool in = v < n && st[v] == stamp;
+    const uint32_t j = in ? GraphOf(vbase, B, static_cast<uint32_t>(v)) : kNone;
+    const unsigned long long d = in ? off[v + 1] - off[v] : 0ull;
+    const unsigned peers = __match_any_sync(kFull, j);
+    unsigned long long tot = 0;
+    for (unsigned mm = peers; mm; mm &= mm - 1) tot += __shfl_sync(peers, d, __ffs(mm) - 1);
+    if (in && int(LaneId()) == __ffs(peers) - 1) {
+      if (flags[j] != stamp) flags[j] = stamp;
+      if (tot) atomicAdd(&edges[j], tot);
+    }
+  }
+}
+
+// Round-0 frontier of the graphs with mask[j] != 0: st = stamp on their
+// vertices of degree > 0.
+__global__ void __launch_bounds__(kT) MarkGraphsKernel(uint32_t n, const uint64_t* __restrict__ off,
+                                                       const uint32_t* __restrict__ vbase, uint32_t B,
+                                                       const uint32_t* __restrict__ mask, uint32_t* st,
+                                                       uint32_t stamp) {
+  for (uint64_t v = uint64_t(blockIdx.x) * kT + threadIdx.x; v < n; v += uint64_t(gridDim.x) * kT)
+    if (off[v + 1] > off[v] && mask[GraphOf(vbase, B, static_cast<uint32_t>(v))]) st[v] = stamp;
+}
+
+// Per-graph dense rank: out[v] = rank[ids[v]] - rank[vbase[j]] (+ vbase[j]
+// when add_base), rank the exclusive prefix count of the ids in use.
+__global__ void __launch_bounds__(kT) GraphRankKernel(uint32_t n, const uint32_t* __restrict__ ids,
+                                                      const uint32_t* __restrict__ rank, uint32_t* out,
+                                                      const uint32_t* __restrict__ vbase, uint32_t B,
+                                                      int add_base) {
+  for (uint64_t v = uint64_t(blockIdx.x) * kT + threadIdx.x; v < n; v += uint64_t(gridDim.x) * kT) {
+    const uint32_t j = GraphOf(vbase, B, static_cast<uint32_t>(v));
+    out[v] = rank[ids[v]] - rank[vbase[j]] + (add_base ? vbase[j] : 0u);
+  }
+}
+
+// out[j] = rank[vbase[j]] (j < B), out[B] = *total.
+__global__ void GraphRankBaseKernel(uint32_t B, const uint32_t* __restrict__ vbase, const uint32_t* __restrict__ rank,
+                                    const uint32_t* __restrict__ total, uint32_t* out) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j <= B; j += gridDim.x * blockDim.x)
+    out[j] = j < B ? rank[vbase[j]] : *total;
+}
+
+// ids[v] = v on the graphs with mask[j] != 0.
+__global__ void __launch_bounds__(kT) IdentityGraphsKernel(uint32_t n, uint32_t* ids,
+                                                           const uint32_t* __restrict__ vbase, uint32_t B,
+                                                           const uint32_t* __restrict__ mask) {
+  for (uint64_t v = uint64_t(blockIdx.x) * kT + threadIdx.x; v < n; v += uint64_t(gridDim.x) * kT)
+    if (mask[GraphOf(vbase, B, static_cast<uint32_t>(v))]) ids[v] = static_cast<uint32_t>(v);
+}
+
+// Entries of each graph at a level of n vertices.
+__global__ void GraphEntriesKernel(uint32_t B, uint32_t n, const uint32_t* __restrict__ vbase,
+                                   const uint64_t* __restrict__ off, unsigned long long* out) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < B; j += gridDim.x * blockDim.x) {
+    const uint32_t a = vbase[j], b = j + 1 < B ? vbase[j + 1] : n;
+    out[j] = off[b < n ? b : n] - off[a];
+  }
+}
+
+// ComputeObjective (parallel-correlation-clusterer-internal.cc:118-149) per
+// graph of a union: edge[j] = sum over graph j's entries with equal labels
+// of (w - offset) / 2, res[j] = sum over its vertices of k (K[L] - k).  The
+// terms are the single-graph ones; with integer weights and node weights
+// every partial sum is exact, so the result equals the single-graph value.
+__global__ void __launch_bounds__(kT) ObjectiveUnionKernel(uint32_t n, const uint64_t* __restrict__ off,
+                                                           const uint32_t* __restrict__ nbr,
+                                                           const float* __restrict__ w,
+                                                           const uint32_t* __restrict__ L,
+                                                           const double* __restrict__ k,
+                                                           const double* __restrict__ K, double offset,
+                                                           const uint32_t* __restrict__ vbase, uint32_t B,
+                                                           double* edge, double* res) {
+  for (uint64_t u = uint64_t(blockIdx.x) * kT + threadIdx.x; u < n; u += uint64_t(gridDim.x) * kT) {
+    const uint32_t cu = L[u];
+    double x = 0.0;
+    for (uint64_t e = off[u]; e < off[u + 1]; ++e)
+      if (L[nbr[e]] == cu) x += Dsub(static_cast<double>(w ? w[e] : 1.0f), offset) / 2;
+    const double r = Dmul(k[u], Dsub(K[cu], k[u]));
+    const uint32_t j = GraphOf(vbase, B, static_cast<uint32_t>(u));
+    if (x != 0.0) atomicAdd(&edge[j], x);
+    if (r != 0.0) atomicAdd(&res[j], r);
+  }
+}
+
 // Marked vertices for the next frontier.
 
 struct PushNeighbors {  // gbbs::edgeMap with an always-true functor
@@ -537,11 +672,16 @@ class Engine {
       ApplyJoinKernel<<<grid, kT, 0, ctx_->stream>>>(ap); PCC_COUNT(1);
       PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, ZeroSizeInput{L->s.p, ctr_.p},
                                               StoreIndexIfSet{zero_ids_.p}, scan_tiles_,
-                                              static_cast<uint32_t*>(nullptr)));
+                                              un_ ? zcount_.p : static_cast<uint32_t*>(nullptr)));
       PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, NewMoverInput{new_stamp_.p, stamp_, ctr_.p},
                                               StoreIndexIfSet{new_list_.p}, scan_tiles_,
                                               static_cast<uint32_t*>(nullptr)));
-      AssignNewKernel<<<grid, kT, 0, ctx_->stream>>>(ap, zero_ids_.p, new_list_.p); PCC_COUNT(1);
+      if (un_) {
+        AssignNewUnionKernel<<<grid, kT, 0, ctx_->stream>>>(ap, zero_ids_.p, zcount_.p, new_list_.p,
+                                                             un_->d_vbase.p, un_->B); PCC_COUNT(1);
+      } else {
+        AssignNewKernel<<<grid, kT, 0, ctx_->stream>>>(ap, zero_ids_.p, new_list_.p); PCC_COUNT(1);
+      }
       if (n) {
         RefreshKfKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->K.p, L->Kf.p, mod_stamp_.p, stamp_);
         PCC_COUNT(1);
@@ -576,11 +716,21 @@ class Engine {
       CountDegreesKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g.off.p, PredStamp{next_stamp_.p, stamp_},
                                                                     &ctr_.p->pend_edges, &ctr_.p->frontier);
       PCC_COUNT(1);
+      if (un_) {
+        PCC_RETURN_IF_ERROR(gedges_.Zero());
+        GraphFrontierKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g.off.p, next_stamp_.p, stamp_,
+                                                                       un_->d_vbase.p, un_->B, gflags_.p,
+                                                                       gedges_.p); PCC_COUNT(1);
+      }
     }
     PCC_RETURN_IF_ERROR(LaunchCheck());
     timer_.End(kPhaseFrontier);
     DevCounters hc;
     PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
+    if (un_) {
+      PCC_RETURN_IF_ERROR(gflags_.ToHost(h_gflags_.data(), un_->B));
+      PCC_RETURN_IF_ERROR(gedges_.ToHost(h_gedges_.data(), un_->B));
+    }
     PCC_RETURN_IF_ERROR(Sync(ctx_));
     if (!cfg_.async) res_.moves += hc.movers;
     *next_front_stamp = stamp_;
@@ -725,6 +875,242 @@ class Engine {
     return Status::Ok();
   }
 
+  // ---- Disjoint-union mode -------------------------------------------------
+  // What RefineClusters_subroutine would record for one graph run alone.
+  struct GraphRun {
+    int64_t iter = -1;  // the subroutine's final `iter`
+    int32_t levels = 0, rounds = 0, refine_passes = 0;
+    uint64_t edge_visits = 0;
+  };
+
+  // IterateBestMoves for every graph j with in_loop[j], all in the same
+  // rounds.  A graph leaves the loop when its next frontier is empty, as it
+  // would alone; its vertices are then in no frontier, so the rounds the
+  // other graphs still run do not touch it.  Round 0 visits every vertex when
+  // all graphs take part, else the vertices of the taking-part graphs.
+  // moved[j] = the graph's IterateBestMoves result.
+  Status IterateUnion(Level* L, int64_t num_inner, std::vector<uint8_t> in_loop, std::vector<uint8_t>* moved,
+                      std::vector<GraphRun>& gr) {
+    const uint32_t B = un_->B;
+    const DevGraph& g = *L->g;
+    bool all = true, any = false;
+    for (uint32_t j = 0; j < B; ++j) {
+      all &= in_loop[j] != 0;
+      any |= in_loop[j] != 0;
+    }
+    moved->assign(B, 0);
+    if (!any) return Status::Ok();
+    if (!all && cfg_.move_method == PCC_ALL_MOVE)
+      return MakeError(PCC_INTERNAL, "ALL_MOVE union rounds must include every graph");
+    GraphEntriesKernel<<<Blocks(B, kT, 1024), kT, 0, ctx_->stream>>>(B, g.n, un_->d_vbase.p, g.off.p, gedges_.p);
+    PCC_COUNT(1);
+    PCC_RETURN_IF_ERROR(gedges_.ToHost(h_gent_.data(), B));
+    uint32_t front = 0;
+    uint64_t fe = g.m, fs = g.n;
+    if (!all) {
+      for (uint32_t j = 0; j < B; ++j) h_mask_[j] = in_loop[j];
+      PCC_RETURN_IF_ERROR(gmask_.FromHost(h_mask_.data(), B));
+      const uint32_t s0 = ++stamp_;
+      MarkGraphsKernel<<<GridFor(ctx_, g.n), kT, 0, ctx_->stream>>>(g.n, g.off.p, un_->d_vbase.p, B, gmask_.p,
+                                                                    next_stamp_.p, s0); PCC_COUNT(1);
+      PCC_CUDA(cudaMemsetAsync(&ctr_.p->frontier, 0, sizeof(uint32_t), ctx_->stream));
+      PCC_CUDA(cudaMemsetAsync(&ctr_.p->pend_edges, 0, sizeof(unsigned long long), ctx_->stream));
+      CountDegreesKernel<<<GridFor(ctx_, g.n), kT, 0, ctx_->stream>>>(g.n, g.off.p, PredStamp{next_stamp_.p, s0},
+                                                                      &ctr_.p->pend_edges, &ctr_.p->frontier);
+      PCC_COUNT(1);
+      DevCounters hc;
+      PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
+      PCC_RETURN_IF_ERROR(Sync(ctx_));
+      front = s0;
+      fe = hc.pend_edges;
+      fs = hc.frontier;
+    } else {
+      PCC_RETURN_IF_ERROR(Sync(ctx_));
+    }
+    std::vector<unsigned long long> pend(h_gent_.begin(), h_gent_.begin() + B);
+    bool local_moved = true;
+    for (int64_t it = 0; it < num_inner && local_moved; ++it) {
+      for (uint32_t j = 0; j < B; ++j) {
+        if (!in_loop[j]) continue;
+        gr[j].rounds++;
+        gr[j].edge_visits += pend[j];
+      }
+      bool next = false;
+      PCC_RETURN_IF_ERROR(Round(L, front, fe, fs, &next, &front, &fe, &fs));
+      for (uint32_t j = 0; j < B; ++j) {
+        if (!in_loop[j]) continue;
+        if (cfg_.move_method == PCC_ALL_MOVE) {
+          (*moved)[j] = 1;  // local_moved = n > 0 (every round visits every vertex)
+        } else if (h_gflags_[j] == stamp_) {
+          (*moved)[j] = 1;
+          pend[j] = h_gedges_[j];
+        } else {
+          in_loop[j] = 0;
+        }
+      }
+      local_moved = next;
+    }
+    return Status::Ok();
+  }
+
+  // RefineClusters_subroutine (parallel-correlation-clusterer.cc:476-629)
+  // for the B graphs of a disjoint union, each following its own control
+  // flow: a graph whose level did not move stops taking part in later levels
+  // (its vertices stay singletons there), refinement visits a graph only on
+  // the levels below its own final level, and a graph whose final `iter` is
+  // not positive keeps the subroutine's singleton output.  d_out receives
+  // each graph's dense labels (local ids); d_ids the cluster ids behind them
+  // (inside each graph's id range); nclusters[j] the graph's cluster count.
+  Status RunUnion(const DevGraph& g0, const UnionLayout& u, const double* d_k, uint32_t* d_out, uint32_t* d_ids,
+                  std::vector<GraphRun>* runs, std::vector<uint32_t>* nclusters) {
+    if (cfg_.clustering_moves_method != PCC_LOUVAIN)
+      return MakeError(PCC_UNIMPLEMENTED, "union batches need clustering_moves_method LOUVAIN");
+    if (cfg_.subclustering_method != PCC_NONE_SUBCLUSTERING)
+      return MakeError(PCC_UNIMPLEMENTED, "subclustering_method other than NONE_SUBCLUSTERING is not available");
+    if (cfg_.async) return MakeError(PCC_INVALID_ARGUMENT, "union batches run synchronous moves only");
+    const int64_t num_iterations = cfg_.louvain_num_iterations > 0 ? cfg_.louvain_num_iterations : 10;
+    const int64_t num_inner = cfg_.louvain_num_inner_iterations > 0 ? cfg_.louvain_num_inner_iterations : 10;
+    const bool refine = cfg_.refine != 0;
+    const uint32_t n = g0.n, B = u.B;
+    un_ = &u;
+    PCC_RETURN_IF_ERROR(Init(n, g0.max_deg));
+    PCC_RETURN_IF_ERROR(gflags_.Alloc(ctx_, B));
+    PCC_RETURN_IF_ERROR(gflags_.Zero());
+    PCC_RETURN_IF_ERROR(gmask_.Alloc(ctx_, B));
+    PCC_RETURN_IF_ERROR(gedges_.Alloc(ctx_, B));
+    PCC_RETURN_IF_ERROR(zcount_.Alloc(ctx_, 1));
+    h_gflags_.assign(B, 0);
+    h_mask_.assign(B, 0);
+    h_gedges_.assign(B, 0);
+    h_gent_.assign(B, 0);
+    runs->assign(B, GraphRun{});
+    std::vector<GraphRun>& gr = *runs;
+
+    std::vector<std::unique_ptr<Level>> rec;
+    if (refine) rec.resize(static_cast<size_t>(num_iterations));
+    std::unique_ptr<Level> helper;
+    PCC_RETURN_IF_ERROR(MakeLevel(&g0, nullptr, d_k, d_k == nullptr, nullptr, &helper));
+    DBuf<uint32_t> cluster_ids;
+    PCC_RETURN_IF_ERROR(cluster_ids.Alloc(ctx_, n));
+    IotaKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, cluster_ids.p); PCC_COUNT(1);
+
+    std::vector<uint8_t> active(B, 1), moved;
+    int64_t iter = 0;
+    for (iter = 0; iter < num_iterations; ++iter) {
+      PCC_RETURN_IF_ERROR(IterateUnion(helper.get(), num_inner, active, &moved, gr));
+      bool any = false;
+      for (uint32_t j = 0; j < B; ++j) {
+        if (!active[j]) continue;
+        if (!moved[j]) {
+          active[j] = 0;
+          gr[j].iter = iter - 1;
+        } else {
+          gr[j].levels++;
+          any = true;
+        }
+      }
+      if (!any) {
+        iter--;
+        break;
+      }
+      res_.levels++;
+      if (!refine) {
+        FlattenKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, cluster_ids.p, helper->C.p); PCC_COUNT(1);
+      } else if (iter == num_iterations - 1) {
+        rec[static_cast<size_t>(iter)] = std::move(helper);
+      }
+      if (iter == num_iterations - 1) {
+        for (uint32_t j = 0; j < B; ++j)
+          if (active[j]) gr[j].iter = iter;
+        break;
+      }
+      std::unique_ptr<DevGraph> next;
+      timer_.Begin(kPhaseCompress);
+      PCC_RETURN_IF_ERROR(CompressGraph(ctx_, *helper->g, helper->C.p, helper->k.p, &next));
+      timer_.End(kPhaseCompress);
+      DevGraph* ng = next.get();
+      if (ng->n <= u.vbase[B - 1]) return MakeError(PCC_INTERNAL, "union contraction lost a graph's range");
+      std::unique_ptr<Level> nl;
+      PCC_RETURN_IF_ERROR(MakeLevel(ng, std::move(next), ng->node_w.p, false, nullptr, &nl));
+      if (refine) rec[static_cast<size_t>(iter)] = std::move(helper);
+      helper = std::move(nl);
+    }
+
+    DBuf<uint32_t> rank, tot;
+    PCC_RETURN_IF_ERROR(rank.Alloc(ctx_, n));
+    PCC_RETURN_IF_ERROR(tot.Alloc(ctx_, 1));
+    if (refine && iter > 0) {
+      DBuf<uint32_t> flat;
+      PCC_RETURN_IF_ERROR(flat.Alloc(ctx_, n));
+      std::vector<uint8_t> in_loop(B);
+      for (int64_t i = iter - 1; i >= 0; --i) {
+        Level* Li = rec[static_cast<size_t>(i)].get();
+        Level* Lu = rec[static_cast<size_t>(i + 1)].get();
+        const uint32_t ni = Li->g->n, nu = Lu->g->n;
+        stamp_++;
+        ProjectKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->C.p, Lu->C.p, flat.p, aux_stamp_.p,
+                                                                  stamp_); PCC_COUNT(1);
+        PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, nu, StampInput{aux_stamp_.p, stamp_},
+                                                StorePrefix<uint32_t>{rank.p}, scan_tiles_,
+                                                static_cast<uint32_t*>(nullptr)));
+        GraphRankKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, flat.p, rank.p, Li->C.p, u.d_vbase.p, B, 1);
+        PCC_COUNT(1);
+        PCC_RETURN_IF_ERROR(Li->s.Zero());
+        PCC_RETURN_IF_ERROR(Li->K.Zero());
+        AccumulateClustersKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->C.p, Li->k.p, Li->s.p,
+                                                                              Li->K.p); PCC_COUNT(1);
+        RefreshKfKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->K.p, Li->Kf.p, nullptr, 0);
+        PCC_COUNT(1);
+        PCC_RETURN_IF_ERROR(LaunchCheck());
+        for (uint32_t j = 0; j < B; ++j) {
+          in_loop[j] = i <= gr[j].iter - 1;
+          if (in_loop[j]) gr[j].refine_passes++;
+        }
+        PCC_RETURN_IF_ERROR(IterateUnion(Li, num_inner, in_loop, &moved, gr));
+        res_.refine_passes++;
+        rec[static_cast<size_t>(i + 1)].reset();
+      }
+      PCC_CUDA(cudaMemcpyAsync(cluster_ids.p, rec[0]->C.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice,
+                               ctx_->stream));
+      // A graph whose own `iter` is not positive outputs singletons.
+      bool anyid = false;
+      for (uint32_t j = 0; j < B; ++j) {
+        h_mask_[j] = gr[j].iter <= 0;
+        anyid |= h_mask_[j] != 0;
+      }
+      if (anyid) {
+        PCC_RETURN_IF_ERROR(gmask_.FromHost(h_mask_.data(), B));
+        IdentityGraphsKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, cluster_ids.p, u.d_vbase.p, B, gmask_.p);
+        PCC_COUNT(1);
+      }
+    }
+    rec.clear();
+    helper.reset();
+
+    // OutputIndicesById per graph.
+    stamp_++;
+    MarkStampKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, cluster_ids.p, aux_stamp_.p, stamp_); PCC_COUNT(1);
+    PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, StampInput{aux_stamp_.p, stamp_}, StorePrefix<uint32_t>{rank.p},
+                                            scan_tiles_, tot.p));
+    GraphRankKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, cluster_ids.p, rank.p, d_out, u.d_vbase.p, B, 0);
+    PCC_COUNT(1);
+    DBuf<uint32_t> base;
+    PCC_RETURN_IF_ERROR(base.Alloc(ctx_, B + 1));
+    GraphRankBaseKernel<<<Blocks(B + 1, kT, 1024), kT, 0, ctx_->stream>>>(B, u.d_vbase.p, rank.p, tot.p, base.p);
+    PCC_COUNT(1);
+    PCC_CUDA(cudaMemcpyAsync(d_ids, cluster_ids.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, ctx_->stream));
+    std::vector<uint32_t> hb(B + 1);
+    PCC_RETURN_IF_ERROR(base.ToHost(hb.data(), B + 1));
+    DevCounters hc;
+    PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
+    PCC_RETURN_IF_ERROR(Sync(ctx_));
+    if (hc.error) return MakeError(PCC_INTERNAL, "device error flag " + std::to_string(hc.error));
+    nclusters->resize(B);
+    for (uint32_t j = 0; j < B; ++j) (*nclusters)[j] = hb[j + 1] - hb[j];
+    res_.moves += hc.moves;
+    return Status::Ok();
+  }
+
   const RunResult& result() const { return res_; }
   double PhaseMs(int k) const { return timer_.TotalMs(k); }
   double FamilyMs(int f) const { return fam_timer_.TotalMs(f); }
@@ -755,6 +1141,13 @@ class Engine {
   RunResult res_;
   PhaseTimer timer_;
   PhaseTimer fam_timer_;  // best-move kernel families (kFam*)
+  // Disjoint-union mode (null for a single graph): per-graph frontier flags
+  // and degree sums of the round, round-0 masks, the empty-id count.
+  const UnionLayout* un_ = nullptr;
+  DBuf<uint32_t> gflags_, gmask_, zcount_;
+  DBuf<unsigned long long> gedges_;
+  std::vector<uint32_t> h_gflags_, h_mask_;
+  std::vector<unsigned long long> h_gedges_, h_gent_;
 };
 
 // Objective of dense labels L (< n) with node weights k (device, or null).
@@ -950,6 +1343,130 @@ Status ClusterImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config* 
   return Status::Ok();
 }
 
+// One disjoint union: graphs gs (each n > 0), results into out_labels[idx[j]]
+// and stats[idx[j]]; totals added to *tot.
+Status UnionChunk(Context* ctx, const pcc_config& cfg, const std::vector<const pcc_batch_graph*>& gs,
+                  const std::vector<uint32_t>& idx, uint32_t* const* out_labels, pcc_stats* stats, pcc_stats* tot) {
+  const uint32_t B = static_cast<uint32_t>(gs.size());
+  EventTimer timer(ctx->stream);
+  const uint64_t launches0 = LaunchCounter();
+  DevGraph g0;
+  UnionLayout u;
+  DBuf<double> dk;
+  bool int_nw = true;
+  PCC_RETURN_IF_ERROR(UploadUnion(ctx, B, gs.data(), &g0, &u, &dk, &int_nw));
+  const uint32_t n = g0.n;
+  std::vector<Engine::GraphRun> runs;
+  std::vector<uint32_t> ncl;
+  DBuf<uint32_t> dout, dids;
+  PCC_RETURN_IF_ERROR(dout.Alloc(ctx, n));
+  PCC_RETURN_IF_ERROR(dids.Alloc(ctx, n));
+  Engine eng(ctx, cfg, int_nw);
+  PCC_RETURN_IF_ERROR(eng.RunUnion(g0, u, dk.p, dout.p, dids.p, &runs, &ncl));
+  // ComputeObjective per graph.
+  DBuf<double> ones, K, acc;
+  DBuf<uint32_t> s;
+  const double* kp = dk.p;
+  if (!kp) {
+    PCC_RETURN_IF_ERROR(ones.Alloc(ctx, n));
+    FillF64Kernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, 1.0, ones.p); PCC_COUNT(1);
+    kp = ones.p;
+  }
+  PCC_RETURN_IF_ERROR(s.Alloc(ctx, n));
+  PCC_RETURN_IF_ERROR(K.Alloc(ctx, n));
+  PCC_RETURN_IF_ERROR(acc.Alloc(ctx, 2ull * B));
+  PCC_RETURN_IF_ERROR(s.Zero());
+  PCC_RETURN_IF_ERROR(K.Zero());
+  PCC_RETURN_IF_ERROR(acc.Zero());
+  AccumulateClustersKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, dids.p, kp, s.p, K.p); PCC_COUNT(1);
+  ObjectiveUnionKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, g0.off.p, g0.nbr.p, g0.wp(), dids.p, kp, K.p,
+                                                                cfg.edge_weight_offset, u.d_vbase.p, B, acc.p,
+                                                                acc.p + B); PCC_COUNT(1);
+  PCC_RETURN_IF_ERROR(LaunchCheck());
+  std::vector<double> hacc(2ull * B);
+  std::vector<uint32_t> hl(n);
+  PCC_RETURN_IF_ERROR(acc.ToHost(hacc.data(), 2ull * B));
+  PCC_RETURN_IF_ERROR(dout.ToHost(hl.data(), n));
+  PCC_RETURN_IF_ERROR(Sync(ctx));
+  const double ms = timer.StopMs();
+  for (uint32_t j = 0; j < B; ++j) {
+    const uint32_t i = idx[j];
+    std::memcpy(out_labels[i], hl.data() + u.vbase[j], sizeof(uint32_t) * gs[j]->n);
+    if (!stats) continue;
+    pcc_stats& st = stats[i];
+    std::memset(&st, 0, sizeof(st));
+    st.objective = hacc[j] - cfg.resolution * hacc[B + j] / 2;
+    st.num_clusters = static_cast<int32_t>(ncl[j]);
+    st.levels = runs[j].levels;
+    st.rounds = runs[j].rounds;
+    st.refine_passes = runs[j].refine_passes;
+    st.edge_visits = runs[j].edge_visits;
+  }
+  if (tot) {
+    const RunResult& r = eng.result();
+    tot->edge_visits += r.edge_visits;
+    tot->vertex_visits += r.vertex_visits;
+    tot->moves += r.moves;
+    tot->levels = std::max(tot->levels, r.levels);
+    tot->rounds += r.rounds;
+    tot->refine_passes += r.refine_passes;
+    tot->ms_total += ms;
+    tot->ms_best_moves += eng.PhaseMs(kPhaseBestMoves);
+    tot->ms_compress += eng.PhaseMs(kPhaseCompress);
+    tot->ms_apply += eng.PhaseMs(kPhaseApply);
+    tot->ms_frontier += eng.PhaseMs(kPhaseFrontier);
+    tot->kernel_launches += LaunchCounter() - launches0;
+    tot->algo_bytes_best_moves += r.algo_bytes;
+    uint64_t fe[kNumFamilies], fv[kNumFamilies];
+    PCC_RETURN_IF_ERROR(eng.FamilyCounts(fe, fv));
+    for (int f = 0; f < kNumFamilies; ++f) {
+      tot->family_ms[f] += eng.FamilyMs(f);
+      tot->family_launches[f] += ctx->fam_launches[f];
+      tot->family_entries[f] += fe[f];
+      tot->family_vertices[f] += fv[f];
+    }
+  }
+  return Status::Ok();
+}
+
+Status ClusterUnionImpl(pcc_context* pctx, uint32_t num_graphs, const pcc_batch_graph* graphs,
+                        const pcc_config* config, uint64_t max_entries, uint32_t* const* out_labels,
+                        pcc_stats* stats, pcc_stats* batch_stats) {
+  if (!pctx || !config) return MakeError(PCC_INVALID_ARGUMENT, "null context or config");
+  if (num_graphs && (!graphs || !out_labels)) return MakeError(PCC_INVALID_ARGUMENT, "null graphs or out_labels");
+  Context* ctx = &pctx->c;
+  PCC_CUDA(cudaSetDevice(ctx->device));
+  if (batch_stats) std::memset(batch_stats, 0, sizeof(*batch_stats));
+  if (max_entries == 0) max_entries = 1ull << 31;
+  for (uint32_t i = 0; i < num_graphs; ++i) {
+    if (!out_labels[i] && graphs[i].n) return MakeError(PCC_INVALID_ARGUMENT, "null out_labels entry");
+    if (graphs[i].n > kMaxVertices) return MakeError(PCC_INVALID_ARGUMENT, "n must be at most 2^32 - 32");
+    if (graphs[i].m >= 0xFFFFFFFFull)
+      return MakeError(PCC_INVALID_ARGUMENT, "graphs with 2^32 or more entries are not supported");
+    if (graphs[i].n == 0 && stats) std::memset(&stats[i], 0, sizeof(pcc_stats));
+  }
+  std::vector<const pcc_batch_graph*> gs;
+  std::vector<uint32_t> idx;
+  uint64_t nv = 0, ne = 0;
+  for (uint32_t i = 0; i <= num_graphs; ++i) {
+    const bool flush = i == num_graphs ||
+                       (!gs.empty() && (ne + graphs[i].m > max_entries || nv + graphs[i].n > kMaxVertices / 2));
+    if (flush && !gs.empty()) {
+      PCC_RETURN_IF_ERROR(UnionChunk(ctx, *config, gs, idx, out_labels, stats, batch_stats));
+      gs.clear();
+      idx.clear();
+      nv = ne = 0;
+    }
+    if (i == num_graphs) break;
+    if (graphs[i].n == 0) continue;  // empty labels, zero stats
+    gs.push_back(&graphs[i]);
+    idx.push_back(i);
+    nv += graphs[i].n;
+    ne += graphs[i].m;
+  }
+  return Status::Ok();
+}
+
 }  // namespace
 
 }  // namespace pcc
@@ -957,6 +1474,17 @@ Status ClusterImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config* 
 using namespace pcc;
 
 extern "C" {
+
+pcc_status pcc_cluster_union(pcc_context* ctx, uint32_t num_graphs, const pcc_batch_graph* graphs,
+                             const pcc_config* config, uint64_t max_union_entries, uint32_t* const* out_labels,
+                             pcc_stats* stats, pcc_stats* batch_stats) {
+  try {
+    return Finish(ctx, ClusterUnionImpl(ctx, num_graphs, graphs, config, max_union_entries, out_labels, stats,
+                                        batch_stats));
+  } catch (const std::exception& e) {
+    return Finish(ctx, MakeError(PCC_INTERNAL, e.what()));
+  }
+}
 
 pcc_status pcc_correlation_cluster(pcc_context* ctx, const pcc_graph* graph, const pcc_config* config,
                                    const double* node_weights, const uint32_t* initial_labels,

@@ -214,6 +214,24 @@ pcc_status pcc_cluster_batch(int device, uint32_t num_graphs, const pcc_batch_gr
     if (objectives && objectives[i] != 0 && objectives[i] != 1) return PCC_INVALID_ARGUMENT;
   }
   const auto t0 = Clock::now();
+  // One shared correlation config: disjoint unions on one context.
+  bool as_union = num_configs == 1 && configs[0].clustering_moves_method == PCC_LOUVAIN && !configs[0].async &&
+                  configs[0].subclustering_method == PCC_NONE_SUBCLUSTERING;
+  for (uint32_t i = 0; as_union && objectives && i < num_graphs; ++i) as_union = objectives[i] == 0;
+  if (as_union) {
+    pcc_context* c = nullptr;
+    pcc_status s = pcc_create(&c, device, hbm_budget);
+    if (s != PCC_OK) return s;
+    // Under a budget, a union's entries are capped so that its device bytes
+    // (about 60 B per entry plus 192 B per vertex, at most one new vertex
+    // per entry counted) fit next to the fixed 64 MB.
+    const uint64_t fixed = 64ull << 20;
+    const uint64_t cap = hbm_budget == 0 ? 0 : std::max<uint64_t>(1, (hbm_budget > fixed ? hbm_budget - fixed : 0) / 252);
+    s = pcc_cluster_union(c, num_graphs, graphs, configs, cap, out_labels, stats, nullptr);
+    pcc_destroy(c);
+    if (wall_ms) *wall_ms = pcc::MsBetween(t0, Clock::now());
+    return s;
+  }
   Pool pool(device, std::min(std::max<uint32_t>(concurrency, 1), num_graphs), hbm_budget);
   pcc_status s = pool.Start();
   if (s != PCC_OK) return s;

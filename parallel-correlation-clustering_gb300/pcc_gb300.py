@@ -217,6 +217,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.pcc_cluster_batch.argtypes = [ctypes.c_int, ctypes.c_uint32, vp, P(PccConfig), ctypes.c_uint32,
                                       vp, ctypes.c_uint32, ctypes.c_uint64, vp, vp, P(ctypes.c_double)]
     lib.pcc_cluster_batch.restype = ctypes.c_int
+    lib.pcc_cluster_union.argtypes = [vp, ctypes.c_uint32, vp, P(PccConfig), ctypes.c_uint64, vp, vp, vp]
+    lib.pcc_cluster_union.restype = ctypes.c_int
     lib.pcc_server_create.argtypes = [P(vp), ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64]
     lib.pcc_server_create.restype = ctypes.c_int
     lib.pcc_server_submit.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint64, P(ctypes.c_uint64),
@@ -476,13 +478,9 @@ class _BatchGraph(ctypes.Structure):
                 ("neighbors", ctypes.c_void_p), ("weights", ctypes.c_void_p), ("node_weights", ctypes.c_void_p)]
 
 
-def cluster_batch(graphs: Sequence[CsrGraph], configs, objectives=None, node_weights=None, concurrency: int = 16,
-                  hbm_budget: int = 0, device: int = 0):
-    """pcc_cluster_batch: clusters independent graphs concurrently on one GPU.
-    configs: one PccConfig or one per graph; objectives: None (correlation)
-    or 0/1 per graph.  Returns (list of label arrays, list of stats dicts,
-    wall ms)."""
-    lib = load_library()
+def _batch_arrays(graphs, node_weights):
+    """The pcc_batch_graph array (and the numpy arrays it points into) and
+    one label array per graph."""
     ng = len(graphs)
     keep = []
     arr = (_BatchGraph * max(ng, 1))()
@@ -501,6 +499,38 @@ def cluster_batch(graphs: Sequence[CsrGraph], configs, objectives=None, node_wei
         arr[i].weights = None if w is None else w.ctypes.data
         arr[i].node_weights = None if k is None else k.ctypes.data
         labels.append(np.empty(max(g.n, 1), dtype=np.uint32))
+    return arr, keep, labels
+
+
+def cluster_union(ctx: "Context", graphs: Sequence[CsrGraph], config: PccConfig, node_weights=None,
+                  max_union_entries: int = 0):
+    """pcc_cluster_union: independent graphs with one correlation config as
+    disjoint-union engine runs on `ctx`.  Returns (label arrays, per-graph
+    stats dicts, batch stats dict)."""
+    lib = load_library()
+    ng = len(graphs)
+    arr, keep, labels = _batch_arrays(graphs, node_weights)
+    outs = (ctypes.c_void_p * max(ng, 1))(*[lab.ctypes.data for lab in labels])
+    stats = (PccStats * max(ng, 1))()
+    tot = PccStats()
+    st = lib.pcc_cluster_union(ctx.handle, ng, ctypes.cast(arr, ctypes.c_void_p), ctypes.byref(config),
+                               max_union_entries, ctypes.cast(outs, ctypes.c_void_p),
+                               ctypes.cast(stats, ctypes.c_void_p), ctypes.byref(tot))
+    del keep
+    ctx.check(st)
+    return [labels[i][:graphs[i].n] for i in range(ng)], [stats[i].as_dict() for i in range(ng)], tot.as_dict()
+
+
+def cluster_batch(graphs: Sequence[CsrGraph], configs, objectives=None, node_weights=None, concurrency: int = 16,
+                  hbm_budget: int = 0, device: int = 0):
+    """pcc_cluster_batch: clusters independent graphs on one GPU (disjoint
+    unions for one shared correlation config, else the concurrent worker
+    pool).  configs: one PccConfig or one per graph; objectives: None
+    (correlation) or 0/1 per graph.  Returns (list of label arrays, list of
+    stats dicts, wall ms)."""
+    lib = load_library()
+    ng = len(graphs)
+    arr, keep, labels = _batch_arrays(graphs, node_weights)
     if isinstance(configs, PccConfig):
         cfgs = (PccConfig * 1)(configs)
         ncfg = 1

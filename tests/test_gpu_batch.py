@@ -20,16 +20,111 @@ def small_graphs(built):
     return G.batch_sbm_graphs(40, seed=3, n_lo=200, n_hi=4000)
 
 
+UNION_STATS = ("objective", "num_clusters", "levels", "rounds", "refine_passes", "edge_visits")
+
+
 def test_batch_matches_single_calls(ctx, small_graphs):
+    """One shared correlation config: the batch runs as a disjoint union;
+    labels, objective and the per-graph control-flow counters equal the
+    standalone call's."""
     cfg = P.make_config(resolution=0.05, refine=True)
     labels, stats, wall = P.cluster_batch(small_graphs, cfg, concurrency=8)
     assert wall > 0
     for g, lab, st in zip(small_graphs, labels, stats):
         ref, rst = _single(ctx, g, cfg, 0)
         np.testing.assert_array_equal(lab, ref)
+        for key in UNION_STATS:
+            assert st[key] == rst[key], key
+
+
+def test_pool_batch_matches_single_calls(ctx, small_graphs):
+    """Per-graph configs run on the worker pool: every stat of the
+    standalone call, launches included, is reproduced."""
+    cfg = P.make_config(resolution=0.05, refine=True)
+    graphs = small_graphs[:16]
+    labels, stats, wall = P.cluster_batch(graphs, [cfg] * len(graphs), concurrency=8)
+    assert wall > 0
+    for g, lab, st in zip(graphs, labels, stats):
+        ref, rst = _single(ctx, g, cfg, 0)
+        np.testing.assert_array_equal(lab, ref)
         assert st["objective"] == rst["objective"]
         assert st["edge_visits"] == rst["edge_visits"] and st["rounds"] == rst["rounds"]
         assert st["kernel_launches"] == rst["kernel_launches"]
+
+
+def _union_mix():
+    """SBMs, an RMAT graph with hubs above both hub thresholds, a graph with
+    isolated vertices, an edgeless graph, an empty graph and a triangle."""
+    out = list(G.batch_sbm_graphs(6, seed=21, n_lo=200, n_hi=3000))
+    out.insert(2, G.rmat(13, 16, seed=5))
+    rng = np.random.default_rng(4)
+    src = rng.integers(0, 300, 900)
+    dst = rng.integers(0, 300, 900)
+    out.insert(4, P.CsrGraph.from_edges(500, src, dst, drop_self_loops=True))   # ids 300-499 isolated
+    out.append(P.CsrGraph(np.zeros(41, np.uint64), np.zeros(0, np.uint32)))      # 40 vertices, no edges
+    out.insert(1, P.CsrGraph(np.zeros(1, np.uint64), np.zeros(0, np.uint32)))    # n = 0
+    out.append(P.CsrGraph.from_edges(3, [0, 1, 2], [1, 2, 0]))
+    return out
+
+
+@pytest.mark.parametrize("move", [P.NBHR_CLUSTER_MOVE, P.NBHR_MOVE, P.ALL_MOVE])
+@pytest.mark.parametrize("refine", [True, False])
+def test_union_matches_single_every_control_path(ctx, move, refine):
+    """Graphs stop their levels, inner loops and refinement at different
+    points; each must follow its own standalone control flow.  Small
+    iteration caps make the caps bind; a small entry cap splits the batch
+    into several unions."""
+    graphs = _union_mix()
+    for iters, inner, cap in [(0, 0, 0), (3, 2, 0), (4, 10, 200_000)]:
+        cfg = P.make_config(resolution=0.05, refine=refine, move_method=move,
+                            louvain_num_iterations=iters, louvain_num_inner_iterations=inner)
+        labels, stats, tot = P.cluster_union(ctx, graphs, cfg, max_union_entries=cap)
+        assert tot["kernel_launches"] > 0
+        for i, g in enumerate(graphs):
+            if g.n == 0:
+                assert len(labels[i]) == 0 and stats[i]["num_clusters"] == 0
+                continue
+            ref, rst = _single(ctx, g, cfg, 0)
+            np.testing.assert_array_equal(labels[i], ref, err_msg=f"graph {i} iters {iters}")
+            for key in UNION_STATS:
+                assert stats[i][key] == rst[key], (i, key, iters)
+
+
+def test_union_node_weights_and_real_weights(ctx, small_graphs):
+    """Integer node weights keep every sum exact (bit-identical objective);
+    real edge weights take the FP64 path (labels identical, objective within
+    FP64 summation order)."""
+    graphs = small_graphs[:10]
+    cfg = P.make_config(resolution=0.05, refine=True)
+    kw = [None if i % 2 else (np.arange(g.n) % 4 + 1.0) for i, g in enumerate(graphs)]
+    labels, stats, _ = P.cluster_union(ctx, graphs, cfg, node_weights=kw)
+    for i, g in enumerate(graphs):
+        ref, rst = P.cluster_host_csr(ctx, g, cfg, objective=0, node_weights=kw[i])
+        np.testing.assert_array_equal(labels[i], ref)
+        assert stats[i]["objective"] == rst["objective"]
+    rng = np.random.default_rng(8)
+    real = []
+    for g in graphs[:6]:
+        d = np.repeat(np.arange(g.n), np.diff(g.offsets).astype(np.int64))
+        src, dst = d[d < g.neighbors], g.neighbors[d < g.neighbors]
+        real.append(P.CsrGraph.from_edges(g.n, src, dst, rng.uniform(0.5, 1.5, len(src))))
+    cfg = P.make_config(resolution=0.1, refine=True, move_method=P.NBHR_CLUSTER_MOVE)
+    labels, stats, _ = P.cluster_union(ctx, real, cfg)
+    for i, g in enumerate(real):
+        ref, rst = _single(ctx, g, cfg, 0)
+        np.testing.assert_array_equal(labels[i], ref)
+        assert stats[i]["objective"] == pytest.approx(rst["objective"], rel=1e-12, abs=1e-9)
+
+
+def test_union_rejects_bad_input(ctx):
+    good = P.CsrGraph.from_edges(3, [0, 1], [1, 2])
+    bad = P.CsrGraph(np.array([0, 1, 2], np.uint64), np.array([1, 2], np.uint32))   # neighbour 2 >= n
+    with pytest.raises(P.PccError) as e:
+        P.cluster_union(ctx, [good, bad], P.make_config(resolution=0.1))
+    assert e.value.code == 3
+    with pytest.raises(P.PccError) as e:
+        P.cluster_union(ctx, [good], P.make_config(resolution=0.1, async_=True))
+    assert e.value.code == 3
 
 
 def test_batch_mixed_configs_and_objectives(ctx, small_graphs):
