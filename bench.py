@@ -17,6 +17,12 @@ round, level and refinement pass, identically to the oracle.
   --impl reference   the oracle (the CPU restatement of the reference
           clusterer) on the host cores, same config, bounded sample
 
+Two more workloads ride on the same JSON line (rank 0, one GPU each):
+  batched   4096 SBM graphs through the batch call (disjoint unions), in
+            graphs/s end to end, beside one call per graph on a sample
+  serving   the continuous-batching server under Poisson arrivals: closed-
+            loop capacity and p50/p99 latency at 0.5x and 0.9x of it
+
 Multi-GPU: the path does not shard (a Louvain round needs the whole graph's
 cluster state), so N GPUs run N independent replicas ("replicas only").
 """
@@ -61,6 +67,13 @@ def parse_args():
     ap.add_argument("--cpu-scale", type=int, default=20,
                     help="RMAT scale of the bounded CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-graphs", type=int, default=4096,
+                    help="graphs of the batched SBM leg (0 = skip the leg)")
+    ap.add_argument("--batch-sample", type=int, default=256,
+                    help="graphs clustered one call each for the per-graph baseline")
+    ap.add_argument("--serve-requests", type=int, default=240,
+                    help="requests of the serving leg (0 = skip the leg)")
+    ap.add_argument("--serve-slots", type=int, default=8)
     return ap.parse_args()
 
 
@@ -165,6 +178,95 @@ def cpu_baseline(args, P, G):
         "sample": f"one full clustering of RMAT scale {args.cpu_scale} (n={g.n}, m={g.m}) with the same "
                   f"config; {st['edge_visits']} edge visits in {dt:.2f} s",
         "modularity": st["modularity"],
+    }
+
+
+def batched_leg(args, P, G, ctx):
+    """Batched SBM workload: graphs with n log-uniform in [200, 50000],
+    blocks U[2, 200], mean degree U[8, 32], p_out/p_in = 0.02, unit weights;
+    correlation, resolution 0.05, refine.  Timed end to end through the
+    public batch call (host CSR in, host labels out: upload, clustering and
+    download inside the timed region).  The per-graph baseline is one
+    pcc_cluster_host_csr call per graph on a sample of the same graphs; the
+    batch's labels and objectives must equal those calls'."""
+    import numpy as np
+    graphs = G.batch_sbm_graphs(args.batch_graphs, seed=7)
+    cfg = P.make_config(resolution=0.05, refine=True)
+    sample = graphs[:min(args.batch_sample, len(graphs))]
+    P.cluster_batch(graphs[:64], cfg)
+    for g in sample[:4]:
+        P.cluster_host_csr(ctx, g, cfg)
+    t = time.perf_counter()
+    ref = [P.cluster_host_csr(ctx, g, cfg) for g in sample]
+    plain_s = time.perf_counter() - t
+    t = time.perf_counter()
+    labels, stats, wall_ms = P.cluster_batch(graphs, cfg)
+    batch_s = time.perf_counter() - t
+    identical = all(np.array_equal(lab, r[0]) and st["objective"] == r[1]["objective"]
+                    for lab, st, r in zip(labels, stats, ref))
+    value = len(graphs) / batch_s
+    plain = len(sample) / plain_s
+    return {
+        "workload": "batched_sbm_correlation_refine",
+        "graphs": len(graphs), "n_total": int(sum(g.n for g in graphs)), "m_total": int(sum(g.m for g in graphs)),
+        "value": value, "unit": "graphs/s", "ms_per_batch": 1000.0 * batch_s,
+        "per_graph_calls": {"value": plain, "unit": "graphs/s", "sample_graphs": len(sample)},
+        "speedup_vs_per_graph_calls": value / plain,
+        "identical_to_per_graph_calls": bool(identical),
+        "path": "pcc_cluster_batch -> disjoint unions (pcc_cluster_union), host buffers in and out",
+    }
+
+
+def serving_leg(args, P, G, ctx):
+    """Serving workload: 95% graphs of the batched SBM distribution, 5% RMAT
+    scale 20 (edge factor 16; two distinct graphs reused), resolution from
+    {0.01, 0.1, 0.5}, modularity or correlation with equal probability,
+    120 GB HBM budget, `--serve-slots` concurrent slots.  Capacity is the
+    closed-loop rate (every request queued at once); then Poisson arrivals at
+    0.5x and 0.9x that rate give latency percentiles (submit to completion).
+    Sampled responses must equal standalone calls."""
+    import numpy as np
+    reqs = G.serving_requests(args.serve_requests, seed=11, rmat_scale=20, distinct_rmat=2)
+    cfgs = [P.make_config(resolution=r["resolution"], refine=True) for r in reqs]
+    srv = P.Server(slots=args.serve_slots, hbm_budget=120 << 30)
+    try:
+        for r, c in list(zip(reqs, cfgs))[:8]:
+            srv.wait(srv.submit(r["graph"], c, r["objective"]))
+        t0 = time.perf_counter()
+        tickets = [srv.submit(r["graph"], c, r["objective"]) for r, c in zip(reqs, cfgs)]
+        closed = [srv.wait(t) for t in tickets]
+        capacity = len(reqs) / (time.perf_counter() - t0)
+        loads = []
+        for frac in (0.5, 0.9):
+            lam = frac * capacity
+            arrivals = np.cumsum(np.random.default_rng(13).exponential(1.0 / lam, len(reqs)))
+            start = time.perf_counter()
+            tickets = []
+            for i, (r, c) in enumerate(zip(reqs, cfgs)):
+                d = start + arrivals[i] - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                tickets.append(srv.submit(r["graph"], c, r["objective"]))
+            res = [srv.wait(t) for t in tickets]
+            total = time.perf_counter() - start
+            lat = np.array([x[2] for x in res])
+            q = np.array([x[3] for x in res])
+            loads.append({"offered_graphs_per_s": lam, "achieved_graphs_per_s": len(reqs) / total,
+                          "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                          "mean_queue_ms": float(q.mean())})
+    finally:
+        srv.close()
+    pick = [i for i, r in enumerate(reqs) if r["kind"] != "sbm"][:2] + list(range(0, len(reqs), max(len(reqs) // 12, 1)))
+    identical = True
+    for i in pick:
+        ref, _ = P.cluster_host_csr(ctx, reqs[i]["graph"], cfgs[i], objective=reqs[i]["objective"])
+        identical &= bool(np.array_equal(closed[i][0], ref))
+    return {
+        "workload": "serving_sbm95_rmat20_5pct_mixed_objectives",
+        "requests": len(reqs), "slots": args.serve_slots, "hbm_budget_gb": 120,
+        "value": capacity, "unit": "graphs/s", "note": "value = closed-loop capacity",
+        "loads": loads,
+        "identical_to_standalone_on_sample": identical, "sample_requests": len(pick),
     }
 
 
@@ -313,6 +415,14 @@ def main():
         a_mod.append(st["modularity"])
     barrier()
 
+    # Batched and serving workloads (rank 0; one GPU each).
+    batched = serving = None
+    if rank == 0 and args.batch_graphs > 0:
+        batched = batched_leg(args, P, G, ctx)
+    if rank == 0 and args.serve_requests > 0:
+        serving = serving_leg(args, P, G, ctx)
+    barrier()
+
     # Max time over ranks; edge visits summed over ranks.
     dev_s = dev_ms / 1000.0
     if dist is not None:
@@ -377,6 +487,8 @@ def main():
             "modes": {"async": {"value": a_ev / (a_ms / 1000.0) if a_ms > 0 else None, "unit": UNIT,
                                 "ms_per_step": a_ms / args.steps, "modularity_mean": sum(a_mod) / len(a_mod),
                                 "note": "same graph and config with async=true, 16 waves per round"}},
+            "batched": batched,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

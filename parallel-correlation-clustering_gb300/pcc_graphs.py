@@ -185,17 +185,25 @@ def batch_sbm_graphs(count: int, seed: int = 7, n_lo: int = 200, n_hi: int = 500
     return [sbm(n, b, pi, po, s)[0] for (n, b, pi, po, s) in batch_sbm_spec(count, seed, n_lo, n_hi)]
 
 
-def serving_requests(count: int, seed: int = 11, rmat_scale: int = 20, n_hi: int = 50000):
+def serving_requests(count: int, seed: int = 11, rmat_scale: int = 20, n_hi: int = 50000,
+                     distinct_rmat: int = 0):
     """Serving workload: 95% graphs of the batched SBM distribution, 5% RMAT
     (edge factor 16); resolution from {0.01, 0.1, 0.5}; objective modularity
-    (1) or correlation (0) with equal probability.  Returns a list of dicts
-    (graph, resolution, objective, kind)."""
+    (1) or correlation (0) with equal probability.  distinct_rmat > 0 reuses
+    that many RMAT graphs (generation time) instead of one per request.
+    Returns a list of dicts (graph, resolution, objective, kind)."""
     rng = np.random.default_rng(seed)
     spec = batch_sbm_spec(count, seed + 1, n_hi=n_hi)
     out = []
+    rmats = []
     for i in range(count):
         if rng.random() < 0.05:
-            g = rmat(rmat_scale, 16, seed=int(rng.integers(1, 2**62)))
+            rseed = int(rng.integers(1, 2**62))
+            if distinct_rmat and len(rmats) >= distinct_rmat:
+                g = rmats[len(out) % distinct_rmat]
+            else:
+                g = rmat(rmat_scale, 16, seed=rseed)
+                rmats.append(g)
             kind = f"rmat{rmat_scale}"
         else:
             n, b, pi, po, s = spec[i]
