@@ -17,7 +17,9 @@ round, level and refinement pass, identically to the oracle.
   --impl reference   the oracle (the CPU restatement of the reference
           clusterer) on the host cores, same config, bounded sample
 
-Two more workloads ride on the same JSON line (rank 0, one GPU each):
+Three more workloads ride on the same JSON line (rank 0, one GPU each):
+  lfr       LFR-like graph, 8M vertices, real weights (FP64 mode), in the
+            same edge-visits/s metric, with the oracle on a 1M-vertex sample
   batched   4096 SBM graphs through the batch call (disjoint unions), in
             graphs/s end to end, beside one call per graph on a sample
   serving   the continuous-batching server under Poisson arrivals: closed-
@@ -74,6 +76,8 @@ def parse_args():
     ap.add_argument("--serve-requests", type=int, default=240,
                     help="requests of the serving leg (0 = skip the leg)")
     ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--lfr-n", type=int, default=8_000_000,
+                    help="vertices of the LFR-like real-weight leg (0 = skip the leg)")
     return ap.parse_args()
 
 
@@ -215,6 +219,49 @@ def batched_leg(args, P, G, ctx):
         "identical_to_per_graph_calls": bool(identical),
         "path": "pcc_cluster_batch -> disjoint unions (pcc_cluster_union), host buffers in and out",
     }
+
+
+def lfr_leg(args, P, G, ctx, dist_steps: int = 2):
+    """LFR-like planted partition with real weights (FP64 mode): degrees
+    power-law(2.2, mean 20, max 2000), community sizes power-law(2.5,
+    5..5000), mixing 0.3, weights U[0.5, 1.5] stored as float32;
+    correlation, resolution 0.1, refine, NBHR_CLUSTER_MOVE, permute, sync.
+    Graph resident in HBM; the oracle runs the same config on a 1M-vertex
+    graph of the same distribution (bounded CPU sample)."""
+    g, _ = G.lfr(args.lfr_n, mean_degree=20, dmax=2000, seed=6)
+    cfg = P.make_config(resolution=0.1, refine=True, move_method=P.NBHR_CLUSTER_MOVE, permute=True, random_seed=1)
+    dg = ctx.upload(g)
+    P.correlation_cluster(dg, cfg)
+    ev, ms = 0, 0.0
+    st = None
+    for _ in range(dist_steps):
+        _, st = P.correlation_cluster(dg, cfg)
+        ev += st["edge_visits"]
+        ms += st["ms_total"]
+    dg.free()
+    out = {
+        "workload": "lfr_like_real_weights_correlation_refine_nbhr_cluster_sync",
+        "n": g.n, "m_entries": g.m, "dtype": "f64 (real weights: FP64 best moves)",
+        "value": ev / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / dist_steps,
+        "objective": st["objective"], "num_clusters": st["num_clusters"], "levels": st["levels"],
+        "rounds": st["rounds"],
+        "phases_ms_per_step": {"best_moves": st["ms_best_moves"], "compress": st["ms_compress"],
+                               "apply": st["ms_apply"], "frontier": st["ms_frontier"]},
+    }
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, ORACLE_DIR)
+        import oracle as O
+        O.set_threads(0)
+        gs, _ = G.lfr(1_000_000, mean_degree=20, dmax=2000, seed=6)
+        og = O.OracleGraph(gs)
+        t = time.perf_counter()
+        _, so = O.correlation_cluster(og, cfg)
+        dt = time.perf_counter() - t
+        out["cpu_baseline"] = {"value": so["edge_visits"] / dt, "unit": UNIT, "cores": O.get_threads(),
+                               "kind": "port",
+                               "sample": f"one clustering of a 1M-vertex graph of the same distribution "
+                                         f"(m={gs.m}) in {dt:.2f} s"}
+    return out
 
 
 def serving_leg(args, P, G, ctx):
@@ -416,7 +463,9 @@ def main():
     barrier()
 
     # Batched and serving workloads (rank 0; one GPU each).
-    batched = serving = None
+    batched = serving = lfr = None
+    if rank == 0 and args.lfr_n > 0:
+        lfr = lfr_leg(args, P, G, ctx)
     if rank == 0 and args.batch_graphs > 0:
         batched = batched_leg(args, P, G, ctx)
     if rank == 0 and args.serve_requests > 0:
@@ -487,6 +536,7 @@ def main():
             "modes": {"async": {"value": a_ev / (a_ms / 1000.0) if a_ms > 0 else None, "unit": UNIT,
                                 "ms_per_step": a_ms / args.steps, "modularity_mean": sum(a_mod) / len(a_mod),
                                 "note": "same graph and config with async=true, 16 waves per round"}},
+            "lfr": lfr,
             "batched": batched,
             "serving": serving,
         }
