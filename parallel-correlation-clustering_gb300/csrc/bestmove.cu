@@ -443,8 +443,12 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
     const int Tsh = __shfl_sync(kFull, S, tmask ? __ffs(tmask) - 1 : int(lane));
     const int T = tmask ? Tsh : 0;  // group sums stay below 2^29 in INT mode
     int smax = leader ? S : INT_MIN;
+    if constexpr (G == 32) {
+      smax = __reduce_max_sync(kFull, smax);
+    } else {
 #pragma unroll
-    for (int o = G / 2; o >= 1; o >>= 1) smax = max(smax, __shfl_xor_sync(kFull, smax, o));
+      for (int o = G / 2; o >= 1; o >>= 1) smax = max(smax, __shfl_xor_sync(kFull, smax, o));
+    }
     const float k32 = vvalid ? a.kf[x.v] : 0.f;
     const float Kc32 = vvalid ? a.Kf[x.c] : 0.f;
     const ChangeApproxT<int> ca = ApproxChange<int>(a.res32, a.int_nw != 0, k32, Kc32, T);
@@ -459,8 +463,12 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
       if (f.sane) lo = __fsub_rn(f.Y, f.e);
     }
     float U = lo;
+    if constexpr (G == 32) {
+      U = WarpMaxFinite(U);
+    } else {
 #pragma unroll
-    for (int o = G / 2; o >= 1; o >>= 1) U = fmaxf(U, __shfl_xor_sync(kFull, U, o));
+      for (int o = G / 2; o >= 1; o >>= 1) U = fmaxf(U, __shfl_xor_sync(kFull, U, o));
+    }
     const bool contender = leader && (!f.sane || __fadd_rn(f.Y, f.e) >= U);
     // The leading (S, K) class of the contenders and the trailing one.
     LexKeyT<int> lead, tail;
@@ -471,9 +479,14 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
       lead.Keep(S, ko, cu);
       tail.Keep(-S, ~ko, cu);
     }
-    LexGroupReduce<G>(lead);
-    LexGroupReduce<G>(tail);
-    const bool single = lead.id == kNone || (-tail.S == lead.S && ~tail.K == lead.K);
+    bool single;
+    if constexpr (G == 32) {
+      single = LexWarpLeadInt(lead, tail);
+    } else {
+      LexGroupReduce<G>(lead);
+      LexGroupReduce<G>(tail);
+      single = lead.id == kNone || (-tail.S == lead.S && ~tail.K == lead.K);
+    }
     int cres = kUncertain;
     uint32_t ctarget = kNone;
     if (vvalid && single) {
@@ -520,7 +533,6 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
   uint32_t* keys = reinterpret_cast<uint32_t*>(base + size_t(HC) * sizeof(V));
   int* stage = reinterpret_cast<int*>(base + size_t(HC) * (sizeof(V) + 4));
   uint16_t* used = reinterpret_cast<uint16_t*>(base + size_t(HC) * (sizeof(V) + 4) + 32 * 4);
-  uint32_t* used_count = reinterpret_cast<uint32_t*>(base + size_t(HC) * (sizeof(V) + 5) + 32 * 4);
   unsigned long long fam_e = 0, fam_v = 0;
   const bool replay = a.out_target != nullptr;
   const bool unit = a.w == nullptr;
@@ -528,7 +540,6 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     keys[i] = kNone;
     vals[i] = 0;
   }
-  if (lane == 0) *used_count = 0;
   __syncwarp();
   // The next vertex id is loaded one iteration ahead, and each vertex's
   // entries are loaded kCertUnroll chunks at a time (up to 128 neighbour ids
@@ -550,6 +561,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
       fam_e += x.d;
       fam_v += 1;
     }
+    uint32_t nused = 0;  // used[] entries (warp-uniform)
     for (uint32_t e0 = 0; e0 < x.d; e0 += 32 * kCertUnroll) {
       uint32_t uu[kCertUnroll], cc[kCertUnroll];
       float ww[kCertUnroll];
@@ -581,11 +593,8 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
       }
       const unsigned im = __ballot_sync(kFull, ins);
       if (im) {
-        uint32_t b0 = 0;
-        const int ld = __ffs(im) - 1;
-        if (int(lane) == ld) b0 = atomicAdd(used_count, uint32_t(__popc(im)));
-        b0 = __shfl_sync(kFull, b0, ld);
-        if (ins) used[b0 + __popc(im & LaneMaskLt())] = static_cast<uint16_t>(slot);
+        if (ins) used[nused + __popc(im & LaneMaskLt())] = static_cast<uint16_t>(slot);
+        nused += __popc(im);
       }
       const int xi = cand ? (WeightToInt(wt) - a.ioffset) : 0;
       const int Sg = GroupSumInt(peers, xi, unit, leader, stage);
@@ -599,14 +608,17 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
       if (slot != kNone) T = vals[slot];
     }
     T = __shfl_sync(kFull, T, 0);
-    const uint32_t nused = *used_count;
     const float k32 = a.kf[x.v];
     const ChangeApproxT<V> ca = ApproxChange<V>(a.res32, a.int_nw != 0, k32, a.Kf[x.c], T);
     const float cabs = ChangeAbsBound(ca);
     V vmax = sizeof(V) == 4 ? V(INT_MIN) : V(LLONG_MIN);
     for (uint32_t i = lane; i < nused; i += 32) vmax = max(vmax, vals[used[i]]);
+    if constexpr (sizeof(V) == 4) {
+      vmax = __reduce_max_sync(kFull, vmax);
+    } else {
 #pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) vmax = max(vmax, __shfl_xor_sync(kFull, vmax, o));
+      for (int o = 16; o >= 1; o >>= 1) vmax = max(vmax, __shfl_xor_sync(kFull, vmax, o));
+    }
     const V smax = vmax;
     float U = -CUDART_INF_F;
     for (uint32_t i = lane; i < nused; i += 32) {
@@ -614,8 +626,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
       const FilterVal f = FilterOf<V>(a.res32, k32, a.Kf[keys[slot]], vals[slot], smax, cabs);
       if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
     }
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) U = fmaxf(U, __shfl_xor_sync(kFull, U, o));
+    U = WarpMaxFinite(U);
     LexKeyT<V> lead, tail;
     for (uint32_t i = lane; i < nused; i += 32) {
       const uint32_t slot = used[i];
@@ -632,9 +643,14 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
       lead.Keep(S, ko, key);
       tail.Keep(-S, ~ko, key);
     }
-    LexGroupReduce<32>(lead);
-    LexGroupReduce<32>(tail);
-    const bool single = lead.id == kNone || (-tail.S == lead.S && ~tail.K == lead.K);
+    bool single;
+    if constexpr (sizeof(V) == 4) {
+      single = LexWarpLeadInt(lead, tail);
+    } else {
+      LexGroupReduce<32>(lead);
+      LexGroupReduce<32>(tail);
+      single = lead.id == kNone || (-tail.S == lead.S && ~tail.K == lead.K);
+    }
     int cres = kUncertain;
     uint32_t ctarget = kNone;
     if (single) {
@@ -659,8 +675,6 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     }
     const uint32_t pos = WarpAppendFull(&a.ctr->movers, append);
     if (append) a.movers[pos] = x.v;
-    __syncwarp();
-    if (lane == 0) *used_count = 0;
     __syncwarp();
   }
   FlushFamily(a, kFamWarp, fam_e, fam_v);

@@ -109,6 +109,43 @@ __device__ __forceinline__ void LexGroupReduce(LexKeyT<I>& x) {
   }
 }
 
+// Warp-wide form of LexGroupReduce<32> for 32-bit sums, by single-
+// instruction warp reductions (REDUX) instead of a shuffle butterfly: the
+// leader's S is the largest S, then the smallest K among those (high word,
+// then low word), then the lowest id.  Returns whether every lane's
+// trailing contender (`tail`, kept with (-S, ~K)) lies in the leader's (S, K)
+// class, i.e. the test the butterfly over `tail` decided.
+__device__ __forceinline__ bool LexWarpLeadInt(LexKeyT<int>& lead, const LexKeyT<int>& tail) {
+  const bool has = lead.id != kNone;
+  const int sm = __reduce_max_sync(kFull, has ? lead.S : INT_MIN);
+  const bool m1 = has && lead.S == sm;
+  const unsigned hi = static_cast<unsigned>(lead.K >> 32), lo = static_cast<unsigned>(lead.K);
+  const unsigned khi = __reduce_min_sync(kFull, m1 ? hi : 0xFFFFFFFFu);
+  const bool m2 = m1 && hi == khi;
+  const unsigned klo = __reduce_min_sync(kFull, m2 ? lo : 0xFFFFFFFFu);
+  const bool m3 = m2 && lo == klo;
+  const unsigned id = __reduce_min_sync(kFull, m3 ? lead.id : kNone);
+  if (id == kNone) {
+    lead = LexKeyT<int>{};
+    return true;
+  }
+  lead.S = sm;
+  lead.K = (static_cast<unsigned long long>(khi) << 32) | klo;
+  lead.id = id;
+  const bool diff = tail.id != kNone && (-tail.S != sm || ~tail.K != lead.K);
+  return !__any_sync(kFull, diff);
+}
+
+// Warp maximum of finite floats (or -inf) by one integer REDUX: the map
+// i -> i ^ 0x7FFFFFFF on negative bit patterns orders floats as signed ints
+// and is its own inverse.
+__device__ __forceinline__ float WarpMaxFinite(float x) {
+  int i = __float_as_int(x);
+  i = i >= 0 ? i : (i ^ 0x7FFFFFFF);
+  i = __reduce_max_sync(kFull, i);
+  return __int_as_float(i >= 0 ? i : (i ^ 0x7FFFFFFF));
+}
+
 // FP32 filter value of a candidate (FilterBound): Y' = fl32(S - Smax) - R'
 // and its bound e; the shift keeps the top-S candidates apart by R alone.
 // (An S - Smax above 2^24 adds at most u (|Y| + R), inside FilterBound's
