@@ -112,10 +112,8 @@ __device__ __forceinline__ void LexGroupReduce(LexKeyT<I>& x) {
 // Warp-wide form of LexGroupReduce<32> for 32-bit sums, by single-
 // instruction warp reductions (REDUX) instead of a shuffle butterfly: the
 // leader's S is the largest S, then the smallest K among those (high word,
-// then low word), then the lowest id.  Returns whether every lane's
-// trailing contender (`tail`, kept with (-S, ~K)) lies in the leader's (S, K)
-// class, i.e. the test the butterfly over `tail` decided.
-__device__ __forceinline__ bool LexWarpLeadInt(LexKeyT<int>& lead, const LexKeyT<int>& tail) {
+// then low word), then the lowest id.
+__device__ __forceinline__ void LexWarpLeaderInt(LexKeyT<int>& lead) {
   const bool has = lead.id != kNone;
   const int sm = __reduce_max_sync(kFull, has ? lead.S : INT_MIN);
   const bool m1 = has && lead.S == sm;
@@ -127,12 +125,20 @@ __device__ __forceinline__ bool LexWarpLeadInt(LexKeyT<int>& lead, const LexKeyT
   const unsigned id = __reduce_min_sync(kFull, m3 ? lead.id : kNone);
   if (id == kNone) {
     lead = LexKeyT<int>{};
-    return true;
+    return;
   }
   lead.S = sm;
   lead.K = (static_cast<unsigned long long>(khi) << 32) | klo;
   lead.id = id;
-  const bool diff = tail.id != kNone && (-tail.S != sm || ~tail.K != lead.K);
+}
+
+// The warp leader, and whether every lane's trailing contender (`tail`,
+// kept with (-S, ~K)) lies in the leader's (S, K) class, i.e. the test the
+// butterfly over `tail` decided.
+__device__ __forceinline__ bool LexWarpLeadInt(LexKeyT<int>& lead, const LexKeyT<int>& tail) {
+  LexWarpLeaderInt(lead);
+  if (lead.id == kNone) return true;
+  const bool diff = tail.id != kNone && (-tail.S != lead.S || ~tail.K != lead.K);
   return !__any_sync(kFull, diff);
 }
 

@@ -24,6 +24,7 @@ constexpr uint32_t kMaxCont = 256;         // contender list per CTA
 
 constexpr int kSmallThreads = 256;         // small hubs: CTA size, table slots
 constexpr uint32_t kSmallSlots = 2 * kHubSmallMax;
+constexpr uint32_t kSmallNarrowSlots = kHubSmallMax;  // hubs with 2d + 2 <= kSmallNarrowSlots
 constexpr int kBigThreads = 1024;          // big hubs
 // Big-hub table: ~192 KB of (key, sum) slots.
 template <typename V>
@@ -34,7 +35,7 @@ __host__ __device__ constexpr uint32_t BigSlots() {
 struct HubArgs {
   BMArgs a;
   const uint32_t* small_v;
-  uint32_t num_small;
+  uint32_t small_lo, small_hi;  // this launch's items of small_v
   const uint32_t* big_v;
   const uint32_t* big_parts;
   const uint32_t* big_pbase;
@@ -218,6 +219,28 @@ __device__ __forceinline__ LexKeyT<I> BlockLex(LexKeyT<I> x, long long* rs, unsi
   return r;
 }
 
+// Block leader of `lead` and the class test over `tail` (the two BlockLex
+// calls and the (S, K) comparison) with 32-bit sums: warp leaders by REDUX,
+// the warps' leaders combined by every thread, the test by one barrier with
+// a predicate.
+template <int BT>
+__device__ __forceinline__ bool BlockLexLeadInt(LexKeyT<int>& lead, const LexKeyT<int>& tail, long long* rs,
+                                                unsigned long long* rk, uint32_t* ri) {
+  LexWarpLeaderInt(lead);
+  if (LaneId() == 0) {
+    rs[threadIdx.x >> 5] = lead.S;
+    rk[threadIdx.x >> 5] = lead.K;
+    ri[threadIdx.x >> 5] = lead.id;
+  }
+  __syncthreads();
+  LexKeyT<int> r;
+#pragma unroll
+  for (int w = 0; w < BT / 32; ++w) r.Keep(static_cast<int>(rs[w]), rk[w], ri[w]);
+  lead = r;
+  const bool diff = r.id != kNone && tail.id != kNone && (-tail.S != r.S || ~tail.K != r.K);
+  return !__syncthreads_or(diff);  // also orders the reads of rs/rk/ri before their next use
+}
+
 // Finds or inserts `key` in a table of `cap` slots (any capacity), probing
 // linearly from the slot the hash picks; kNone when the table is full.
 __device__ __forceinline__ uint32_t HubInsert(uint32_t* keys, uint32_t cap, uint32_t hsh, uint32_t key,
@@ -321,10 +344,15 @@ __device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double
         KeepBest(lv, lid, ValOf(a, x.kv, change, static_cast<double>(S), KD), key);  // list full: now
       }
     }
-    lead = BlockLex<BT, I>(lead, sh.red_ll, sh.red_k, sh.red_i);
-    tail = BlockLex<BT, I>(tail, sh.red_ll, sh.red_k, sh.red_i);
+    bool single;
+    if constexpr (std::is_same<I, int>::value) {
+      single = BlockLexLeadInt<BT>(lead, tail, sh.red_ll, sh.red_k, sh.red_i);
+    } else {
+      lead = BlockLex<BT, I>(lead, sh.red_ll, sh.red_k, sh.red_i);
+      tail = BlockLex<BT, I>(tail, sh.red_ll, sh.red_k, sh.red_i);
+      single = lead.id == kNone || (-tail.S == lead.S && ~tail.K == lead.K);
+    }
     const uint32_t nc = min(sh.ncont, kMaxCont);
-    const bool single = lead.id == kNone || (-tail.S == lead.S && ~tail.K == lead.K);
     if (!single) {
       for (uint32_t i = tid; i < nc; i += BT) {
         const uint32_t key = sh.cont_key[i];
@@ -451,17 +479,17 @@ __device__ __forceinline__ double HubChange(const BMArgs& a, const VertexCtx& x,
 // ---------------------------------------------------------------------------
 // Small hubs: one CTA per hub, a table of 2 * degree slots (never full).
 // ---------------------------------------------------------------------------
-template <bool kInt, bool kAsync, typename V>
+template <bool kInt, bool kAsync, typename V, uint32_t kSlots>
 __global__ void __launch_bounds__(kSmallThreads) HubSmallKernel(HubArgs h) {
   constexpr int BT = kSmallThreads;
   extern __shared__ __align__(16) unsigned char smem[];
   V* svals = reinterpret_cast<V*>(smem);
-  uint32_t* skeys = reinterpret_cast<uint32_t*>(smem + size_t(kSmallSlots) * sizeof(V));
+  uint32_t* skeys = reinterpret_cast<uint32_t*>(smem + size_t(kSlots) * sizeof(V));
   __shared__ HubShared<BT> sh;
   const BMArgs& a = h.a;
   const unsigned tid = threadIdx.x;
   unsigned long long fam_e = 0, fam_v = 0;  // entries and vertices evaluated (tid 0)
-  for (uint32_t i = tid; i < kSmallSlots; i += BT) {
+  for (uint32_t i = tid; i < kSlots; i += BT) {
     skeys[i] = kNone;
     svals[i] = V(0);
   }
@@ -470,11 +498,11 @@ __global__ void __launch_bounds__(kSmallThreads) HubSmallKernel(HubArgs h) {
     sh.nkeys = 0;
   }
   __syncthreads();
-  for (uint32_t item = blockIdx.x; item < h.num_small; item += gridDim.x) {
+  for (uint32_t item = h.small_lo + blockIdx.x; item < h.small_hi; item += gridDim.x) {
     const uint32_t v = h.small_v[item];
     if (!InFront(a, v)) continue;  // uniform over the CTA
     const VertexCtx x = LoadVertex<kAsync>(a, v);
-    const uint32_t cap = min(kSmallSlots, 2 * x.d + 2);
+    const uint32_t cap = min(kSlots, 2 * x.d + 2);
     if (tid == 0) {
       fam_e += x.d;
       fam_v += 1;
@@ -632,18 +660,36 @@ int PrepareOnce(K kernel, int threads, size_t smem) {
 }
 
 template <bool kInt, bool kAsync, typename V>
-Status LaunchHubT(Context* ctx, const HubArgs& h) {
+Status LaunchHubT(Context* ctx, const HubArgs& h, uint32_t num_small, uint32_t num_wide) {
   const unsigned sms = unsigned(ctx->num_sms);
-  if (h.num_small) {
-    constexpr size_t smem = size_t(kSmallSlots) * (sizeof(V) + sizeof(uint32_t));
-    auto k = HubSmallKernel<kInt, kAsync, V>;
-    const int per_sm = PrepareOnce(k, kSmallThreads, smem);
-    if (per_sm <= 0) return MakeError(PCC_INTERNAL, "small-hub kernel cannot be configured");
-    const unsigned grid = Blocks(h.num_small, 1, sms * unsigned(std::max(per_sm, 1)));
+  if (num_small) {
+    // Hubs whose 2d + 2 slots exceed the narrow table (listed first) take
+    // the wide one; the rest run with twice the CTAs per SM.
+    const int nl = (num_wide > 0) + (num_small > num_wide);
     FamBegin(ctx, kFamHubSmall);
-    k<<<grid, kSmallThreads, smem, ctx->stream>>>(h);
-    FamEnd(ctx, kFamHubSmall, 1);
-    PCC_COUNT(1);
+    if (num_wide) {
+      constexpr size_t smem = size_t(kSmallSlots) * (sizeof(V) + sizeof(uint32_t));
+      auto k = HubSmallKernel<kInt, kAsync, V, kSmallSlots>;
+      const int per_sm = PrepareOnce(k, kSmallThreads, smem);
+      if (per_sm <= 0) return MakeError(PCC_INTERNAL, "small-hub kernel cannot be configured");
+      HubArgs hw = h;
+      hw.small_lo = 0;
+      hw.small_hi = num_wide;
+      k<<<Blocks(num_wide, 1, sms * unsigned(per_sm)), kSmallThreads, smem, ctx->stream>>>(hw);
+      PCC_COUNT(1);
+    }
+    if (num_small > num_wide) {
+      constexpr size_t smem = size_t(kSmallNarrowSlots) * (sizeof(V) + sizeof(uint32_t));
+      auto k = HubSmallKernel<kInt, kAsync, V, kSmallNarrowSlots>;
+      const int per_sm = PrepareOnce(k, kSmallThreads, smem);
+      if (per_sm <= 0) return MakeError(PCC_INTERNAL, "small-hub kernel cannot be configured");
+      HubArgs hn = h;
+      hn.small_lo = num_wide;
+      hn.small_hi = num_small;
+      k<<<Blocks(num_small - num_wide, 1, sms * unsigned(per_sm)), kSmallThreads, smem, ctx->stream>>>(hn);
+      PCC_COUNT(1);
+    }
+    FamEnd(ctx, kFamHubSmall, nl);
   }
   if (h.num_items) {
     constexpr size_t smem = size_t(BigSlots<V>()) * (sizeof(V) + sizeof(uint32_t));
@@ -689,6 +735,7 @@ Status BuildHubPlan(Context* ctx, const DevGraph& g, const BinSet& bins, HubPlan
     const uint32_t i = order[r];
     if (hd[i] <= kHubSmallMax) {
       small_v.push_back(hv[i]);
+      if (2 * hd[i] + 2 > kSmallNarrowSlots) plan->num_small_wide++;
       continue;
     }
     const uint32_t P = std::max<uint32_t>(1, (hd[i] + kHubBigKeys - 1) / kHubBigKeys);
@@ -738,7 +785,8 @@ Status LaunchHubBestMoves(Context* ctx, const BMArgs& a, const HubPlan& plan, Hu
   HubArgs h;
   h.a = a;
   h.small_v = plan.small_v.p;
-  h.num_small = plan.num_small;
+  h.small_lo = 0;
+  h.small_hi = plan.num_small;
   h.big_v = plan.big_v.p;
   h.big_parts = plan.big_parts.p;
   h.big_pbase = plan.big_pbase.p;
@@ -749,11 +797,11 @@ Status LaunchHubBestMoves(Context* ctx, const BMArgs& a, const HubPlan& plan, Hu
   h.part_id = st.part_id.p;
   h.done = st.done.p;
   if (a.async) {
-    if (!int_mode) return LaunchHubT<false, true, double>(ctx, h);
-    return narrow ? LaunchHubT<true, true, int>(ctx, h) : LaunchHubT<true, true, long long>(ctx, h);
+    if (!int_mode) return LaunchHubT<false, true, double>(ctx, h, plan.num_small, plan.num_small_wide);
+    return narrow ? LaunchHubT<true, true, int>(ctx, h, plan.num_small, plan.num_small_wide) : LaunchHubT<true, true, long long>(ctx, h, plan.num_small, plan.num_small_wide);
   }
-  if (!int_mode) return LaunchHubT<false, false, double>(ctx, h);
-  return narrow ? LaunchHubT<true, false, int>(ctx, h) : LaunchHubT<true, false, long long>(ctx, h);
+  if (!int_mode) return LaunchHubT<false, false, double>(ctx, h, plan.num_small, plan.num_small_wide);
+  return narrow ? LaunchHubT<true, false, int>(ctx, h, plan.num_small, plan.num_small_wide) : LaunchHubT<true, false, long long>(ctx, h, plan.num_small, plan.num_small_wide);
 }
 
 }  // namespace pcc

@@ -6,7 +6,8 @@
 // sums live in shared memory only:
 //
 //   small hubs (1000 < degree <= kHubSmallMax): one 256-thread CTA per hub,
-//     a table of 2 * degree slots, so it never fills;
+//     a table of at least 2 * degree + 2 slots, so it never fills (4096
+//     slots up to degree 2047, else 8192);
 //   big hubs (degree > kHubSmallMax): one 1024-thread CTA per (hub,
 //     partition) with a ~192 KB table.  Hubs with more than kHubBigKeys
 //     distinct neighbour clusters are split into P hash partitions (P =
@@ -33,6 +34,7 @@ constexpr uint32_t kHubBigKeys = 12288;   // expected distinct keys per big-hub 
 struct HubPlan {
   uint32_t num_hubs = 0;
   uint32_t num_small = 0;      // hubs with degree <= kHubSmallMax
+  uint32_t num_small_wide = 0; // of those, the first ones, with degree > kHubSmallMax / 2 - 1
   uint32_t num_big = 0;
   uint32_t num_items = 0;      // big-hub work items (hub, partition)
   uint64_t num_partials = 0;   // one per big-hub item
