@@ -680,17 +680,25 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
   FlushFamily(a, kFamWarp, fam_e, fam_v);
 }
 
-// Sets the kernel's dynamic shared-memory limit once per process (the
-// runtime call takes a lock that serialises concurrent contexts).
+// Sets the kernel's dynamic shared-memory limit and queries its resident
+// CTAs per SM once per process (the runtime calls take a lock that
+// serialises concurrent contexts).  Each kernel is launched with one fixed
+// shared-memory size.
 template <class K>
-Status SetSmem(K kernel, size_t bytes) {
+Status SetSmem(K kernel, size_t bytes, int threads, int* per_sm) {
   static std::mutex mu;
-  static std::unordered_map<const void*, size_t> done;
+  static std::unordered_map<const void*, int> occ;
   std::lock_guard<std::mutex> lk(mu);
-  auto it = done.find(reinterpret_cast<const void*>(kernel));
-  if (it != done.end() && it->second >= bytes) return Status::Ok();
+  auto it = occ.find(reinterpret_cast<const void*>(kernel));
+  if (it != occ.end()) {
+    *per_sm = it->second;
+    return Status::Ok();
+  }
   PCC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
-  done[reinterpret_cast<const void*>(kernel)] = bytes;
+  int n = 0;
+  PCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, bytes));
+  occ[reinterpret_cast<const void*>(kernel)] = n;
+  *per_sm = n;
   return Status::Ok();
 }
 
@@ -709,14 +717,19 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
   for (int b = kBinG4; b <= kBinG32; ++b) ng += want(b) ? 1 : 0;
   FamBegin(ctx, kFamGroup);
   if (kCert) {
-    if (want(kBinG4))
-      CertGroupKernel<4><<<grid(kBinG4, 64, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG4); PCC_COUNT(1);
-    if (want(kBinG8))
-      CertGroupKernel<8><<<grid(kBinG8, 32, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG8); PCC_COUNT(1);
-    if (want(kBinG16))
-      CertGroupKernel<16><<<grid(kBinG16, 16, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG16); PCC_COUNT(1);
-    if (want(kBinG32))
-      CertGroupKernel<32><<<grid(kBinG32, 8, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG32); PCC_COUNT(1);
+    // One wave of resident CTAs (grid-stride kernels).
+    auto group_bin = [&](auto k, int bin, uint64_t per_block) -> Status {
+      if (!want(bin)) return Status::Ok();
+      int per_sm = 0;
+      PCC_RETURN_IF_ERROR(SetSmem(k, 0, 256, &per_sm));
+      k<<<grid(bin, per_block, sms * unsigned(per_sm > 0 ? per_sm : 8)), 256, 0, st>>>(a, list, counts, starts, bin);
+      PCC_COUNT(1);
+      return Status::Ok();
+    };
+    PCC_RETURN_IF_ERROR(group_bin(CertGroupKernel<4>, kBinG4, 64));
+    PCC_RETURN_IF_ERROR(group_bin(CertGroupKernel<8>, kBinG8, 32));
+    PCC_RETURN_IF_ERROR(group_bin(CertGroupKernel<16>, kBinG16, 16));
+    PCC_RETURN_IF_ERROR(group_bin(CertGroupKernel<32>, kBinG32, 8));
   } else {
     if (want(kBinG4))
       BestMoveGroupKernel<4, kInt, kAsync><<<grid(kBinG4, 64, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG4); PCC_COUNT(1);
@@ -731,9 +744,13 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
   int nw = 0;
   for (int b = kBinW128; b <= kBinW1000; ++b) nw += want(b) ? 1 : 0;
   FamBegin(ctx, kFamWarp);
+  // Grid-stride kernels: at most one wave of resident CTAs, so no partial
+  // last wave.
   auto warp_bin = [&](auto k, size_t smem, int bin, unsigned cap) -> Status {
     if (!want(bin)) return Status::Ok();
-    PCC_RETURN_IF_ERROR(SetSmem(k, smem));
+    int per_sm = 0;
+    PCC_RETURN_IF_ERROR(SetSmem(k, smem, kWarpKernelWarps * 32, &per_sm));
+    if (per_sm > 0) cap = sms * unsigned(per_sm);
     k<<<grid(bin, kWarpKernelWarps, cap), kWarpKernelWarps * 32, smem, st>>>(a, list, counts, starts, bin);
     PCC_COUNT(1);
     return Status::Ok();
