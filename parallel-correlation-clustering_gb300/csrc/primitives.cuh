@@ -4,6 +4,8 @@
 // calls (parallel/parallel-sequence-ops.h:38-232).
 #pragma once
 
+#include <mutex>
+
 #include "common.cuh"
 
 namespace pcc {
@@ -228,14 +230,27 @@ static __global__ void __launch_bounds__(kSortThreads) RadixHistKernel(const uin
   hist[uint64_t(threadIdx.x) * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
+// Scatter of one tile: ranks inside the tile in stable order (digit, then
+// item order: warps, rounds, lanes), the tile staged in shared memory in
+// that order, then each digit's run written by consecutive threads to its
+// global range (coalesced stores).  Dynamic shared memory: kSortScatterSmem.
+constexpr size_t kSortScatterSmem = size_t(kSortTile) * (sizeof(uint64_t) + sizeof(uint32_t));
+
 static __global__ void __launch_bounds__(kSortThreads) RadixScatterKernel(const uint64_t* keys_in, const uint32_t* vals_in,
                                                                    uint64_t* keys_out, uint32_t* vals_out, uint64_t n,
                                                                    int shift, const uint32_t* offsets, uint32_t tiles) {
+  extern __shared__ __align__(16) unsigned char sort_smem[];
+  uint64_t* sk = reinterpret_cast<uint64_t*>(sort_smem);
+  uint32_t* sv = reinterpret_cast<uint32_t*>(sort_smem + size_t(kSortTile) * sizeof(uint64_t));
   __shared__ uint32_t wcount[kSortWarps][256];
+  __shared__ uint32_t dstart[256];   // tile-local start of each digit's run
+  __shared__ uint32_t goff[256];     // global start of this tile's run of each digit
+  __shared__ uint32_t wsum[kSortWarps];
   const unsigned lane = LaneId(), warp = threadIdx.x >> 5;
   for (int d = lane; d < 256; d += 32) wcount[warp][d] = 0;
   __syncwarp();
-  const uint64_t wbase = uint64_t(blockIdx.x) * kSortTile + uint64_t(warp) * 32 * kSortItems;
+  const uint64_t tbase = uint64_t(blockIdx.x) * kSortTile;
+  const uint64_t wbase = tbase + uint64_t(warp) * 32 * kSortItems;
   uint64_t k[kSortItems];
   uint32_t v[kSortItems];
   uint32_t pos[kSortItems];
@@ -255,27 +270,49 @@ static __global__ void __launch_bounds__(kSortThreads) RadixScatterKernel(const 
     pos[r] = base + __popc(peers & LaneMaskLt());
   }
   __syncthreads();
-  // Exclusive scan across warps per digit, plus the global digit offset.
-  {
-    const unsigned d = threadIdx.x;
-    uint32_t acc = offsets[uint64_t(d) * tiles + blockIdx.x];
+  // Thread d: exclusive scan across warps of digit d (in place), the
+  // digit's tile total, and its global offset.
+  const unsigned d = threadIdx.x;
+  uint32_t tot = 0;
 #pragma unroll
-    for (int w = 0; w < kSortWarps; ++w) {
-      const uint32_t t = wcount[w][d];
-      wcount[w][d] = acc;
-      acc += t;
-    }
+  for (int w = 0; w < kSortWarps; ++w) {
+    const uint32_t t = wcount[w][d];
+    wcount[w][d] = tot;
+    tot += t;
   }
+  goff[d] = offsets[uint64_t(d) * tiles + blockIdx.x];
+  // Exclusive scan of the digit totals over the block (digit order).
+  uint32_t incl = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, incl, o);
+    if (lane >= unsigned(o)) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  uint32_t wpre = 0;
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w) wpre += unsigned(w) < warp ? wsum[w] : 0u;
+  dstart[d] = wpre + incl - tot;
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
     const uint64_t i = wbase + uint64_t(r) * 32 + lane;
     if (i < n) {
-      const uint32_t d = uint32_t((k[r] >> shift) & 255u);
-      const uint32_t o = wcount[warp][d] + pos[r];
-      keys_out[o] = k[r];
-      vals_out[o] = v[r];
+      const uint32_t dg = uint32_t((k[r] >> shift) & 255u);
+      const uint32_t li = dstart[dg] + wcount[warp][dg] + pos[r];
+      sk[li] = k[r];
+      sv[li] = v[r];
     }
+  }
+  __syncthreads();
+  const uint32_t cnt = n - tbase < uint64_t(kSortTile) ? uint32_t(n - tbase) : uint32_t(kSortTile);
+  for (uint32_t t = threadIdx.x; t < cnt; t += kSortThreads) {
+    const uint64_t key = sk[t];
+    const uint32_t dg = uint32_t((key >> shift) & 255u);
+    const uint32_t o = goff[dg] + (t - dstart[dg]);
+    keys_out[o] = key;
+    vals_out[o] = sv[t];
   }
 }
 
@@ -293,7 +330,7 @@ struct SortScratch {
 
 // Sorts keys[0..n) (with vals) by the low `bits` bits of the key; the
 // result is left in keys/vals.  n < 2^32.
-inline Status RadixSortPairs(Context* ctx, uint64_t* keys, uint32_t* vals, uint64_t n, int bits,
+static inline Status RadixSortPairs(Context* ctx, uint64_t* keys, uint32_t* vals, uint64_t n, int bits,
                              SortScratch& sc) {
   if (n <= 1 || bits <= 0) return Status::Ok();
   const uint32_t tiles = uint32_t((n + kSortTile - 1) / kSortTile);
@@ -305,14 +342,23 @@ inline Status RadixSortPairs(Context* ctx, uint64_t* keys, uint32_t* vals, uint6
   uint64_t* kout = sc.keys.p;
   uint32_t* vout = sc.vals.p;
   const int passes = (bits + 7) / 8;
+  {
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+      attr = cudaFuncSetAttribute(RadixScatterKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(kSortScatterSmem));
+    });
+    PCC_CUDA(attr);
+  }
   for (int p = 0; p < passes; ++p) {
     const int shift = p * 8;
     RadixHistKernel<<<tiles, kSortThreads, 0, ctx->stream>>>(kin, n, shift, sc.hist.p, tiles); PCC_COUNT(1);
     PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx, uint64_t(tiles) * 256, HistInput{sc.hist.p},
                                             StorePrefix<uint32_t>{sc.hist.p}, sc.tile_sums,
                                             static_cast<uint32_t*>(nullptr)));
-    RadixScatterKernel<<<tiles, kSortThreads, 0, ctx->stream>>>(kin, vin, kout, vout, n, shift, sc.hist.p,
-                                                                tiles); PCC_COUNT(1);
+    RadixScatterKernel<<<tiles, kSortThreads, kSortScatterSmem, ctx->stream>>>(kin, vin, kout, vout, n, shift,
+                                                                               sc.hist.p, tiles); PCC_COUNT(1);
     std::swap(kin, kout);
     std::swap(vin, vout);
   }
