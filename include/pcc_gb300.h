@@ -135,6 +135,15 @@ uint64_t pcc_device_bytes_in_use(const pcc_context* ctx);
 /* High-water mark of the context's device memory since creation or the last
  * reset (reset != 0 restarts it from the current use). */
 uint64_t pcc_device_peak_bytes(pcc_context* ctx, int32_t reset);
+/*
+ * Detailed timing (no reference counterpart).  Off (the default):
+ * synchronous best-move rounds run as a device-side loop, one round captured
+ * into a CUDA graph WHILE node, with one host read per level; pcc_stats
+ * then carries the compress time but no per-phase or per-family kernel
+ * times.  On: the host drives every round and CUDA events time each phase
+ * and best-move kernel family.  Results are identical either way.
+ */
+void pcc_set_detailed_timing(pcc_context* ctx, int32_t on);
 
 /*
  * Graph upload.  Copies a host CSR graph into HBM.  Replaces

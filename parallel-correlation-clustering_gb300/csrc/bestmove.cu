@@ -775,7 +775,39 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
   return LaunchCheck();
 }
 
+template <class K>
+Status Prep(K kernel, size_t smem, int threads) {
+  int per_sm = 0;
+  return SetSmem(kernel, smem, threads, &per_sm);
+}
+
 }  // namespace
+
+Status PrepareBestMoveKernels() {
+  static std::mutex mu;
+  static bool done = false;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done) return Status::Ok();
+  PCC_RETURN_IF_ERROR(Prep(CertGroupKernel<4>, 0, 256));
+  PCC_RETURN_IF_ERROR(Prep(CertGroupKernel<8>, 0, 256));
+  PCC_RETURN_IF_ERROR(Prep(CertGroupKernel<16>, 0, 256));
+  PCC_RETURN_IF_ERROR(Prep(CertGroupKernel<32>, 0, 256));
+  constexpr int kW = kWarpKernelWarps * 32;
+  PCC_RETURN_IF_ERROR(Prep(CertWarpKernel<256, int>, CertWarpSmem<256, int>(), kW));
+  PCC_RETURN_IF_ERROR(Prep(CertWarpKernel<512, int>, CertWarpSmem<512, int>(), kW));
+  PCC_RETURN_IF_ERROR(Prep(CertWarpKernel<1024, int>, CertWarpSmem<1024, int>(), kW));
+  PCC_RETURN_IF_ERROR(Prep(CertWarpKernel<2048, int>, CertWarpSmem<2048, int>(), kW));
+  PCC_RETURN_IF_ERROR(Prep(CertWarpKernel<256, long long>, CertWarpSmem<256, long long>(), kW));
+  PCC_RETURN_IF_ERROR(Prep(CertWarpKernel<512, long long>, CertWarpSmem<512, long long>(), kW));
+  PCC_RETURN_IF_ERROR(Prep(CertWarpKernel<1024, long long>, CertWarpSmem<1024, long long>(), kW));
+  PCC_RETURN_IF_ERROR(Prep(CertWarpKernel<2048, long long>, CertWarpSmem<2048, long long>(), kW));
+  PCC_RETURN_IF_ERROR(Prep(BestMoveWarpKernel<256, false, false>, WarpKernelSmem<256>(), kW));
+  PCC_RETURN_IF_ERROR(Prep(BestMoveWarpKernel<512, false, false>, WarpKernelSmem<512>(), kW));
+  PCC_RETURN_IF_ERROR(Prep(BestMoveWarpKernel<1024, false, false>, WarpKernelSmem<1024>(), kW));
+  PCC_RETURN_IF_ERROR(Prep(BestMoveWarpKernel<2048, false, false>, WarpKernelSmem<2048>(), kW));
+  done = true;
+  return Status::Ok();
+}
 
 Status LaunchBestMoves(Context* ctx, const BMArgs& a, const uint32_t* list, const uint32_t* bin_counts,
                        const uint32_t* bin_starts, const uint32_t* host_counts, bool int_mode,

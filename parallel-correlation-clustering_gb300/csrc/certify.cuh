@@ -272,7 +272,7 @@ __device__ __forceinline__ uint32_t CertifiedMove(const BMArgs& a, const VertexC
 // true when the vertex must be appended to the movers list.
 __device__ __forceinline__ bool ApplyCertified(const BMArgs& a, const VertexCtx& x, uint32_t move) {
   if (move == kNone) return false;
-  a.moved_stamp[x.v] = a.stamp;
+  a.moved_stamp[x.v] = StampIn(a.rs, a.stamp);
   if (move == x.c) return false;
   a.moves[x.v] = move;
   return true;

@@ -74,6 +74,11 @@ struct Context {
   size_t smem_optin = 0;
   cudaStream_t stream = nullptr;
   uint64_t budget = 0;             // 0 = device capacity
+  // Synchronous rounds run as a device-side graph loop (one host read per
+  // level) unless detailed timing (CUDA events around every phase and kernel
+  // family, host-driven rounds) is on, or graphs are unavailable.
+  bool detailed_timing = false;
+  bool graphs_failed = false;
   std::atomic<uint64_t> in_use{0};
   std::atomic<uint64_t> peak{0};   // high-water mark of in_use
   std::mutex mu;
@@ -225,14 +230,17 @@ struct PhaseTimer {
   Context* ctx;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> spans[4];
   cudaEvent_t open[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool enabled = true;  // off while work is captured into a graph
   explicit PhaseTimer(Context* c) : ctx(c) {}
   PhaseTimer(const PhaseTimer&) = delete;
   PhaseTimer& operator=(const PhaseTimer&) = delete;
   void Begin(int k) {
+    if (!enabled) return;
     open[k] = ctx->GetEvent();
     cudaEventRecord(open[k], ctx->stream);
   }
   void End(int k) {
+    if (!enabled) return;
     cudaEvent_t e = ctx->GetEvent();
     cudaEventRecord(e, ctx->stream);
     spans[k].emplace_back(open[k], e);

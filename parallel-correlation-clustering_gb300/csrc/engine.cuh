@@ -139,12 +139,36 @@ struct DevCounters {
   // bytes of the roofline); accumulated over the call.
   unsigned long long fam_entries[kNumFamilies];
   unsigned long long fam_vertices[kNumFamilies];
+  // Accumulated by the device-side round loop (sync mode).
+  unsigned long long sync_moves;     // real movers over the loop's rounds
+  unsigned long long visited;        // vertices evaluated over the loop's rounds
 };
 
 constexpr int kErrProbeLimit = 1;   // async new-cluster probe exceeded its bound
 constexpr int kErrHashFull = 2;     // a best-move hash table filled up
 constexpr int kErrCertMismatch = 3; // a certified decision differed from FP64 (replay self-check)
 constexpr int kErrUnionRange = 4;   // a union graph's new-cluster id fell outside its range
+
+// Round state in device memory for rounds that run inside a device-side
+// graph loop: the kernel arguments stay fixed from round to round, and the
+// kernels take the stamp and the frontier from here.
+struct RoundState {
+  uint32_t stamp;                  // this round's stamp
+  uint32_t front_val;              // frontier: front_stamp[v] == front_val
+  uint32_t front_all;              // 1: every binned vertex is in the frontier
+  uint32_t iter;                   // rounds run in this loop so far
+  unsigned long long front_edges;  // degree sum of this round's frontier
+  unsigned long long front_size;   // its vertices (n when front_all)
+  unsigned long long visited;      // vertices evaluated (the binned ones when front_all)
+};
+
+__host__ __device__ __forceinline__ uint32_t StampIn(const RoundState* rs, uint32_t stamp) {
+#ifdef __CUDA_ARCH__
+  return rs ? rs->stamp : stamp;
+#else
+  return stamp;
+#endif
+}
 
 // Best-move kernel arguments.
 struct BMArgs {
@@ -188,7 +212,14 @@ struct BMArgs {
   double* K_mut;
   uint32_t* C_mut;
   uint32_t* moved_cluster_stamp;
+  // non-null: stamp and frontier come from here (front_stamp is the array)
+  const RoundState* rs;
 };
+
+// Configures (shared-memory limit, occupancy) every synchronous best-move
+// kernel once per process, so that launches captured into a graph make no
+// runtime configuration calls.
+Status PrepareBestMoveKernels();
 
 // Launches the best-move kernels of the bins up to degree 1000 over `bins`
 // (counts read on the device); hubs go through LaunchHubBestMoves.

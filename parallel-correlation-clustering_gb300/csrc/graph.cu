@@ -368,6 +368,10 @@ const char* pcc_last_error(const pcc_context* ctx) { return ctx ? ctx->c.last_er
 
 uint64_t pcc_device_bytes_in_use(const pcc_context* ctx) { return ctx ? ctx->c.in_use.load() : 0; }
 
+void pcc_set_detailed_timing(pcc_context* ctx, int32_t on) {
+  if (ctx) ctx->c.detailed_timing = on != 0;
+}
+
 uint64_t pcc_device_peak_bytes(pcc_context* ctx, int32_t reset) {
   if (!ctx) return 0;
   const uint64_t p = ctx->c.peak.load();

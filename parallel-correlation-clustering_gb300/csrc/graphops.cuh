@@ -162,7 +162,8 @@ struct PredAll {
 struct PredStamp {
   const uint32_t* st;
   uint32_t stamp;
-  __device__ bool operator()(uint32_t v) const { return st[v] == stamp; }
+  const RoundState* rs = nullptr;  // non-null: the stamp comes from here
+  __device__ bool operator()(uint32_t v) const { return st[v] == StampIn(rs, stamp); }
 };
 
 template <class P>

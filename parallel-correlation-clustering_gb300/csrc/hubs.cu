@@ -779,6 +779,32 @@ Status AllocHubState(Context* ctx, const HubPlan& plan, HubState* st) {
   return st->done.Zero();
 }
 
+Status PrepareHubKernels() {
+  static std::mutex mu;
+  static bool done = false;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done) return Status::Ok();
+  bool ok = true;
+  auto small = [&](auto k, size_t slots, size_t vsize) {
+    ok = ok && PrepareOnce(k, kSmallThreads, slots * (vsize + sizeof(uint32_t))) > 0;
+  };
+  auto big = [&](auto k, size_t slots, size_t vsize) {
+    ok = ok && PrepareOnce(k, kBigThreads, slots * (vsize + sizeof(uint32_t))) > 0;
+  };
+  small(HubSmallKernel<true, false, int, kSmallSlots>, kSmallSlots, sizeof(int));
+  small(HubSmallKernel<true, false, int, kSmallNarrowSlots>, kSmallNarrowSlots, sizeof(int));
+  small(HubSmallKernel<true, false, long long, kSmallSlots>, kSmallSlots, sizeof(long long));
+  small(HubSmallKernel<true, false, long long, kSmallNarrowSlots>, kSmallNarrowSlots, sizeof(long long));
+  small(HubSmallKernel<false, false, double, kSmallSlots>, kSmallSlots, sizeof(double));
+  small(HubSmallKernel<false, false, double, kSmallNarrowSlots>, kSmallNarrowSlots, sizeof(double));
+  big(HubBigKernel<true, false, int>, BigSlots<int>(), sizeof(int));
+  big(HubBigKernel<true, false, long long>, BigSlots<long long>(), sizeof(long long));
+  big(HubBigKernel<false, false, double>, BigSlots<double>(), sizeof(double));
+  if (!ok) return MakeError(PCC_INTERNAL, "hub kernels cannot be configured");
+  done = true;
+  return Status::Ok();
+}
+
 Status LaunchHubBestMoves(Context* ctx, const BMArgs& a, const HubPlan& plan, HubState& st, bool int_mode,
                           bool narrow) {
   if (plan.num_hubs == 0) return Status::Ok();

@@ -54,6 +54,9 @@ struct HubState {
 };
 
 Status BuildHubPlan(Context* ctx, const DevGraph& g, const BinSet& bins, HubPlan* plan);
+// Configures every synchronous hub kernel once per process (for launches
+// captured into a graph).
+Status PrepareHubKernels();
 Status AllocHubState(Context* ctx, const HubPlan& plan, HubState* st);
 // narrow: INT mode with every neighbour-cluster sum below 2^31 in
 // magnitude, so the tables hold 32-bit sums.

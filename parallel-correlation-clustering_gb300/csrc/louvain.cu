@@ -82,10 +82,13 @@ __global__ void AccumulateClustersKernel(uint32_t n, const uint32_t* __restrict_
 // Kf[c] = fl32(K[c]) for every c (stamp == 0) or for the clusters modified
 // in the round `stamp` (the FP32 pre-filter of the best-move kernels needs
 // Kf == fl32(K) exactly).
+// Kf = FilterF32(K) on every cluster (stamp 0) or on the clusters modified
+// in the round (mod_stamp == the round's stamp).
 __global__ void RefreshKfKernel(uint32_t n, const double* __restrict__ K, float* Kf,
-                                const uint32_t* __restrict__ mod_stamp, uint32_t stamp) {
+                                const uint32_t* __restrict__ mod_stamp, uint32_t stamp, const RoundState* rs) {
+  const uint32_t st = StampIn(rs, stamp);
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
-    if (stamp == 0 || mod_stamp[i] == stamp) Kf[i] = FilterF32(K[i]);
+    if (st == 0 || mod_stamp[i] == st) Kf[i] = FilterF32(K[i]);
 }
 
 // kf = FilterF32(k): node weights for the FP32 pre-filter and certified
@@ -150,6 +153,7 @@ struct ApplyArgs {
   uint32_t* new_stamp;
   uint32_t stamp;
   DevCounters* ctr;
+  const RoundState* rs;  // non-null: the stamp comes from here
 };
 
 // Sum of x over the lanes of `peers` (the caller's match group), in lane
@@ -182,10 +186,10 @@ __global__ void __launch_bounds__(kT) ApplyLeaveKernel(ApplyArgs a) {
     if (in && int(LaneId()) == __ffs(peers) - 1) {
       atomicSub(&a.s[c], uint32_t(__popc(peers)));
       atomicAdd(&a.K[c], -tot);
-      a.mod_stamp[c] = a.stamp;
+      a.mod_stamp[c] = StampIn(a.rs, a.stamp);
     }
     const bool isnew = in && a.moves[v] == a.n;
-    if (isnew) a.new_stamp[v] = a.stamp;
+    if (isnew) a.new_stamp[v] = StampIn(a.rs, a.stamp);
     const unsigned nb = __ballot_sync(kFull, isnew);
     if (nb && LaneId() == 0) atomicAdd(&a.ctr->new_movers, uint32_t(__popc(nb)));
   }
@@ -206,7 +210,7 @@ __global__ void __launch_bounds__(kT) ApplyJoinKernel(ApplyArgs a) {
     if (in && int(LaneId()) == __ffs(peers) - 1) {
       atomicAdd(&a.s[t], uint32_t(__popc(peers)));
       atomicAdd(&a.K[t], tot);
-      a.mod_stamp[t] = a.stamp;
+      a.mod_stamp[t] = StampIn(a.rs, a.stamp);
     }
     if (in) a.C[v] = t;
   }
@@ -223,7 +227,10 @@ struct NewMoverInput {
   const uint32_t* st;
   uint32_t stamp;
   const DevCounters* ctr;
-  __device__ uint32_t operator()(uint64_t i) const { return ctr->new_movers && st[i] == stamp ? 1u : 0u; }
+  const RoundState* rs = nullptr;
+  __device__ uint32_t operator()(uint64_t i) const {
+    return ctr->new_movers && st[i] == StampIn(rs, stamp) ? 1u : 0u;
+  }
 };
 
 // New clusters take the ascending list of empty ids, in ascending node order.
@@ -236,7 +243,7 @@ __global__ void __launch_bounds__(kT) AssignNewKernel(ApplyArgs a, const uint32_
     a.C[v] = cid;
     a.s[cid] = 1u;
     a.K[cid] = a.k[v];
-    a.mod_stamp[cid] = a.stamp;
+    a.mod_stamp[cid] = StampIn(a.rs, a.stamp);
   }
 }
 
@@ -279,7 +286,7 @@ __global__ void __launch_bounds__(kT) AssignNewUnionKernel(ApplyArgs a, const ui
     a.C[v] = cid;
     a.s[cid] = 1u;
     a.K[cid] = a.k[v];
-    a.mod_stamp[cid] = a.stamp;
+    a.mod_stamp[cid] = StampIn(a.rs, a.stamp);
   }
 }
 
@@ -381,7 +388,8 @@ struct PushNeighbors {  // gbbs::edgeMap with an always-true functor
   const uint32_t* nbr;
   uint32_t* next_stamp;
   uint32_t stamp;
-  __device__ void operator()(uint32_t, uint64_t j, uint64_t) const { next_stamp[nbr[j]] = stamp; }
+  const RoundState* rs = nullptr;
+  __device__ void operator()(uint32_t, uint64_t j, uint64_t) const { next_stamp[nbr[j]] = StampIn(rs, stamp); }
 };
 
 // Marked vertices of the next frontier.
@@ -389,7 +397,8 @@ struct PredModifiedCluster {  // NBHR_CLUSTER_MOVE: vertices of modified cluster
   const uint32_t* C;
   const uint32_t* mod_stamp;
   uint32_t stamp;
-  __device__ bool operator()(uint32_t v) const { return mod_stamp[C[v]] == stamp; }
+  const RoundState* rs = nullptr;
+  __device__ bool operator()(uint32_t v) const { return mod_stamp[C[v]] == StampIn(rs, stamp); }
 };
 
 // ---------------------------------------------------------------------------
@@ -472,6 +481,41 @@ __global__ void DegreeF64Kernel(uint32_t n, const uint64_t* __restrict__ off, do
 }
 
 // ---------------------------------------------------------------------------
+// Device-side round loop (IterateBestMoves inside a graph WHILE node).
+// ---------------------------------------------------------------------------
+__global__ void RoundBeginKernel(RoundState* rs) { rs->stamp += 1; }
+
+// End of a round: accounts it (the frontier it evaluated, its movers), sets
+// the next round's frontier and whether the loop goes on -- the next frontier
+// is non-empty (ALL_MOVE: n > 0, every vertex again) and rounds are left.
+__global__ void RoundEndKernel(RoundState* rs, DevCounters* ctr, cudaGraphConditionalHandle loop, uint32_t num_inner,
+                               int all_move, uint32_t n, uint64_t m, uint64_t binned) {
+  ctr->rounds += 1;
+  ctr->edge_visits += rs->front_edges;
+  ctr->vertex_visits += rs->front_size;
+  ctr->visited += rs->visited;
+  ctr->sync_moves += ctr->movers;
+  bool next;
+  if (all_move) {
+    next = n > 0;
+    rs->front_all = 1;
+    rs->front_edges = m;
+    rs->front_size = n;
+    rs->visited = binned;
+  } else {
+    next = ctr->frontier > 0;
+    rs->front_all = 0;
+    rs->front_val = rs->stamp;
+    rs->front_edges = ctr->pend_edges;
+    rs->front_size = ctr->frontier;
+    rs->visited = ctr->frontier;
+  }
+  if (next) ctr->level_moved = 1;
+  rs->iter += 1;
+  cudaGraphSetConditional(loop, (next && rs->iter < num_inner) ? 1u : 0u);
+}
+
+// ---------------------------------------------------------------------------
 // Level state (one ClusteringHelper + its graph).
 // ---------------------------------------------------------------------------
 struct Level {
@@ -548,6 +592,9 @@ class Engine {
 
     PCC_RETURN_IF_ERROR(ctr_.Alloc(ctx_, 1));
     PCC_RETURN_IF_ERROR(ctr_.Zero());
+    PCC_RETURN_IF_ERROR(rs_.Alloc(ctx_, 1));
+    // Scan scratch for every level (no allocation inside a captured round).
+    PCC_RETURN_IF_ERROR(scan_tiles_.Reserve(ctx_, (nn + kScanTile - 1) / kScanTile + 1));
     (void)max_deg;
     return Status::Ok();
   }
@@ -581,7 +628,7 @@ class Engine {
       } else {
         SingletonsKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->k.p, L->C.p, L->s.p, L->K.p); PCC_COUNT(1);
       }
-      RefreshKfKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->K.p, L->Kf.p, nullptr, 0); PCC_COUNT(1);
+      RefreshKfKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->K.p, L->Kf.p, nullptr, 0, nullptr); PCC_COUNT(1);
       NodeKfKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->k.p, L->kf.p); PCC_COUNT(1);
       PCC_RETURN_IF_ERROR(LaunchCheck());
     }
@@ -598,21 +645,15 @@ class Engine {
     return Status::Ok();
   }
 
-  // One best-move round over `front` (host_counts known).  Builds the next
-  // frontier in dyn_ unless ALL_MOVE.  Returns whether the next frontier is
-  // non-empty (local_moved).
-  // front_stamp == 0: all vertices; else vertices with next_stamp == it.
-  Status Round(Level* L, uint32_t front_stamp, uint64_t front_edges, uint64_t front_size, bool* next_nonempty,
-               uint32_t* next_front_stamp, uint64_t* next_edges, uint64_t* next_size) {
+  // The work of one best-move round, enqueued on the context stream with no
+  // host read: counter resets, the best-move kernels, the application of the
+  // moves (sync) and, unless ALL_MOVE, the next frontier with its size and
+  // degree sum in the counters.  rs == null: the stamp is stamp_ and the
+  // frontier is front_stamp (0: every vertex); else both come from rs in
+  // device memory (rounds of a device-side loop).
+  Status EnqueueRound(Level* L, uint32_t front_stamp, uint64_t front_size, const RoundState* rs) {
     const DevGraph& g = *L->g;
     const uint32_t n = g.n;
-    stamp_++;
-    res_.rounds++;
-    res_.edge_visits += front_edges;
-    res_.vertex_visits += front_size;
-    // Isolated vertices outside L->bins are not visited by any kernel.
-    const uint64_t visited = front_stamp ? front_size : L->bins->size;
-    res_.algo_bytes += (g.w.p ? 12ull : 8ull) * front_edges + 40ull * visited;
     // Reset per-round counters: frontier, movers, new_movers, marked, pend_edges.
     PCC_CUDA(cudaMemsetAsync(&ctr_.p->frontier, 0, sizeof(uint32_t) * 4, ctx_->stream));
     PCC_CUDA(cudaMemsetAsync(&ctr_.p->pend_edges, 0, sizeof(unsigned long long), ctx_->stream));
@@ -644,7 +685,8 @@ class Engine {
     a.K_mut = L->K.p;
     a.C_mut = L->C.p;
     a.moved_cluster_stamp = mod_stamp_.p;
-    a.front_stamp = front_stamp ? next_stamp_.p : nullptr;
+    a.rs = rs;
+    a.front_stamp = (rs || front_stamp) ? next_stamp_.p : nullptr;
     a.front_val = front_stamp;
     const BinSet& bins = *L->bins;
     timer_.Begin(kPhaseBestMoves);
@@ -666,14 +708,14 @@ class Engine {
     timer_.Begin(kPhaseApply);
     if (!cfg_.async) {
       ApplyArgs ap{n, L->C.p, L->s.p, L->k.p, L->K.p, moves_.p, movers_.p, mod_stamp_.p, new_stamp_.p, stamp_,
-                   ctr_.p};
-      const unsigned grid = GridFor(ctx_, front_size);
+                   ctr_.p, rs};
+      const unsigned grid = GridFor(ctx_, rs ? uint64_t(n) : front_size);
       ApplyLeaveKernel<<<grid, kT, 0, ctx_->stream>>>(ap); PCC_COUNT(1);
       ApplyJoinKernel<<<grid, kT, 0, ctx_->stream>>>(ap); PCC_COUNT(1);
       PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, ZeroSizeInput{L->s.p, ctr_.p},
                                               StoreIndexIfSet{zero_ids_.p}, scan_tiles_,
                                               un_ ? zcount_.p : static_cast<uint32_t*>(nullptr)));
-      PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, NewMoverInput{new_stamp_.p, stamp_, ctr_.p},
+      PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, NewMoverInput{new_stamp_.p, stamp_, ctr_.p, rs},
                                               StoreIndexIfSet{new_list_.p}, scan_tiles_,
                                               static_cast<uint32_t*>(nullptr)));
       if (un_) {
@@ -683,37 +725,27 @@ class Engine {
         AssignNewKernel<<<grid, kT, 0, ctx_->stream>>>(ap, zero_ids_.p, new_list_.p); PCC_COUNT(1);
       }
       if (n) {
-        RefreshKfKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->K.p, L->Kf.p, mod_stamp_.p, stamp_);
+        RefreshKfKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->K.p, L->Kf.p, mod_stamp_.p, stamp_, rs);
         PCC_COUNT(1);
       }
       PCC_RETURN_IF_ERROR(LaunchCheck());
     }
     timer_.End(kPhaseApply);
+    if (cfg_.move_method == PCC_ALL_MOVE) return Status::Ok();
 
-    if (cfg_.move_method == PCC_ALL_MOVE) {
-      DevCounters hc;
-      PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
-      PCC_RETURN_IF_ERROR(Sync(ctx_));
-      if (!cfg_.async) res_.moves += hc.movers;
-      *next_nonempty = n > 0;
-      *next_front_stamp = 0;
-      *next_size = n;
-      *next_edges = g.m;
-      return Status::Ok();
-    }
     // Neighbourhood of the marked set (edgeMap), rows taken from the static
     // degree bins with a marked-row predicate, then the next frontier's size.
     timer_.Begin(kPhaseFrontier);
-    const PushNeighbors push{g.nbr.p, next_stamp_.p, stamp_};
+    const PushNeighbors push{g.nbr.p, next_stamp_.p, stamp_, rs};
     if (cfg_.move_method == PCC_NBHR_CLUSTER_MOVE) {
       LaunchEdgeIter(ctx_, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins, g.bins.host_counts,
-                     g.off.p, push, PredModifiedCluster{L->C.p, mod_stamp_.p, stamp_});  // rows with d > 0
+                     g.off.p, push, PredModifiedCluster{L->C.p, mod_stamp_.p, stamp_, rs});  // rows with d > 0
     } else {
       LaunchEdgeIter(ctx_, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins, g.bins.host_counts,
-                     g.off.p, push, PredStamp{moved_stamp_.p, stamp_});
+                     g.off.p, push, PredStamp{moved_stamp_.p, stamp_, rs});
     }
     if (n) {
-      CountDegreesKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g.off.p, PredStamp{next_stamp_.p, stamp_},
+      CountDegreesKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g.off.p, PredStamp{next_stamp_.p, stamp_, rs},
                                                                     &ctr_.p->pend_edges, &ctr_.p->frontier);
       PCC_COUNT(1);
       if (un_) {
@@ -725,19 +757,157 @@ class Engine {
     }
     PCC_RETURN_IF_ERROR(LaunchCheck());
     timer_.End(kPhaseFrontier);
+    return Status::Ok();
+  }
+
+  // One best-move round over `front` (host_counts known), driven from the
+  // host.  Builds the next frontier unless ALL_MOVE.  Returns whether the
+  // next frontier is non-empty (local_moved).
+  // front_stamp == 0: all vertices; else vertices with next_stamp == it.
+  Status Round(Level* L, uint32_t front_stamp, uint64_t front_edges, uint64_t front_size, bool* next_nonempty,
+               uint32_t* next_front_stamp, uint64_t* next_edges, uint64_t* next_size) {
+    const DevGraph& g = *L->g;
+    const uint32_t n = g.n;
+    stamp_++;
+    res_.rounds++;
+    res_.edge_visits += front_edges;
+    res_.vertex_visits += front_size;
+    // Isolated vertices outside L->bins are not visited by any kernel.
+    const uint64_t visited = front_stamp ? front_size : L->bins->size;
+    res_.algo_bytes += (g.w.p ? 12ull : 8ull) * front_edges + 40ull * visited;
+    PCC_RETURN_IF_ERROR(EnqueueRound(L, front_stamp, front_size, nullptr));
     DevCounters hc;
     PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
-    if (un_) {
+    if (un_ && cfg_.move_method != PCC_ALL_MOVE) {
       PCC_RETURN_IF_ERROR(gflags_.ToHost(h_gflags_.data(), un_->B));
       PCC_RETURN_IF_ERROR(gedges_.ToHost(h_gedges_.data(), un_->B));
     }
     PCC_RETURN_IF_ERROR(Sync(ctx_));
     if (!cfg_.async) res_.moves += hc.movers;
+    if (cfg_.move_method == PCC_ALL_MOVE) {
+      *next_nonempty = n > 0;
+      *next_front_stamp = 0;
+      *next_size = n;
+      *next_edges = g.m;
+      return Status::Ok();
+    }
     *next_front_stamp = stamp_;
     *next_size = hc.frontier;
     *next_edges = hc.pend_edges;
     *next_nonempty = hc.frontier > 0;
     return Status::Ok();
+  }
+
+  // IterateBestMoves with the round loop on the device: one round is
+  // captured into the body of a graph WHILE node, RoundEndKernel decides
+  // whether it runs again, and the host reads the counters once the loop is
+  // over.  Same kernels and arguments as the host-driven loop, with the stamp
+  // and the frontier taken from rs_.
+  Status IterateDevice(Level* L, int64_t num_inner, bool* moved_out) {
+    const DevGraph& g = *L->g;
+    PCC_RETURN_IF_ERROR(PrepareBestMoveKernels());
+    PCC_RETURN_IF_ERROR(PrepareHubKernels());
+    RoundState h{};
+    h.stamp = stamp_;  // RoundBeginKernel increments it first
+    h.front_all = 1;
+    h.front_edges = g.m;
+    h.front_size = g.n;
+    h.visited = L->bins->size;
+    PCC_RETURN_IF_ERROR(rs_.FromHost(&h, 1));
+    PCC_CUDA(cudaMemsetAsync(&ctr_.p->level_moved, 0, sizeof(uint32_t) * 2, ctx_->stream));  // level_moved, rounds
+    PCC_CUDA(cudaMemsetAsync(&ctr_.p->edge_visits, 0, sizeof(unsigned long long) * 2, ctx_->stream));
+    PCC_CUDA(cudaMemsetAsync(&ctr_.p->sync_moves, 0, sizeof(unsigned long long) * 2, ctx_->stream));
+
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    auto cleanup = [&] {
+      if (exec) cudaGraphExecDestroy(exec);
+      if (graph) cudaGraphDestroy(graph);
+    };
+    PCC_CUDA(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle loop;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&loop, graph, num_inner > 0 ? 1u : 0u,
+                                                     cudaGraphCondAssignDefault);
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = loop;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp);
+    if (e != cudaSuccess) {
+      cleanup();
+      cudaGetLastError();
+      ctx_->graphs_failed = true;
+      return IterateBestMoves(L, num_inner, moved_out);
+    }
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    const uint64_t launches0 = LaunchCounter();
+    const uint64_t fam0[kNumFamilies] = {ctx_->fam_launches[0], ctx_->fam_launches[1], ctx_->fam_launches[2],
+                                         ctx_->fam_launches[3]};
+    PhaseTimer* fam = ctx_->fam_timer;
+    ctx_->fam_timer = nullptr;
+    timer_.enabled = false;
+    if (cudaStreamBeginCaptureToGraph(ctx_->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+        cudaSuccess) {
+      timer_.enabled = true;
+      ctx_->fam_timer = fam;
+      cleanup();
+      cudaGetLastError();
+      ctx_->graphs_failed = true;
+      return IterateBestMoves(L, num_inner, moved_out);
+    }
+    RoundBeginKernel<<<1, 1, 0, ctx_->stream>>>(rs_.p); PCC_COUNT(1);
+    Status st = EnqueueRound(L, 0, g.n, rs_.p);
+    RoundEndKernel<<<1, 1, 0, ctx_->stream>>>(rs_.p, ctr_.p, loop, static_cast<uint32_t>(num_inner),
+                                              cfg_.move_method == PCC_ALL_MOVE ? 1 : 0, g.n, g.m, L->bins->size);
+    PCC_COUNT(1);
+    cudaGraph_t captured = nullptr;
+    e = cudaStreamEndCapture(ctx_->stream, &captured);
+    timer_.enabled = true;
+    ctx_->fam_timer = fam;
+    const uint64_t body_launches = LaunchCounter() - launches0;
+    uint64_t body_fam[kNumFamilies];
+    for (int f = 0; f < kNumFamilies; ++f) body_fam[f] = ctx_->fam_launches[f] - fam0[f];
+    if (!st.ok()) {
+      cleanup();
+      return st;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e == cudaSuccess) e = cudaGraphLaunch(exec, ctx_->stream);
+    if (e != cudaSuccess) {
+      cleanup();
+      cudaGetLastError();
+      return MakeError(PCC_INTERNAL, std::string("device round loop: ") + cudaGetErrorString(e));
+    }
+    DevCounters hc;
+    RoundState hr;
+    PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
+    PCC_RETURN_IF_ERROR(rs_.ToHost(&hr, 1));
+    const Status ss = Sync(ctx_);
+    cleanup();
+    PCC_RETURN_IF_ERROR(ss);
+    stamp_ = hr.stamp;
+    res_.rounds += static_cast<int32_t>(hc.rounds);
+    res_.edge_visits += hc.edge_visits;
+    res_.vertex_visits += hc.vertex_visits;
+    res_.algo_bytes += (g.w.p ? 12ull : 8ull) * hc.edge_visits + 40ull * hc.visited;
+    res_.moves += hc.sync_moves;
+    // Launch counts: the captured round once per executed round.
+    if (hc.rounds > 1) {
+      LaunchCounter() += body_launches * (hc.rounds - 1);
+      for (int f = 0; f < kNumFamilies; ++f) ctx_->fam_launches[f] += body_fam[f] * (hc.rounds - 1);
+    }
+    *moved_out = hc.level_moved != 0;
+    return Status::Ok();
+  }
+
+  // The round loop of one level: on the device when it can be (synchronous
+  // moves, one graph, no detailed timing), else driven from the host.
+  Status Iterate(Level* L, int64_t num_inner, bool* moved_out) {
+    if (!cfg_.async && !un_ && !ctx_->detailed_timing && !ctx_->graphs_failed)
+      return IterateDevice(L, num_inner, moved_out);
+    return IterateBestMoves(L, num_inner, moved_out);
   }
 
   // IterateBestMoves (parallel-correlation-clusterer.cc:340-365).
@@ -788,7 +958,7 @@ class Engine {
     int64_t iter = 0;
     for (iter = 0; iter < num_iterations; ++iter) {
       bool moved = false;
-      PCC_RETURN_IF_ERROR(IterateBestMoves(helper.get(), num_inner, &moved));
+      PCC_RETURN_IF_ERROR(Iterate(helper.get(), num_inner, &moved));
       if (!moved) {
         iter--;
         break;
@@ -833,12 +1003,12 @@ class Engine {
           PCC_RETURN_IF_ERROR(Li->K.Zero());
           AccumulateClustersKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->C.p, Li->k.p, Li->s.p,
                                                                                 Li->K.p); PCC_COUNT(1);
-          RefreshKfKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->K.p, Li->Kf.p, nullptr, 0);
+          RefreshKfKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->K.p, Li->Kf.p, nullptr, 0, nullptr);
           PCC_COUNT(1);
           PCC_RETURN_IF_ERROR(LaunchCheck());
         }
         bool moved = false;
-        PCC_RETURN_IF_ERROR(IterateBestMoves(Li, num_inner, &moved));
+        PCC_RETURN_IF_ERROR(Iterate(Li, num_inner, &moved));
         res_.refine_passes++;
         rec[static_cast<size_t>(i + 1)].reset();
       }
@@ -1059,7 +1229,7 @@ class Engine {
         PCC_RETURN_IF_ERROR(Li->K.Zero());
         AccumulateClustersKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->C.p, Li->k.p, Li->s.p,
                                                                               Li->K.p); PCC_COUNT(1);
-        RefreshKfKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->K.p, Li->Kf.p, nullptr, 0);
+        RefreshKfKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->K.p, Li->Kf.p, nullptr, 0, nullptr);
         PCC_COUNT(1);
         PCC_RETURN_IF_ERROR(LaunchCheck());
         for (uint32_t j = 0; j < B; ++j) {
@@ -1143,6 +1313,7 @@ class Engine {
   PhaseTimer fam_timer_;  // best-move kernel families (kFam*)
   // Disjoint-union mode (null for a single graph): per-graph frontier flags
   // and degree sums of the round, round-0 masks, the empty-id count.
+  DBuf<RoundState> rs_;  // device-side round loop state
   const UnionLayout* un_ = nullptr;
   DBuf<uint32_t> gflags_, gmask_, zcount_;
   DBuf<unsigned long long> gedges_;
@@ -1596,7 +1767,7 @@ Status BestMovesImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config
   PCC_RETURN_IF_ERROR(dk.FromHost(k, n));
   PCC_RETURN_IF_ERROR(dK.FromHost(K, n));
   if (n) {
-    RefreshKfKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, dK.p, dKf.p, nullptr, 0);
+    RefreshKfKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, dK.p, dKf.p, nullptr, 0, nullptr);
     PCC_COUNT(1);
     NodeKfKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, dk.p, dkf.p);
     PCC_COUNT(1);

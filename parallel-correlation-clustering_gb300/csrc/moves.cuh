@@ -80,6 +80,7 @@ __device__ __forceinline__ uint32_t WaveOf(uint32_t v, uint32_t salt, uint32_t w
 
 __device__ __forceinline__ bool InFront(const BMArgs& a, uint32_t v) {
   if (a.waves > 1 && WaveOf(v, a.wave_salt, a.waves) != a.wave) return false;
+  if (a.rs) return a.rs->front_all || a.front_stamp[v] == a.rs->front_val;
   return a.front_stamp == nullptr || a.front_stamp[v] == a.front_val;
 }
 
@@ -181,8 +182,8 @@ __device__ __forceinline__ bool Decide(const BMArgs& a, const VertexCtx& x, doub
       dest = uint32_t(i);
     }
     __stcg(&a.C_mut[x.v], dest);
-    a.moved_cluster_stamp[dest] = a.stamp;
-    a.moved_stamp[x.v] = a.stamp;
+    a.moved_cluster_stamp[dest] = StampIn(a.rs, a.stamp);
+    a.moved_stamp[x.v] = StampIn(a.rs, a.stamp);
     atomicAdd(&a.ctr->moves, 1ull);
     return false;
   }
@@ -196,7 +197,7 @@ __device__ __forceinline__ bool Decide(const BMArgs& a, const VertexCtx& x, doub
   }
   if (a.out_moves) a.out_moves[x.v] = v2 > 0 ? t2 : kNone;
   if (v2 > 0) {
-    a.moved_stamp[x.v] = a.stamp;
+    a.moved_stamp[x.v] = StampIn(a.rs, a.stamp);
     if (t2 != x.c) {
       a.moves[x.v] = t2;
       return true;

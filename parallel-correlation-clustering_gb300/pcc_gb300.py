@@ -217,6 +217,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.pcc_cluster_batch.argtypes = [ctypes.c_int, ctypes.c_uint32, vp, P(PccConfig), ctypes.c_uint32,
                                       vp, ctypes.c_uint32, ctypes.c_uint64, vp, vp, P(ctypes.c_double)]
     lib.pcc_cluster_batch.restype = ctypes.c_int
+    lib.pcc_set_detailed_timing.argtypes = [vp, ctypes.c_int32]
+    lib.pcc_set_detailed_timing.restype = None
     lib.pcc_cluster_union.argtypes = [vp, ctypes.c_uint32, vp, P(PccConfig), ctypes.c_uint64, vp, vp, vp]
     lib.pcc_cluster_union.restype = ctypes.c_int
     lib.pcc_server_create.argtypes = [P(vp), ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64]
@@ -316,6 +318,12 @@ class Context:
         if st != 0:
             msg = self.lib.pcc_last_error(self._h)
             raise PccError(st, msg.decode() if msg else "")
+
+    def set_detailed_timing(self, on: bool):
+        """pcc_set_detailed_timing: host-driven rounds with per-phase and
+        per-kernel-family CUDA events (on), or the device-side round loop
+        (off, the default)."""
+        self.lib.pcc_set_detailed_timing(self._h, 1 if on else 0)
 
     def bytes_in_use(self) -> int:
         return int(self.lib.pcc_device_bytes_in_use(self._h))

@@ -306,3 +306,35 @@ def test_async_mean_objective_matches_oracle(ctx, graphs, name, kind, res, move)
     mg, mc = float(np.mean(gpu)), float(np.mean(cpu))
     assert mg >= mc - 0.005 * abs(mc), (gpu, cpu)
     assert abs(mg - mc) <= 0.02 * abs(mc), (gpu, cpu)
+
+
+@pytest.mark.parametrize("move", [P.NBHR_CLUSTER_MOVE, P.NBHR_MOVE, P.ALL_MOVE])
+@pytest.mark.parametrize("refine", [True, False])
+def test_device_round_loop_matches_host_loop(graphs, move, refine):
+    """Synchronous rounds run as a device-side graph loop by default; with
+    detailed timing the host drives every round.  Labels, objective and the
+    control-flow counters must be identical (RMAT-16 has hubs above both hub
+    thresholds; the real-weight LFR graph takes the FP64 kernels)."""
+    c = P.Context(0)
+    try:
+        for name, kind, res in [("rmat16", "mod", 1.0), ("sbm3k_int", "corr", 0.05), ("lfr20k_real", "corr", 0.1)]:
+            dg = c.upload(graphs[name])
+            cfg = P.make_config(resolution=res, refine=refine, move_method=move, louvain_num_iterations=6,
+                                louvain_num_inner_iterations=5)
+            out = []
+            for detailed in (False, True):
+                c.set_detailed_timing(detailed)
+                if kind == "mod":
+                    lab, st = P.modularity_cluster(dg, cfg)
+                else:
+                    lab, st = P.correlation_cluster(dg, cfg)
+                out.append((lab, st))
+            (l0, s0), (l1, s1) = out
+            np.testing.assert_array_equal(l0, l1, err_msg=name)
+            for key in ("objective", "modularity", "num_clusters", "levels", "rounds", "refine_passes",
+                        "edge_visits", "vertex_visits", "moves", "algo_bytes_best_moves"):
+                assert s0[key] == s1[key], (name, key, s0[key], s1[key])
+            assert s1["ms_best_moves"] > 0
+            dg.free()
+    finally:
+        c.close()
