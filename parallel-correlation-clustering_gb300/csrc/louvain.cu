@@ -905,7 +905,8 @@ class Engine {
   // The round loop of one level: on the device when it can be (synchronous
   // moves, one graph, no detailed timing), else driven from the host.
   Status Iterate(Level* L, int64_t num_inner, bool* moved_out) {
-    if (!cfg_.async && !un_ && !ctx_->detailed_timing && !ctx_->graphs_failed)
+    if (!cfg_.async && !un_ && !ctx_->detailed_timing && !ctx_->graphs_failed &&
+        L->g->m >= ctx_->device_loop_min_entries)
       return IterateDevice(L, num_inner, moved_out);
     return IterateBestMoves(L, num_inner, moved_out);
   }

@@ -28,6 +28,11 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// Pool workers drive the rounds from the host: concurrent per-level graph
+// captures and instantiations contend for driver locks, which cost the
+// serving mix more capacity than the device-side loop saves.
+constexpr uint64_t kPoolDeviceLoopMinEntries = ~0ull;
+
 double MsBetween(Clock::time_point a, Clock::time_point b) {
   return std::chrono::duration<double, std::milli>(b - a).count();
 }
@@ -72,6 +77,7 @@ class Pool {
         Stop();
         return s;
       }
+      c->c.device_loop_min_entries = kPoolDeviceLoopMinEntries;
       ctxs_.push_back(c);
     }
     for (uint32_t i = 0; i < slots_; ++i) workers_.emplace_back([this, i] { Work(i); });

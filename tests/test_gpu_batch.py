@@ -38,8 +38,10 @@ def test_batch_matches_single_calls(ctx, small_graphs):
 
 
 def test_pool_batch_matches_single_calls(ctx, small_graphs):
-    """Per-graph configs run on the worker pool: every stat of the
-    standalone call, launches included, is reproduced."""
+    """Per-graph configs run on the worker pool: labels, objective and the
+    control-flow counters of the standalone call are reproduced (launch
+    counts differ: pool workers drive small graphs' rounds from the host,
+    a plain context runs them as a device-side loop)."""
     cfg = P.make_config(resolution=0.05, refine=True)
     graphs = small_graphs[:16]
     labels, stats, wall = P.cluster_batch(graphs, [cfg] * len(graphs), concurrency=8)
@@ -48,8 +50,8 @@ def test_pool_batch_matches_single_calls(ctx, small_graphs):
         ref, rst = _single(ctx, g, cfg, 0)
         np.testing.assert_array_equal(lab, ref)
         assert st["objective"] == rst["objective"]
-        assert st["edge_visits"] == rst["edge_visits"] and st["rounds"] == rst["rounds"]
-        assert st["kernel_launches"] == rst["kernel_launches"]
+        for key in ("edge_visits", "vertex_visits", "rounds", "levels", "moves", "num_clusters"):
+            assert st[key] == rst[key], key
 
 
 def _union_mix():
