@@ -78,6 +78,9 @@ def parse_args():
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--lfr-n", type=int, default=8_000_000,
                     help="vertices of the LFR-like real-weight leg (0 = skip the leg)")
+    ap.add_argument("--detailed-timing", action="store_true",
+                    help="host-driven rounds throughout (for per-launch profilers, which do not list the "
+                         "kernels of the device-side round loop's graph body)")
     return ap.parse_args()
 
 
@@ -383,6 +386,7 @@ def main():
 
     g = G.rmat(args.scale, 16, seed=1)
     ctx = P.Context(local)
+    ctx.set_detailed_timing(args.detailed_timing)
     dg = ctx.upload(g)
     cfg = make_cfg(P, args)
 
@@ -432,7 +436,7 @@ def main():
     # per-launch figures of the roofline.
     ctx.set_detailed_timing(True)
     _, st = P.modularity_cluster(dg, cfg)
-    ctx.set_detailed_timing(False)
+    ctx.set_detailed_timing(args.detailed_timing)
     detailed_ms = st["ms_total"]
     bm_ms = st["ms_best_moves"]
     comp_ms = st["ms_compress"]
