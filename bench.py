@@ -320,6 +320,17 @@ def serving_leg(args, P, G, ctx):
     }
 
 
+def reduce_over_ranks(dist, to_max, to_sum, device):
+    """Replicas: the slowest rank's times and the sum of every rank's counts
+    (one process per GPU; any backend)."""
+    import torch
+    t = torch.tensor([float(x) for x in to_max], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    s = torch.tensor([float(x) for x in to_sum], dtype=torch.float64, device=device)
+    dist.all_reduce(s, op=dist.ReduceOp.SUM)
+    return [float(x) for x in t.tolist()], [float(x) for x in s.tolist()]
+
+
 def run_reference(args):
     """--impl reference: the oracle port on all host threads; rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
@@ -488,12 +499,8 @@ def main():
     # Max time over ranks; edge visits summed over ranks.
     dev_s = dev_ms / 1000.0
     if dist is not None:
-        t = torch.tensor([dev_s, e2e_t], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        s = torch.tensor([ev, e2e_ev], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(s, op=dist.ReduceOp.SUM)
-        dev_s, e2e_t = float(t[0]), float(t[1])
-        ev_all, e2e_ev_all = float(s[0]), float(s[1])
+        (dev_s, e2e_t), (ev_all, e2e_ev_all) = reduce_over_ranks(dist, [dev_s, e2e_t], [ev, e2e_ev],
+                                                                 f"cuda:{local}")
     else:
         ev_all, e2e_ev_all = float(ev), float(e2e_ev)
 
