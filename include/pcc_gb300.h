@@ -326,8 +326,12 @@ pcc_status pcc_cluster_union(pcc_context* ctx, uint32_t num_graphs, const pcc_ba
  * pcc_server_submit and admitted, first come first served, as soon as a
  * worker slot is free and the request's device-memory estimate fits the HBM
  * budget next to the requests already running; admitted requests run
- * concurrently.  Each result is identical to a standalone
- * pcc_cluster_host_csr call.
+ * concurrently.  A worker that admits a correlation request (synchronous
+ * LOUVAIN, no subclustering) also admits the queued requests with the same
+ * config, up to 64 graphs and 8M entries, and runs them as one
+ * disjoint-union engine run (pcc_cluster_union).  The stats of such requests
+ * are the per-graph stats pcc_cluster_union documents.  Each label set and
+ * objective is identical to a standalone pcc_cluster_host_csr call.
  */
 typedef struct pcc_server pcc_server;
 

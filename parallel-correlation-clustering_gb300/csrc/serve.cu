@@ -63,9 +63,24 @@ struct Request {
   Clock::time_point t_submit, t_start, t_end;
 };
 
+// A request that can share a disjoint-union run (pcc_cluster_union):
+// correlation objective, synchronous LOUVAIN moves, no subclustering.
+bool UnionEligible(const Request& r) {
+  return r.objective == 0 && r.n > 0 && r.cfg.clustering_moves_method == PCC_LOUVAIN && !r.cfg.async &&
+         r.cfg.subclustering_method == PCC_NONE_SUBCLUSTERING;
+}
+
+constexpr size_t kMaxGroupGraphs = 64;
+constexpr uint64_t kMaxGroupEntries = 8ull << 20;
+
 class Pool {
  public:
-  Pool(int device, uint32_t slots, uint64_t budget) : device_(device), budget_(budget) {
+  // group_unions: a worker that takes a union-eligible request also takes
+  // the queued requests with the same config (up to kMaxGroupGraphs graphs
+  // and kMaxGroupEntries entries, within the budget) and runs them as one
+  // disjoint union; every label and objective equals its standalone call.
+  Pool(int device, uint32_t slots, uint64_t budget, bool group_unions = false)
+      : device_(device), budget_(budget), group_unions_(group_unions) {
     slots_ = std::max<uint32_t>(1, slots);
   }
 
@@ -133,11 +148,17 @@ class Pool {
     cv_done_.notify_all();
   }
 
+  static uint32_t* OutOf(Request* r) {
+    if (r->labels_out) return r->labels_out;
+    r->labels.resize(std::max<uint32_t>(r->n, 1));
+    return r->labels.data();
+  }
+
   void Work(uint32_t slot) {
     pcc_context* ctx = ctxs_[slot];
     cudaSetDevice(device_);
     for (;;) {
-      Request* r = nullptr;
+      std::vector<Request*> group;
       {
         std::unique_lock<std::mutex> lk(mu_);
         // First come, first served: the head of the queue runs when its
@@ -146,23 +167,60 @@ class Pool {
           return stop_ || (!queue_.empty() && (!budget_ || reserved_ + queue_.front()->est_bytes <= budget_));
         });
         if (stop_) return;
-        r = queue_.front();
+        const auto now = Clock::now();
+        Request* r = queue_.front();
         queue_.pop_front();
         reserved_ += r->est_bytes;
-        r->t_start = Clock::now();
+        r->t_start = now;
+        group.push_back(r);
+        if (group_unions_ && UnionEligible(*r)) {
+          uint64_t entries = r->m;
+          for (auto it = queue_.begin(); it != queue_.end() && group.size() < kMaxGroupGraphs;) {
+            Request* q = *it;
+            if (UnionEligible(*q) && std::memcmp(&q->cfg, &r->cfg, sizeof(pcc_config)) == 0 &&
+                entries + q->m <= kMaxGroupEntries && (!budget_ || reserved_ + q->est_bytes <= budget_)) {
+              reserved_ += q->est_bytes;
+              q->t_start = now;
+              entries += q->m;
+              group.push_back(q);
+              it = queue_.erase(it);
+            } else {
+              ++it;
+            }
+          }
+        }
       }
-      uint32_t* out = r->labels_out;
-      if (!out) {
-        r->labels.resize(std::max<uint32_t>(r->n, 1));
-        out = r->labels.data();
+      std::vector<pcc_status> st(group.size(), PCC_OK);
+      bool done = false;
+      if (group.size() > 1) {
+        std::vector<pcc_batch_graph> gs;
+        std::vector<uint32_t*> outs;
+        std::vector<pcc_stats> stats(group.size());
+        for (Request* q : group) {
+          gs.push_back(pcc_batch_graph{q->n, q->m, q->off, q->nbr, q->w, q->k});
+          outs.push_back(OutOf(q));
+        }
+        if (pcc_cluster_union(ctx, static_cast<uint32_t>(group.size()), gs.data(), &group[0]->cfg, 0, outs.data(),
+                              stats.data(), nullptr) == PCC_OK) {
+          for (size_t i = 0; i < group.size(); ++i) group[i]->stats = stats[i];
+          done = true;
+        }
       }
-      const pcc_status s = pcc_cluster_host_csr(ctx, r->n, r->m, r->off, r->nbr, r->w, &r->cfg, r->objective,
-                                                r->objective == 1 ? nullptr : r->k, out, &r->stats);
-      if (r->stats_out) *r->stats_out = r->stats;
+      if (!done) {  // one request, or the union failed: standalone calls
+        for (size_t i = 0; i < group.size(); ++i) {
+          Request* r = group[i];
+          st[i] = pcc_cluster_host_csr(ctx, r->n, r->m, r->off, r->nbr, r->w, &r->cfg, r->objective,
+                                       r->objective == 1 ? nullptr : r->k, OutOf(r), &r->stats);
+        }
+      }
       {
         std::lock_guard<std::mutex> lk(mu_);
-        reserved_ -= r->est_bytes;
-        Finish(r, s);
+        for (size_t i = 0; i < group.size(); ++i) {
+          Request* r = group[i];
+          if (r->stats_out) *r->stats_out = r->stats;
+          reserved_ -= r->est_bytes;
+          Finish(r, st[i]);
+        }
       }
       cv_work_.notify_all();  // memory was released: the queue head may fit now
     }
@@ -171,6 +229,7 @@ class Pool {
   int device_;
   uint32_t slots_;
   uint64_t budget_;
+  bool group_unions_ = false;
   uint64_t reserved_ = 0;
   bool stop_ = false;
   std::vector<pcc_context*> ctxs_;
@@ -280,7 +339,7 @@ pcc_status pcc_server_create(pcc_server** out, int device, uint32_t slots, uint6
   if (!out) return PCC_INVALID_ARGUMENT;
   *out = nullptr;
   auto s = std::make_unique<pcc_server>();
-  s->pool = std::make_unique<Pool>(device, slots, hbm_budget);
+  s->pool = std::make_unique<Pool>(device, slots, hbm_budget, /*group_unions=*/true);
   const pcc_status st = s->pool->Start();
   if (st != PCC_OK) return st;
   *out = s.release();

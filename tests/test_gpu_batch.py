@@ -165,6 +165,30 @@ def test_server_results_alone_and_in_the_mix(ctx, small_graphs):
         srv.close()
 
 
+def test_server_groups_queued_requests_into_unions(ctx, small_graphs):
+    """One worker slot and a burst of same-config correlation requests: the
+    queued ones are admitted together as a union run (their stats carry no
+    launch count), and every result equals the standalone call."""
+    cfg = P.make_config(resolution=0.05, refine=True)
+    other = P.make_config(resolution=0.1, refine=True)
+    srv = P.Server(slots=1, hbm_budget=0)
+    try:
+        tickets = []
+        for i, g in enumerate(small_graphs[:20]):
+            c, obj = (other, 1) if i % 5 == 4 else (cfg, 0)
+            tickets.append((srv.submit(g, c, obj), g, c, obj))
+        grouped = 0
+        for t, g, c, obj in tickets:
+            lab, st, _, _ = srv.wait(t)
+            ref, rst = _single(ctx, g, c, obj)
+            np.testing.assert_array_equal(lab, ref)
+            assert st["objective"] == rst["objective"]
+            grouped += obj == 0 and st["kernel_launches"] == 0 and st["rounds"] == rst["rounds"]
+        assert grouped > 1
+    finally:
+        srv.close()
+
+
 def test_server_rejects_request_over_budget(built, small_graphs):
     srv = P.Server(slots=2, hbm_budget=1 << 20)
     try:
