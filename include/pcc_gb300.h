@@ -283,11 +283,11 @@ typedef struct pcc_batch_graph {
  * be NULL) receives the batch's wall time.  The first failing graph's
  * status is returned; the others stop taking new work.
  *
- * When num_configs == 1, every objective is correlation and the config is
- * LOUVAIN, synchronous and without subclustering, the batch runs as disjoint
- * unions (pcc_cluster_union on one context; stats as documented there).
- * Otherwise each graph runs on the worker pool and its stats equal a
- * standalone call's.
+ * When the configs differ in resolution only (num_configs == 1 included), are
+ * LOUVAIN, synchronous and without subclustering, and the offset is 0 or every
+ * objective is correlation, the batch runs as disjoint unions
+ * (pcc_cluster_union on one context; stats as documented there).  Otherwise
+ * each graph runs on the worker pool and its stats equal a standalone call's.
  */
 pcc_status pcc_cluster_batch(int device, uint32_t num_graphs, const pcc_batch_graph* graphs,
                              const pcc_config* configs, uint32_t num_configs,
@@ -296,28 +296,33 @@ pcc_status pcc_cluster_batch(int device, uint32_t num_graphs, const pcc_batch_gr
                              pcc_stats* stats, double* wall_ms);
 
 /*
- * Batched clustering as a disjoint-union graph: graphs that share one
- * correlation config run as one engine run, and each kernel launch of a
- * round covers all of them.  Each graph keeps the control flow of
- * RefineClusters_subroutine
+ * Batched clustering as a disjoint-union graph: the graphs run as one engine
+ * run, and each kernel launch of a round covers all of them.  Each graph keeps
+ * the control flow of RefineClusters_subroutine
  * (clustering/clusterers/parallel-correlation-clusterer.cc:476-629) for itself:
  *   - its own level count;
  *   - its own inner-loop exit;
  *   - its own refinement levels;
- *   - new-cluster ids from its own empty ids.
- * So its labels and objective equal those of a standalone
- * pcc_correlation_cluster call (bit for bit with integer weights and node
- * weights, else within FP64 summation order for the objective).
- * config: LOUVAIN, synchronous, NONE_SUBCLUSTERING.  Graphs are packed in
- * order into unions of at most max_union_entries adjacency entries (0:
- * 2^31) and 2^31 vertices.  out_labels[i]: host uint32[n_i] (may be NULL
- * when n_i == 0).  stats (NULL or one per graph) carries objective,
- * num_clusters, levels, rounds, refine_passes and edge_visits of each graph
- * (the other fields are 0).  batch_stats (may be NULL) receives the totals,
- * phase times and kernel launches of the whole call.
+ *   - new-cluster ids from its own empty ids;
+ *   - its own resolution.
+ * So its labels and objective equal those of a standalone call (bit for bit
+ * with integer weights and node weights, else within FP64 summation order for
+ * the objective; modularity within 1e-12 relative).
+ * configs: one for all graphs or one per graph, equal in every field but the
+ * resolution; LOUVAIN, synchronous, NONE_SUBCLUSTERING.  objectives: NULL
+ * (correlation) or one per graph (0 correlation, 1 modularity: node weights
+ * = degrees, resolution / sum of degrees, which needs edge_weight_offset 0).
+ * Graphs are packed in order into unions of at most max_union_entries
+ * adjacency entries (0: 2^31) and 2^31 vertices.  out_labels[i]: host
+ * uint32[n_i] (may be NULL when n_i == 0).  stats (NULL or one per graph)
+ * carries objective, modularity, num_clusters, levels, rounds,
+ * refine_passes and edge_visits of each graph (the other fields are 0).
+ * batch_stats (may be NULL) receives the totals, phase times and kernel
+ * launches of the whole call.
  */
 pcc_status pcc_cluster_union(pcc_context* ctx, uint32_t num_graphs, const pcc_batch_graph* graphs,
-                             const pcc_config* config, uint64_t max_union_entries,
+                             const pcc_config* configs, uint32_t num_configs,
+                             const int32_t* objectives, uint64_t max_union_entries,
                              uint32_t* const* out_labels, pcc_stats* stats,
                              pcc_stats* batch_stats);
 
@@ -326,10 +331,11 @@ pcc_status pcc_cluster_union(pcc_context* ctx, uint32_t num_graphs, const pcc_ba
  * pcc_server_submit and admitted, first come first served, as soon as a
  * worker slot is free and the request's device-memory estimate fits the HBM
  * budget next to the requests already running; admitted requests run
- * concurrently.  A worker that admits a correlation request (synchronous
- * LOUVAIN, no subclustering) also admits the queued requests with the same
- * config, up to 64 graphs and 8M entries, and runs them as one
- * disjoint-union engine run (pcc_cluster_union).  The stats of such requests
+ * concurrently.  A worker that admits a request with a synchronous LOUVAIN
+ * config without subclustering also admits the queued requests whose config
+ * differs in resolution only (and objective, with offset 0), up to 64 graphs
+ * and 8M entries, and runs them as one disjoint-union engine run
+ * (pcc_cluster_union).  The stats of such requests
  * are the per-graph stats pcc_cluster_union documents.  Each label set and
  * objective is identical to a standalone pcc_cluster_host_csr call.
  */

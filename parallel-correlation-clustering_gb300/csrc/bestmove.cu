@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
       for (int o = G / 2; o >= 1; o >>= 1) smax = max(smax, __shfl_xor_sync(kFull, smax, o));
       float Y = 0.f, e = 0.f, lo = -CUDART_INF_F;
       if (leader) {
-        const float R = __fmul_rn(a.res32, __fmul_rn(static_cast<float>(x.kv), a.Kf[cu]));
+        const float R = __fmul_rn(Res32Of(a, x.v), __fmul_rn(static_cast<float>(x.kv), a.Kf[cu]));
         Y = __fsub_rn(static_cast<float>(Si - smax), R);
         e = FilterBound(R, Y, static_cast<float>(Si), static_cast<float>(change));
         lo = __fsub_rn(Y, e);
@@ -113,11 +113,11 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
 #pragma unroll
       for (int o = G / 2; o >= 1; o >>= 1) U = fmaxf(U, __shfl_xor_sync(kFull, U, o));
       if (leader && __fadd_rn(Y, e) >= U) {
-        val = ValOf(a, x.kv, change, S, LdK<kAsync>(a.K + cu));
+        val = ValOf(a, x, change, S, LdK<kAsync>(a.K + cu));
         id = cu;
       }
     } else if (leader) {
-      val = ValOf(a, x.kv, change, S, LdK<kAsync>(a.K + cu));
+      val = ValOf(a, x, change, S, LdK<kAsync>(a.K + cu));
       id = cu;
     }
 #pragma unroll
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
       for (uint32_t i = lane; i < nused; i += 32) {
         const uint32_t slot = used[i];
         const long long Si = static_cast<long long>(vals[slot]);
-        const float R = __fmul_rn(a.res32, __fmul_rn(k32, a.Kf[keys[slot]]));
+        const float R = __fmul_rn(Res32Of(a, x.v), __fmul_rn(k32, a.Kf[keys[slot]]));
         const float Y = __fsub_rn(static_cast<float>(Si - smax), R);
         U = fmaxf(U, __fsub_rn(Y, FilterBound(R, Y, static_cast<float>(Si), c32)));
       }
@@ -264,10 +264,10 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
         const uint32_t slot = used[i];
         const uint32_t key = keys[slot];
         const long long Si = static_cast<long long>(vals[slot]);
-        const float R = __fmul_rn(a.res32, __fmul_rn(k32, a.Kf[key]));
+        const float R = __fmul_rn(Res32Of(a, x.v), __fmul_rn(k32, a.Kf[key]));
         const float Y = __fsub_rn(static_cast<float>(Si - smax), R);
         if (__fadd_rn(Y, FilterBound(R, Y, static_cast<float>(Si), c32)) < U) continue;
-        const double val = ValOf(a, x.kv, change, static_cast<double>(Si), LdK<kAsync>(a.K + key));
+        const double val = ValOf(a, x, change, static_cast<double>(Si), LdK<kAsync>(a.K + key));
         if (Better(val, key, best, bid)) {
           best = val;
           bid = key;
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
         const uint32_t slot = used[i];
         const uint32_t key = keys[slot];
         const double S = AsDouble<kInt>(vals[slot]);
-        const double val = ValOf(a, x.kv, change, S, LdK<kAsync>(a.K + key));
+        const double val = ValOf(a, x, change, S, LdK<kAsync>(a.K + key));
         if (Better(val, key, best, bid)) {
           best = val;
           bid = key;
@@ -335,7 +335,7 @@ __device__ __noinline__ bool GroupExact(const BMArgs& a, const VertexCtx& x, boo
   if (fp64) {
     change = ChangeOf(a, x, static_cast<double>(T));
     if (contender) {
-      val = ValOf(a, x.kv, change, static_cast<double>(S), KD);
+      val = ValOf(a, x, change, static_cast<double>(S), KD);
       id = cu;
     }
   }
@@ -369,7 +369,7 @@ __device__ __noinline__ bool WarpExact(const BMArgs& a, const VertexCtx& x, V T,
     const uint32_t slot = used[i];
     if (slot == 0xFFFFu) continue;
     const uint32_t key = keys[slot];
-    const double val = ValOf(a, x.kv, change, static_cast<double>(vals[slot]), a.K[key]);
+    const double val = ValOf(a, x, change, static_cast<double>(vals[slot]), a.K[key]);
     if (Better(val, key, best, bid)) {
       best = val;
       bid = key;
@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
     }
     const float k32 = vvalid ? a.kf[x.v] : 0.f;
     const float Kc32 = vvalid ? a.Kf[x.c] : 0.f;
-    const ChangeApproxT<int> ca = ApproxChange<int>(a.res32, a.int_nw != 0, k32, Kc32, T);
+    const ChangeApproxT<int> ca = ApproxChange<int>(Res32Of(a, x.v), a.int_nw != 0, k32, Kc32, T);
     const float cabs = ChangeAbsBound(ca);
     // FP32 pre-filter over the group's leaders.
     FilterVal f{0.f, 0.f, false};
@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
     float lo = -CUDART_INF_F;
     if (leader) {
       KfD = a.Kf[cu];
-      f = FilterOf<int>(a.res32, k32, KfD, S, smax, cabs);
+      f = FilterOf<int>(Res32Of(a, x.v), k32, KfD, S, smax, cabs);
       if (f.sane) lo = __fsub_rn(f.Y, f.e);
     }
     float U = lo;
@@ -491,7 +491,7 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
     uint32_t ctarget = kNone;
     if (vvalid && single) {
       const float KfA = lead.id != kNone ? a.Kf[lead.id] : 0.f;
-      cres = CertifyDecision<int>(ca, a.res32, k32, lead.id != kNone, lead.S, KfA, lead.id, a.n, &ctarget);
+      cres = CertifyDecision<int>(ca, Res32Of(a, x.v), k32, lead.id != kNone, lead.S, KfA, lead.id, a.n, &ctarget);
     }
     const uint32_t cmove = cres == kUncertain ? kNone : CertifiedMove(a, x, ctarget, cres == kCertMove);
     const bool fp64 = vvalid && (replay || cres == kUncertain);
@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     }
     T = __shfl_sync(kFull, T, 0);
     const float k32 = a.kf[x.v];
-    const ChangeApproxT<V> ca = ApproxChange<V>(a.res32, a.int_nw != 0, k32, a.Kf[x.c], T);
+    const ChangeApproxT<V> ca = ApproxChange<V>(Res32Of(a, x.v), a.int_nw != 0, k32, a.Kf[x.c], T);
     const float cabs = ChangeAbsBound(ca);
     V vmax = sizeof(V) == 4 ? V(INT_MIN) : V(LLONG_MIN);
     for (uint32_t i = lane; i < nused; i += 32) vmax = max(vmax, vals[used[i]]);
@@ -623,7 +623,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     float U = -CUDART_INF_F;
     for (uint32_t i = lane; i < nused; i += 32) {
       const uint32_t slot = used[i];
-      const FilterVal f = FilterOf<V>(a.res32, k32, a.Kf[keys[slot]], vals[slot], smax, cabs);
+      const FilterVal f = FilterOf<V>(Res32Of(a, x.v), k32, a.Kf[keys[slot]], vals[slot], smax, cabs);
       if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
     }
     U = WarpMaxFinite(U);
@@ -631,7 +631,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     for (uint32_t i = lane; i < nused; i += 32) {
       const uint32_t slot = used[i];
       const uint32_t key = keys[slot];
-      const FilterVal f = FilterOf<V>(a.res32, k32, a.Kf[key], vals[slot], smax, cabs);
+      const FilterVal f = FilterOf<V>(Res32Of(a, x.v), k32, a.Kf[key], vals[slot], smax, cabs);
       if (f.sane && __fadd_rn(f.Y, f.e) < U) {
         keys[slot] = kNone;  // not a contender: cleared now, skipped later
         vals[slot] = 0;
@@ -655,7 +655,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     uint32_t ctarget = kNone;
     if (single) {
       const float KfA = lead.id != kNone ? a.Kf[lead.id] : 0.f;
-      cres = CertifyDecision<V>(ca, a.res32, k32, lead.id != kNone, lead.S, KfA, lead.id, a.n, &ctarget);
+      cres = CertifyDecision<V>(ca, Res32Of(a, x.v), k32, lead.id != kNone, lead.S, KfA, lead.id, a.n, &ctarget);
     }
     const uint32_t cmove = cres == kUncertain ? kNone : CertifiedMove(a, x, ctarget, cres == kCertMove);
     bool append = false;

@@ -95,6 +95,11 @@ struct UnionLayout {
   std::vector<uint32_t> vbase;  // B + 1 (host)
   std::vector<uint64_t> ebase;  // B + 1 (host)
   DBuf<uint32_t> d_vbase;       // B + 1
+  // Per-graph resolution the moves use (modularity graphs: res / sum of
+  // degrees); d_res / d_res32 are set when the graphs' resolutions differ.
+  std::vector<double> res;
+  DBuf<double> d_res;
+  DBuf<float> d_res32;
 };
 
 // Index j < B of the last base[j] <= x (bases ascending): the graph owning
@@ -112,10 +117,11 @@ __device__ __forceinline__ uint32_t GraphOf(const T* __restrict__ base, uint32_t
 
 // Uploads graphs[0..B) (host CSR, each n > 0) as one union graph with
 // shifted offsets and neighbour ids, validating every graph's CSR.  Node
-// weights: *k receives the union's node weights when any graph has them
-// (1 for the graphs without); *int_nw = every node weight is an integer.
-Status UploadUnion(Context* ctx, uint32_t B, const pcc_batch_graph* const* graphs, DevGraph* g, UnionLayout* u,
-                   DBuf<double>* k, bool* int_nw);
+// weights: *k receives the union's node weights when any graph has them or
+// takes its degrees (degree_weights[j], modularity), 1 for the others;
+// *int_nw = every node weight is an integer.
+Status UploadUnion(Context* ctx, uint32_t B, const pcc_batch_graph* const* graphs, const uint8_t* degree_weights,
+                   DevGraph* g, UnionLayout* u, DBuf<double>* k, bool* int_nw);
 
 // Device counters of one call (all in one allocation).
 struct DevCounters {
@@ -214,7 +220,14 @@ struct BMArgs {
   uint32_t* moved_cluster_stamp;
   // non-null: stamp and frontier come from here (front_stamp is the array)
   const RoundState* rs;
+  // non-null: per-vertex resolution (graphs of a union with their own
+  // resolutions); else res / res32 for every vertex
+  const double* vres;
+  const float* vres32;
 };
+
+__device__ __forceinline__ double ResOf(const BMArgs& a, uint32_t v) { return a.vres ? a.vres[v] : a.res; }
+__device__ __forceinline__ float Res32Of(const BMArgs& a, uint32_t v) { return a.vres32 ? a.vres32[v] : a.res32; }
 
 // Configures (shared-memory limit, occupancy) every synchronous best-move
 // kernel once per process, so that launches captured into a graph make no

@@ -173,10 +173,19 @@ __global__ void UnionEntryFixKernel(uint64_t m, const uint32_t* __restrict__ vba
   }
 }
 
+// Node weights = degrees on the graphs with has_k[j] == 2 (modularity).
+__global__ void UnionDegreeWeightsKernel(uint32_t n, const uint64_t* __restrict__ off,
+                                         const uint32_t* __restrict__ vbase, uint32_t B,
+                                         const uint8_t* __restrict__ has_k, double* k) {
+  for (uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; v < n; v += uint64_t(gridDim.x) * blockDim.x)
+    if (has_k[GraphOf(vbase, B, static_cast<uint32_t>(v))] == 2)
+      k[v] = static_cast<double>(off[v + 1] - off[v]);
+}
+
 }  // namespace
 
-Status UploadUnion(Context* ctx, uint32_t B, const pcc_batch_graph* const* graphs, DevGraph* g, UnionLayout* u,
-                   DBuf<double>* k, bool* int_nw) {
+Status UploadUnion(Context* ctx, uint32_t B, const pcc_batch_graph* const* graphs, const uint8_t* degree_weights,
+                   DevGraph* g, UnionLayout* u, DBuf<double>* k, bool* int_nw) {
   if (B == 0) return MakeError(PCC_INVALID_ARGUMENT, "empty union");
   u->B = B;
   u->vbase.assign(B + 1, 0);
@@ -197,10 +206,10 @@ Status UploadUnion(Context* ctx, uint32_t B, const pcc_batch_graph* const* graph
     u->vbase[j + 1] = static_cast<uint32_t>(nv);
     u->ebase[j + 1] = ne;
     has_w[j] = x.weights != nullptr;
-    has_k[j] = x.node_weights != nullptr;
+    has_k[j] = (degree_weights && degree_weights[j]) ? 2 : (x.node_weights != nullptr ? 1 : 0);
     any_w |= has_w[j] != 0;
     any_k |= has_k[j] != 0;
-    if (x.node_weights)
+    if (x.node_weights && has_k[j] == 1)
       for (uint32_t v = 0; v < x.n && *int_nw; ++v)
         if (x.node_weights[v] != std::floor(x.node_weights[v])) *int_nw = false;
   }
@@ -225,7 +234,7 @@ Status UploadUnion(Context* ctx, uint32_t B, const pcc_batch_graph* const* graph
         PCC_CUDA(cudaMemcpyAsync(g->w.p + u->ebase[j], x.weights, sizeof(float) * x.m, cudaMemcpyHostToDevice,
                                  ctx->stream));
     }
-    if (x.node_weights)
+    if (has_k[j] == 1)
       PCC_CUDA(cudaMemcpyAsync(k->p + u->vbase[j], x.node_weights, sizeof(double) * x.n, cudaMemcpyHostToDevice,
                                ctx->stream));
   }
@@ -251,6 +260,10 @@ Status UploadUnion(Context* ctx, uint32_t B, const pcc_batch_graph* const* graph
   }
   CheckCsrKernel<<<Blocks(std::max<uint64_t>(m, uint64_t(n) + 1), 256, cap), 256, 0, ctx->stream>>>(
       n, m, g->off.p, g->nbr.p, bad.p); PCC_COUNT(1);
+  if (any_k) {
+    UnionDegreeWeightsKernel<<<Blocks(n, 256, cap), 256, 0, ctx->stream>>>(n, g->off.p, u->d_vbase.p, B, d_has_k.p,
+                                                                          k->p); PCC_COUNT(1);
+  }
   int hbad = 0;
   PCC_RETURN_IF_ERROR(bad.ToHost(&hbad, 1));
   PCC_RETURN_IF_ERROR(Sync(ctx));

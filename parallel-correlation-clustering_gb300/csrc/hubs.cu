@@ -318,7 +318,7 @@ __device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double
     for (uint32_t s = tid; s < cap; s += BT) {
       const uint32_t key = skeys[s];
       if (key == kNone) continue;
-      const FilterVal f = FilterOf<I>(a.res32, k32, a.Kf[key], static_cast<I>(svals[s]), smax, c32);
+      const FilterVal f = FilterOf<I>(Res32Of(a, x.v), k32, a.Kf[key], static_cast<I>(svals[s]), smax, c32);
       if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
     }
     if (tid == 0) sh.ncont = 0;
@@ -330,7 +330,7 @@ __device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double
       const I S = static_cast<I>(svals[s]);
       skeys[s] = kNone;
       svals[s] = V(0);
-      const FilterVal f = FilterOf<I>(a.res32, k32, a.Kf[key], S, smax, c32);
+      const FilterVal f = FilterOf<I>(Res32Of(a, x.v), k32, a.Kf[key], S, smax, c32);
       if (f.sane && __fadd_rn(f.Y, f.e) < U) continue;
       const double KD = a.K[key];
       const unsigned long long ko = KOrder(KD);
@@ -341,7 +341,7 @@ __device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double
         sh.cont_key[pos] = key;
         sh.cont_S[pos] = S;
       } else {
-        KeepBest(lv, lid, ValOf(a, x.kv, change, static_cast<double>(S), KD), key);  // list full: now
+        KeepBest(lv, lid, ValOf(a, x, change, static_cast<double>(S), KD), key);  // list full: now
       }
     }
     bool single;
@@ -359,11 +359,11 @@ __device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double
         const I S = static_cast<I>(sh.cont_S[i]);
         const double KD = a.K[key];
         if (S == lead.S && KOrder(KD) == lead.K) continue;  // the leading class
-        KeepBest(lv, lid, ValOf(a, x.kv, change, static_cast<double>(S), KD), key);
+        KeepBest(lv, lid, ValOf(a, x, change, static_cast<double>(S), KD), key);
       }
     }
     if (tid == 0 && lead.id != kNone)
-      KeepBest(lv, lid, ValOf(a, x.kv, change, static_cast<double>(lead.S), a.K[lead.id]), lead.id);
+      KeepBest(lv, lid, ValOf(a, x, change, static_cast<double>(lead.S), a.K[lead.id]), lead.id);
   } else {
     for (uint32_t s = tid; s < cap; s += BT) {
       const uint32_t key = skeys[s];
@@ -371,7 +371,7 @@ __device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double
       const V sv = svals[s];
       skeys[s] = kNone;
       svals[s] = V(0);
-      KeepBest(lv, lid, ValOf(a, x.kv, change, static_cast<double>(sv), LdK<kAsync>(a.K + key)), key);
+      KeepBest(lv, lid, ValOf(a, x, change, static_cast<double>(sv), LdK<kAsync>(a.K + key)), key);
     }
   }
   BlockArgmax<BT>(lv, lid, sh.red_k, sh.red_i);

@@ -340,6 +340,17 @@ __global__ void GraphRankBaseKernel(uint32_t B, const uint32_t* __restrict__ vba
     out[j] = j < B ? rank[vbase[j]] : *total;
 }
 
+// Per-vertex resolution of a union level: the owning graph's.
+__global__ void __launch_bounds__(kT) GraphResKernel(uint32_t n, const uint32_t* __restrict__ vbase, uint32_t B,
+                                                     const double* __restrict__ res, const float* __restrict__ res32,
+                                                     double* vres, float* vres32) {
+  for (uint64_t v = uint64_t(blockIdx.x) * kT + threadIdx.x; v < n; v += uint64_t(gridDim.x) * kT) {
+    const uint32_t j = GraphOf(vbase, B, static_cast<uint32_t>(v));
+    vres[v] = res[j];
+    vres32[v] = res32[j];
+  }
+}
+
 // ids[v] = v on the graphs with mask[j] != 0.
 __global__ void __launch_bounds__(kT) IdentityGraphsKernel(uint32_t n, uint32_t* ids,
                                                            const uint32_t* __restrict__ vbase, uint32_t B,
@@ -531,6 +542,9 @@ struct Level {
   // its value is 0 and no vertex can join it.
   const BinSet* bins = nullptr;
   bool int_mode = false;
+  // Per-vertex resolution (unions of graphs with different resolutions).
+  DBuf<double> vres;
+  DBuf<float> vres32;
 };
 
 struct RunResult {
@@ -633,6 +647,13 @@ class Engine {
       PCC_RETURN_IF_ERROR(LaunchCheck());
     }
     L->int_mode = IntModeFor(*g, cfg_.edge_weight_offset);
+    if (un_ && un_->d_res.p && n) {
+      PCC_RETURN_IF_ERROR(L->vres.Alloc(ctx_, n));
+      PCC_RETURN_IF_ERROR(L->vres32.Alloc(ctx_, n));
+      GraphResKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, un_->d_vbase.p, un_->B, un_->d_res.p,
+                                                                un_->d_res32.p, L->vres.p, L->vres32.p);
+      PCC_COUNT(1);
+    }
     if (d_labels) {
       PCC_RETURN_IF_ERROR(EnsureAllBins(ctx_, g));
       L->bins = &g->bins_all;
@@ -686,6 +707,8 @@ class Engine {
     a.C_mut = L->C.p;
     a.moved_cluster_stamp = mod_stamp_.p;
     a.rs = rs;
+    a.vres = L->vres.p;
+    a.vres32 = L->vres32.p;
     a.front_stamp = (rs || front_stamp) ? next_stamp_.p : nullptr;
     a.front_val = front_stamp;
     const BinSet& bins = *L->bins;
@@ -1515,10 +1538,47 @@ Status ClusterImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config* 
   return Status::Ok();
 }
 
-// One disjoint union: graphs gs (each n > 0), results into out_labels[idx[j]]
-// and stats[idx[j]]; totals added to *tot.
+// Modularity of the union's modularity graphs (want[j] != 0), segmented by
+// graph: entries whose ends share a label, and degree sums per label.
+__global__ void __launch_bounds__(kT) ModularityCountsKernel(uint32_t n, const uint64_t* __restrict__ off,
+                                                             const uint32_t* __restrict__ nbr,
+                                                             const uint32_t* __restrict__ L,
+                                                             const uint32_t* __restrict__ vbase, uint32_t B,
+                                                             const uint8_t* __restrict__ want,
+                                                             unsigned long long* same, unsigned long long* deg) {
+  for (uint64_t u = uint64_t(blockIdx.x) * kT + threadIdx.x; u < n; u += uint64_t(gridDim.x) * kT) {
+    const uint32_t j = GraphOf(vbase, B, static_cast<uint32_t>(u));
+    if (!want[j]) continue;
+    const uint32_t lu = L[u];
+    unsigned long long cnt = 0;
+    for (uint64_t e = off[u]; e < off[u + 1]; ++e) cnt += L[nbr[e]] == lu ? 1ull : 0ull;
+    if (cnt) atomicAdd(&same[j], cnt);
+    if (off[u + 1] > off[u]) atomicAdd(&deg[lu], static_cast<unsigned long long>(off[u + 1] - off[u]));
+  }
+}
+
+// sub[j] = sum over graph j's labels c of res_j * d_c * d_c / total_j
+// (ComputeModularity, parallel-modularity-clusterer.cc:36-66).
+__global__ void __launch_bounds__(kT) ModularitySubKernel(uint32_t n, const unsigned long long* __restrict__ deg,
+                                                          const uint32_t* __restrict__ vbase, uint32_t B,
+                                                          const double* __restrict__ res,
+                                                          const double* __restrict__ total, double* sub) {
+  for (uint64_t c = uint64_t(blockIdx.x) * kT + threadIdx.x; c < n; c += uint64_t(gridDim.x) * kT) {
+    if (!deg[c]) continue;
+    const uint32_t j = GraphOf(vbase, B, static_cast<uint32_t>(c));
+    const double d = static_cast<double>(deg[c]);
+    atomicAdd(&sub[j], Dmul(Dmul(res[j], d), d) / total[j]);
+  }
+}
+
+// One disjoint union: graphs gs (each n > 0) with their own resolutions and
+// objectives (modularity: node weights = degrees, resolution / sum of
+// degrees), results into out_labels[idx[j]] and stats[idx[j]]; totals added
+// to *tot.
 Status UnionChunk(Context* ctx, const pcc_config& cfg, const std::vector<const pcc_batch_graph*>& gs,
-                  const std::vector<uint32_t>& idx, uint32_t* const* out_labels, pcc_stats* stats, pcc_stats* tot) {
+                  const std::vector<uint32_t>& idx, const std::vector<double>& res_in,
+                  const std::vector<uint8_t>& modularity, uint32_t* const* out_labels, pcc_stats* stats,
+                  pcc_stats* tot) {
   const uint32_t B = static_cast<uint32_t>(gs.size());
   EventTimer timer(ctx->stream);
   const uint64_t launches0 = LaunchCounter();
@@ -1526,14 +1586,32 @@ Status UnionChunk(Context* ctx, const pcc_config& cfg, const std::vector<const p
   UnionLayout u;
   DBuf<double> dk;
   bool int_nw = true;
-  PCC_RETURN_IF_ERROR(UploadUnion(ctx, B, gs.data(), &g0, &u, &dk, &int_nw));
+  PCC_RETURN_IF_ERROR(UploadUnion(ctx, B, gs.data(), modularity.data(), &g0, &u, &dk, &int_nw));
   const uint32_t n = g0.n;
+  // ComputeModularityConfig (parallel/parallel-graph-utils.cc:141-153) per
+  // modularity graph: resolution / sum of degrees (= its entries).
+  u.res.resize(B);
+  bool uniform = true;
+  for (uint32_t j = 0; j < B; ++j) {
+    u.res[j] = modularity[j] ? res_in[j] / static_cast<double>(gs[j]->m) : res_in[j];
+    uniform = uniform && u.res[j] == u.res[0];
+  }
+  if (!uniform) {
+    std::vector<float> r32(B);
+    for (uint32_t j = 0; j < B; ++j) r32[j] = FilterF32(u.res[j]);
+    PCC_RETURN_IF_ERROR(u.d_res.Alloc(ctx, B));
+    PCC_RETURN_IF_ERROR(u.d_res32.Alloc(ctx, B));
+    PCC_RETURN_IF_ERROR(u.d_res.FromHost(u.res.data(), B));
+    PCC_RETURN_IF_ERROR(u.d_res32.FromHost(r32.data(), B));
+  }
+  pcc_config ecfg = cfg;
+  ecfg.resolution = u.res[0];  // every vertex's resolution when uniform
   std::vector<Engine::GraphRun> runs;
   std::vector<uint32_t> ncl;
   DBuf<uint32_t> dout, dids;
   PCC_RETURN_IF_ERROR(dout.Alloc(ctx, n));
   PCC_RETURN_IF_ERROR(dids.Alloc(ctx, n));
-  Engine eng(ctx, cfg, int_nw);
+  Engine eng(ctx, ecfg, int_nw);
   PCC_RETURN_IF_ERROR(eng.RunUnion(g0, u, dk.p, dout.p, dids.p, &runs, &ncl));
   // ComputeObjective per graph.
   DBuf<double> ones, K, acc;
@@ -1552,8 +1630,41 @@ Status UnionChunk(Context* ctx, const pcc_config& cfg, const std::vector<const p
   PCC_RETURN_IF_ERROR(acc.Zero());
   AccumulateClustersKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, dids.p, kp, s.p, K.p); PCC_COUNT(1);
   ObjectiveUnionKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, g0.off.p, g0.nbr.p, g0.wp(), dids.p, kp, K.p,
-                                                                cfg.edge_weight_offset, u.d_vbase.p, B, acc.p,
+                                                                ecfg.edge_weight_offset, u.d_vbase.p, B, acc.p,
                                                                 acc.p + B); PCC_COUNT(1);
+  // ComputeModularity per modularity graph.
+  bool any_mod = false;
+  for (uint32_t j = 0; j < B; ++j) any_mod = any_mod || modularity[j];
+  std::vector<unsigned long long> hsame(B, 0);
+  std::vector<double> hsub(B, 0.0);
+  DBuf<unsigned long long> same, deg;
+  DBuf<double> sub, mres, mtot;
+  DBuf<uint8_t> want;
+  if (any_mod) {
+    std::vector<double> r(B), t(B);
+    for (uint32_t j = 0; j < B; ++j) {
+      r[j] = res_in[j];
+      t[j] = static_cast<double>(gs[j]->m);
+    }
+    PCC_RETURN_IF_ERROR(same.Alloc(ctx, B));
+    PCC_RETURN_IF_ERROR(sub.Alloc(ctx, B));
+    PCC_RETURN_IF_ERROR(deg.Alloc(ctx, n));
+    PCC_RETURN_IF_ERROR(mres.Alloc(ctx, B));
+    PCC_RETURN_IF_ERROR(mtot.Alloc(ctx, B));
+    PCC_RETURN_IF_ERROR(want.Alloc(ctx, B));
+    PCC_RETURN_IF_ERROR(same.Zero());
+    PCC_RETURN_IF_ERROR(sub.Zero());
+    PCC_RETURN_IF_ERROR(deg.Zero());
+    PCC_RETURN_IF_ERROR(mres.FromHost(r.data(), B));
+    PCC_RETURN_IF_ERROR(mtot.FromHost(t.data(), B));
+    PCC_RETURN_IF_ERROR(want.FromHost(modularity.data(), B));
+    ModularityCountsKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, g0.off.p, g0.nbr.p, dids.p, u.d_vbase.p, B,
+                                                                    want.p, same.p, deg.p); PCC_COUNT(1);
+    ModularitySubKernel<<<GridFor(ctx, n), kT, 0, ctx->stream>>>(n, deg.p, u.d_vbase.p, B, mres.p, mtot.p, sub.p);
+    PCC_COUNT(1);
+    PCC_RETURN_IF_ERROR(same.ToHost(hsame.data(), B));
+    PCC_RETURN_IF_ERROR(sub.ToHost(hsub.data(), B));
+  }
   PCC_RETURN_IF_ERROR(LaunchCheck());
   std::vector<double> hacc(2ull * B);
   std::vector<uint32_t> hl(n);
@@ -1567,7 +1678,11 @@ Status UnionChunk(Context* ctx, const pcc_config& cfg, const std::vector<const p
     if (!stats) continue;
     pcc_stats& st = stats[i];
     std::memset(&st, 0, sizeof(st));
-    st.objective = hacc[j] - cfg.resolution * hacc[B + j] / 2;
+    st.objective = hacc[j] - u.res[j] * hacc[B + j] / 2;
+    if (modularity[j] && gs[j]->m) {
+      const double total = static_cast<double>(gs[j]->m);
+      st.modularity = (static_cast<double>(hsame[j]) - hsub[j]) / total;
+    }
     st.num_clusters = static_cast<int32_t>(ncl[j]);
     st.levels = runs[j].levels;
     st.rounds = runs[j].rounds;
@@ -1601,38 +1716,66 @@ Status UnionChunk(Context* ctx, const pcc_config& cfg, const std::vector<const p
   return Status::Ok();
 }
 
+// Configs that can share a union run: equal in every field but the
+// resolution.
+bool UnionCompatible(const pcc_config& a, const pcc_config& b) {
+  pcc_config x = a, y = b;
+  x.resolution = 0;
+  y.resolution = 0;
+  return std::memcmp(&x, &y, sizeof(pcc_config)) == 0;
+}
+
 Status ClusterUnionImpl(pcc_context* pctx, uint32_t num_graphs, const pcc_batch_graph* graphs,
-                        const pcc_config* config, uint64_t max_entries, uint32_t* const* out_labels,
-                        pcc_stats* stats, pcc_stats* batch_stats) {
-  if (!pctx || !config) return MakeError(PCC_INVALID_ARGUMENT, "null context or config");
+                        const pcc_config* configs, uint32_t num_configs, const int32_t* objectives,
+                        uint64_t max_entries, uint32_t* const* out_labels, pcc_stats* stats,
+                        pcc_stats* batch_stats) {
+  if (!pctx || !configs) return MakeError(PCC_INVALID_ARGUMENT, "null context or config");
   if (num_graphs && (!graphs || !out_labels)) return MakeError(PCC_INVALID_ARGUMENT, "null graphs or out_labels");
+  if (num_configs != 1 && num_configs != num_graphs)
+    return MakeError(PCC_INVALID_ARGUMENT, "num_configs must be 1 or num_graphs");
   Context* ctx = &pctx->c;
   PCC_CUDA(cudaSetDevice(ctx->device));
   if (batch_stats) std::memset(batch_stats, 0, sizeof(*batch_stats));
   if (max_entries == 0) max_entries = 1ull << 31;
+  const pcc_config& cfg0 = configs[0];
+  bool any_mod = false;
   for (uint32_t i = 0; i < num_graphs; ++i) {
     if (!out_labels[i] && graphs[i].n) return MakeError(PCC_INVALID_ARGUMENT, "null out_labels entry");
     if (graphs[i].n > kMaxVertices) return MakeError(PCC_INVALID_ARGUMENT, "n must be at most 2^32 - 32");
     if (graphs[i].m >= 0xFFFFFFFFull)
       return MakeError(PCC_INVALID_ARGUMENT, "graphs with 2^32 or more entries are not supported");
+    if (objectives && objectives[i] != 0 && objectives[i] != 1)
+      return MakeError(PCC_INVALID_ARGUMENT, "objective must be 0 (correlation) or 1 (modularity)");
+    if (num_configs > 1 && !UnionCompatible(configs[i], cfg0))
+      return MakeError(PCC_INVALID_ARGUMENT, "union configs may differ in resolution only");
+    any_mod = any_mod || (objectives && objectives[i] == 1);
     if (graphs[i].n == 0 && stats) std::memset(&stats[i], 0, sizeof(pcc_stats));
   }
+  // ComputeModularityConfig sets the offset to 0 for modularity graphs.
+  if (any_mod && cfg0.edge_weight_offset != 0)
+    return MakeError(PCC_INVALID_ARGUMENT, "a union with modularity graphs needs edge_weight_offset 0");
   std::vector<const pcc_batch_graph*> gs;
   std::vector<uint32_t> idx;
+  std::vector<double> res;
+  std::vector<uint8_t> mod;
   uint64_t nv = 0, ne = 0;
   for (uint32_t i = 0; i <= num_graphs; ++i) {
     const bool flush = i == num_graphs ||
                        (!gs.empty() && (ne + graphs[i].m > max_entries || nv + graphs[i].n > kMaxVertices / 2));
     if (flush && !gs.empty()) {
-      PCC_RETURN_IF_ERROR(UnionChunk(ctx, *config, gs, idx, out_labels, stats, batch_stats));
+      PCC_RETURN_IF_ERROR(UnionChunk(ctx, cfg0, gs, idx, res, mod, out_labels, stats, batch_stats));
       gs.clear();
       idx.clear();
+      res.clear();
+      mod.clear();
       nv = ne = 0;
     }
     if (i == num_graphs) break;
     if (graphs[i].n == 0) continue;  // empty labels, zero stats
     gs.push_back(&graphs[i]);
     idx.push_back(i);
+    res.push_back(configs[num_configs == 1 ? 0 : i].resolution);
+    mod.push_back(objectives && objectives[i] == 1 ? 1 : 0);
     nv += graphs[i].n;
     ne += graphs[i].m;
   }
@@ -1648,11 +1791,12 @@ using namespace pcc;
 extern "C" {
 
 pcc_status pcc_cluster_union(pcc_context* ctx, uint32_t num_graphs, const pcc_batch_graph* graphs,
-                             const pcc_config* config, uint64_t max_union_entries, uint32_t* const* out_labels,
-                             pcc_stats* stats, pcc_stats* batch_stats) {
+                             const pcc_config* configs, uint32_t num_configs, const int32_t* objectives,
+                             uint64_t max_union_entries, uint32_t* const* out_labels, pcc_stats* stats,
+                             pcc_stats* batch_stats) {
   try {
-    return Finish(ctx, ClusterUnionImpl(ctx, num_graphs, graphs, config, max_union_entries, out_labels, stats,
-                                        batch_stats));
+    return Finish(ctx, ClusterUnionImpl(ctx, num_graphs, graphs, configs, num_configs, objectives, max_union_entries,
+                                        out_labels, stats, batch_stats));
   } catch (const std::exception& e) {
     return Finish(ctx, MakeError(PCC_INTERNAL, e.what()));
   }

@@ -107,12 +107,12 @@ __device__ __forceinline__ VertexCtx LoadVertex(const BMArgs& a, uint32_t v) {
 
 __device__ __forceinline__ double ChangeOf(const BMArgs& a, const VertexCtx& x, double T) {
   // change_in_objective -= together.NetWeight(kv * (K_c - kv))   (:483-488)
-  return Dsub(0.0, Dsub(T, Dmul(a.res, Dmul(x.kv, Dsub(x.Kc, x.kv)))));
+  return Dsub(0.0, Dsub(T, Dmul(ResOf(a, x.v), Dmul(x.kv, Dsub(x.Kc, x.kv)))));
 }
 
-__device__ __forceinline__ double ValOf(const BMArgs& a, double kv, double change, double S, double KD) {
+__device__ __forceinline__ double ValOf(const BMArgs& a, const VertexCtx& x, double change, double S, double KD) {
   // change + data.NetWeight(moving_nodes_weight * K_D)   (:493-497)
-  return Dadd(change, Dsub(S, Dmul(a.res, Dmul(kv, KD))));
+  return Dadd(change, Dsub(S, Dmul(ResOf(a, x.v), Dmul(x.kv, KD))));
 }
 
 // FP32 pre-filter of the INT-mode sync path.  For candidate D with exact

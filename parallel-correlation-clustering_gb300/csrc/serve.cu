@@ -64,10 +64,21 @@ struct Request {
 };
 
 // A request that can share a disjoint-union run (pcc_cluster_union):
-// correlation objective, synchronous LOUVAIN moves, no subclustering.
+// synchronous LOUVAIN moves without subclustering; modularity needs offset 0.
 bool UnionEligible(const Request& r) {
-  return r.objective == 0 && r.n > 0 && r.cfg.clustering_moves_method == PCC_LOUVAIN && !r.cfg.async &&
-         r.cfg.subclustering_method == PCC_NONE_SUBCLUSTERING;
+  return r.n > 0 && r.cfg.clustering_moves_method == PCC_LOUVAIN && !r.cfg.async &&
+         r.cfg.subclustering_method == PCC_NONE_SUBCLUSTERING &&
+         (r.objective == 0 || r.cfg.edge_weight_offset == 0);
+}
+
+// Two eligible requests share a run when their configs differ in resolution
+// only (and, with modularity in the run, the offset is 0 -- checked above).
+bool SameRunConfig(const Request& a, const Request& b) {
+  pcc_config x = a.cfg, y = b.cfg;
+  x.resolution = 0;
+  y.resolution = 0;
+  if (std::memcmp(&x, &y, sizeof(pcc_config)) != 0) return false;
+  return (a.objective == 0 && b.objective == 0) || a.cfg.edge_weight_offset == 0;
 }
 
 constexpr size_t kMaxGroupGraphs = 64;
@@ -177,7 +188,7 @@ class Pool {
           uint64_t entries = r->m;
           for (auto it = queue_.begin(); it != queue_.end() && group.size() < kMaxGroupGraphs;) {
             Request* q = *it;
-            if (UnionEligible(*q) && std::memcmp(&q->cfg, &r->cfg, sizeof(pcc_config)) == 0 &&
+            if (UnionEligible(*q) && SameRunConfig(*q, *r) &&
                 entries + q->m <= kMaxGroupEntries && (!budget_ || reserved_ + q->est_bytes <= budget_)) {
               reserved_ += q->est_bytes;
               q->t_start = now;
@@ -196,12 +207,17 @@ class Pool {
         std::vector<pcc_batch_graph> gs;
         std::vector<uint32_t*> outs;
         std::vector<pcc_stats> stats(group.size());
+        std::vector<pcc_config> cfgs;
+        std::vector<int32_t> objs;
         for (Request* q : group) {
-          gs.push_back(pcc_batch_graph{q->n, q->m, q->off, q->nbr, q->w, q->k});
+          gs.push_back(pcc_batch_graph{q->n, q->m, q->off, q->nbr, q->w, q->objective == 1 ? nullptr : q->k});
           outs.push_back(OutOf(q));
+          cfgs.push_back(q->cfg);
+          objs.push_back(q->objective);
         }
-        if (pcc_cluster_union(ctx, static_cast<uint32_t>(group.size()), gs.data(), &group[0]->cfg, 0, outs.data(),
-                              stats.data(), nullptr) == PCC_OK) {
+        if (pcc_cluster_union(ctx, static_cast<uint32_t>(group.size()), gs.data(), cfgs.data(),
+                              static_cast<uint32_t>(cfgs.size()), objs.data(), 0, outs.data(), stats.data(),
+                              nullptr) == PCC_OK) {
           for (size_t i = 0; i < group.size(); ++i) group[i]->stats = stats[i];
           done = true;
         }
@@ -279,10 +295,17 @@ pcc_status pcc_cluster_batch(int device, uint32_t num_graphs, const pcc_batch_gr
     if (objectives && objectives[i] != 0 && objectives[i] != 1) return PCC_INVALID_ARGUMENT;
   }
   const auto t0 = Clock::now();
-  // One shared correlation config: disjoint unions on one context.
-  bool as_union = num_configs == 1 && configs[0].clustering_moves_method == PCC_LOUVAIN && !configs[0].async &&
+  // Configs that differ in resolution only: disjoint unions on one context.
+  bool as_union = configs[0].clustering_moves_method == PCC_LOUVAIN && !configs[0].async &&
                   configs[0].subclustering_method == PCC_NONE_SUBCLUSTERING;
-  for (uint32_t i = 0; as_union && objectives && i < num_graphs; ++i) as_union = objectives[i] == 0;
+  for (uint32_t i = 1; as_union && i < num_configs; ++i) {
+    pcc_config x = configs[i], y = configs[0];
+    x.resolution = 0;
+    y.resolution = 0;
+    as_union = std::memcmp(&x, &y, sizeof(pcc_config)) == 0;
+  }
+  for (uint32_t i = 0; as_union && objectives && i < num_graphs; ++i)
+    as_union = objectives[i] == 0 || configs[0].edge_weight_offset == 0;
   if (as_union) {
     pcc_context* c = nullptr;
     pcc_status s = pcc_create(&c, device, hbm_budget);
@@ -292,7 +315,7 @@ pcc_status pcc_cluster_batch(int device, uint32_t num_graphs, const pcc_batch_gr
     // per entry counted) fit next to the fixed 64 MB.
     const uint64_t fixed = 64ull << 20;
     const uint64_t cap = hbm_budget == 0 ? 0 : std::max<uint64_t>(1, (hbm_budget > fixed ? hbm_budget - fixed : 0) / 252);
-    s = pcc_cluster_union(c, num_graphs, graphs, configs, cap, out_labels, stats, nullptr);
+    s = pcc_cluster_union(c, num_graphs, graphs, configs, num_configs, objectives, cap, out_labels, stats, nullptr);
     pcc_destroy(c);
     if (wall_ms) *wall_ms = pcc::MsBetween(t0, Clock::now());
     return s;

@@ -219,7 +219,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.pcc_cluster_batch.restype = ctypes.c_int
     lib.pcc_set_detailed_timing.argtypes = [vp, ctypes.c_int32]
     lib.pcc_set_detailed_timing.restype = None
-    lib.pcc_cluster_union.argtypes = [vp, ctypes.c_uint32, vp, P(PccConfig), ctypes.c_uint64, vp, vp, vp]
+    lib.pcc_cluster_union.argtypes = [vp, ctypes.c_uint32, vp, vp, ctypes.c_uint32, vp, ctypes.c_uint64, vp, vp,
+                                      vp]
     lib.pcc_cluster_union.restype = ctypes.c_int
     lib.pcc_server_create.argtypes = [P(vp), ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64]
     lib.pcc_server_create.restype = ctypes.c_int
@@ -510,20 +511,29 @@ def _batch_arrays(graphs, node_weights):
     return arr, keep, labels
 
 
-def cluster_union(ctx: "Context", graphs: Sequence[CsrGraph], config: PccConfig, node_weights=None,
+def cluster_union(ctx: "Context", graphs: Sequence[CsrGraph], configs, objectives=None, node_weights=None,
                   max_union_entries: int = 0):
-    """pcc_cluster_union: independent graphs with one correlation config as
-    disjoint-union engine runs on `ctx`.  Returns (label arrays, per-graph
-    stats dicts, batch stats dict)."""
+    """pcc_cluster_union: independent graphs as disjoint-union engine runs on
+    `ctx`.  configs: one PccConfig or one per graph (differing in resolution
+    only); objectives: None (correlation) or 0/1 per graph.  Returns (label
+    arrays, per-graph stats dicts, batch stats dict)."""
     lib = load_library()
     ng = len(graphs)
     arr, keep, labels = _batch_arrays(graphs, node_weights)
+    if isinstance(configs, PccConfig):
+        cfgs = (PccConfig * 1)(configs)
+        ncfg = 1
+    else:
+        cfgs = (PccConfig * ng)(*configs)
+        ncfg = ng
+    objs = None if objectives is None else np.ascontiguousarray(objectives, dtype=np.int32)
     outs = (ctypes.c_void_p * max(ng, 1))(*[lab.ctypes.data for lab in labels])
     stats = (PccStats * max(ng, 1))()
     tot = PccStats()
-    st = lib.pcc_cluster_union(ctx.handle, ng, ctypes.cast(arr, ctypes.c_void_p), ctypes.byref(config),
-                               max_union_entries, ctypes.cast(outs, ctypes.c_void_p),
-                               ctypes.cast(stats, ctypes.c_void_p), ctypes.byref(tot))
+    st = lib.pcc_cluster_union(ctx.handle, ng, ctypes.cast(arr, ctypes.c_void_p), ctypes.cast(cfgs, ctypes.c_void_p),
+                               ncfg, None if objs is None else objs.ctypes.data, max_union_entries,
+                               ctypes.cast(outs, ctypes.c_void_p), ctypes.cast(stats, ctypes.c_void_p),
+                               ctypes.byref(tot))
     del keep
     ctx.check(st)
     return [labels[i][:graphs[i].n] for i in range(ng)], [stats[i].as_dict() for i in range(ng)], tot.as_dict()

@@ -42,11 +42,13 @@ def test_pool_batch_matches_single_calls(ctx, small_graphs):
     control-flow counters of the standalone call are reproduced (launch
     counts differ: pool workers drive small graphs' rounds from the host,
     a plain context runs them as a device-side loop)."""
-    cfg = P.make_config(resolution=0.05, refine=True)
+    # Configs that differ in more than the resolution cannot share a union.
+    cfgs = [P.make_config(resolution=0.05, refine=True, move_method=P.NBHR_MOVE if i % 2 else P.NBHR_CLUSTER_MOVE)
+            for i in range(16)]
     graphs = small_graphs[:16]
-    labels, stats, wall = P.cluster_batch(graphs, [cfg] * len(graphs), concurrency=8)
+    labels, stats, wall = P.cluster_batch(graphs, cfgs, concurrency=8)
     assert wall > 0
-    for g, lab, st in zip(graphs, labels, stats):
+    for g, lab, st, cfg in zip(graphs, labels, stats, cfgs):
         ref, rst = _single(ctx, g, cfg, 0)
         np.testing.assert_array_equal(lab, ref)
         assert st["objective"] == rst["objective"]
@@ -90,6 +92,31 @@ def test_union_matches_single_every_control_path(ctx, move, refine):
             np.testing.assert_array_equal(labels[i], ref, err_msg=f"graph {i} iters {iters}")
             for key in UNION_STATS:
                 assert stats[i][key] == rst[key], (i, key, iters)
+
+
+@pytest.mark.parametrize("move", [P.NBHR_CLUSTER_MOVE, P.ALL_MOVE])
+def test_union_mixed_resolutions_and_objectives(ctx, small_graphs, move):
+    """Graphs with their own resolutions and objectives in one union: every
+    vertex reads its graph's resolution (modularity: resolution / sum of
+    degrees, degree node weights).  Labels and objective are bit-identical to
+    standalone calls (integer sums); modularity within 1e-12."""
+    rng = np.random.default_rng(12)
+    graphs = small_graphs[:14] + [G.rmat(12, 16, seed=3)]
+    cfgs = [P.make_config(resolution=float(rng.choice([0.01, 0.1, 0.5])), refine=True, move_method=move)
+            for _ in graphs]
+    objs = np.array([i % 2 for i in range(len(graphs))], dtype=np.int32)
+    labels, stats, _ = P.cluster_union(ctx, graphs, cfgs, objectives=objs)
+    for i, g in enumerate(graphs):
+        ref, rst = _single(ctx, g, cfgs[i], int(objs[i]))
+        np.testing.assert_array_equal(labels[i], ref, err_msg=f"graph {i}")
+        assert stats[i]["objective"] == rst["objective"]
+        assert stats[i]["rounds"] == rst["rounds"] and stats[i]["levels"] == rst["levels"]
+        if objs[i] == 1:
+            assert stats[i]["modularity"] == pytest.approx(rst["modularity"], rel=1e-12, abs=1e-15)
+    # The batch call routes such a batch to the union as well.
+    labels2, stats2, _ = P.cluster_batch(graphs, cfgs, objectives=objs)
+    for a, b in zip(labels, labels2):
+        np.testing.assert_array_equal(a, b)
 
 
 def test_union_node_weights_and_real_weights(ctx, small_graphs):
