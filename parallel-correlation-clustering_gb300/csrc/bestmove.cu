@@ -96,27 +96,7 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
     const double change = ChangeOf(a, x, T);
     double val = -CUDART_INF;
     uint32_t id = kNone;
-    if (kInt && !kAsync) {
-      // FP32 pre-filter; exact FP64 only for the survivors.
-      const int Si = static_cast<int>(S);
-      int smax = leader ? Si : INT_MIN;
-#pragma unroll
-      for (int o = G / 2; o >= 1; o >>= 1) smax = max(smax, __shfl_xor_sync(kFull, smax, o));
-      float Y = 0.f, e = 0.f, lo = -CUDART_INF_F;
-      if (leader) {
-        const float R = __fmul_rn(Res32Of(a, x.v), __fmul_rn(static_cast<float>(x.kv), a.Kf[cu]));
-        Y = __fsub_rn(static_cast<float>(Si - smax), R);
-        e = FilterBound(R, Y, static_cast<float>(Si), static_cast<float>(change));
-        lo = __fsub_rn(Y, e);
-      }
-      float U = lo;
-#pragma unroll
-      for (int o = G / 2; o >= 1; o >>= 1) U = fmaxf(U, __shfl_xor_sync(kFull, U, o));
-      if (leader && __fadd_rn(Y, e) >= U) {
-        val = ValOf(a, x, change, S, LdK<kAsync>(a.K + cu));
-        id = cu;
-      }
-    } else if (leader) {
+    if (leader) {
       val = ValOf(a, x, change, S, LdK<kAsync>(a.K + cu));
       id = cu;
     }
@@ -243,46 +223,14 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
     const uint32_t nused = *used_count;
     double best = -CUDART_INF;
     uint32_t bid = kNone;
-    if (kInt && !kAsync) {
-      // FP32 pre-filter (see FilterBound); exact FP64 only for survivors.
-      long long smax = LLONG_MIN;
-      for (uint32_t i = lane; i < nused; i += 32) smax = max(smax, static_cast<long long>(vals[used[i]]));
-#pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) smax = max(smax, __shfl_xor_sync(kFull, smax, o));
-      const float k32 = static_cast<float>(x.kv), c32 = static_cast<float>(change);
-      float U = -CUDART_INF_F;
-      for (uint32_t i = lane; i < nused; i += 32) {
-        const uint32_t slot = used[i];
-        const long long Si = static_cast<long long>(vals[slot]);
-        const float R = __fmul_rn(Res32Of(a, x.v), __fmul_rn(k32, a.Kf[keys[slot]]));
-        const float Y = __fsub_rn(static_cast<float>(Si - smax), R);
-        U = fmaxf(U, __fsub_rn(Y, FilterBound(R, Y, static_cast<float>(Si), c32)));
-      }
-#pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) U = fmaxf(U, __shfl_xor_sync(kFull, U, o));
-      for (uint32_t i = lane; i < nused; i += 32) {
-        const uint32_t slot = used[i];
-        const uint32_t key = keys[slot];
-        const long long Si = static_cast<long long>(vals[slot]);
-        const float R = __fmul_rn(Res32Of(a, x.v), __fmul_rn(k32, a.Kf[key]));
-        const float Y = __fsub_rn(static_cast<float>(Si - smax), R);
-        if (__fadd_rn(Y, FilterBound(R, Y, static_cast<float>(Si), c32)) < U) continue;
-        const double val = ValOf(a, x, change, static_cast<double>(Si), LdK<kAsync>(a.K + key));
-        if (Better(val, key, best, bid)) {
-          best = val;
-          bid = key;
-        }
-      }
-    } else {
-      for (uint32_t i = lane; i < nused; i += 32) {
-        const uint32_t slot = used[i];
-        const uint32_t key = keys[slot];
-        const double S = AsDouble<kInt>(vals[slot]);
-        const double val = ValOf(a, x, change, S, LdK<kAsync>(a.K + key));
-        if (Better(val, key, best, bid)) {
-          best = val;
-          bid = key;
-        }
+    for (uint32_t i = lane; i < nused; i += 32) {
+      const uint32_t slot = used[i];
+      const uint32_t key = keys[slot];
+      const double S = AsDouble<kInt>(vals[slot]);
+      const double val = ValOf(a, x, change, S, LdK<kAsync>(a.K + key));
+      if (Better(val, key, best, bid)) {
+        best = val;
+        bid = key;
       }
     }
 #pragma unroll
@@ -716,7 +664,7 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
   int ng = 0;
   for (int b = kBinG4; b <= kBinG32; ++b) ng += want(b) ? 1 : 0;
   FamBegin(ctx, kFamGroup);
-  if (kCert) {
+  if constexpr (kCert) {
     // One wave of resident CTAs (grid-stride kernels).
     auto group_bin = [&](auto k, int bin, uint64_t per_block) -> Status {
       if (!want(bin)) return Status::Ok();
@@ -755,16 +703,22 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
     PCC_COUNT(1);
     return Status::Ok();
   };
-  if (kCert && a.narrow) {
-    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<256, int>, CertWarpSmem<256, int>(), kBinW128, sms * 16));
-    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<512, int>, CertWarpSmem<512, int>(), kBinW256, sms * 8));
-    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<1024, int>, CertWarpSmem<1024, int>(), kBinW512, sms * 6));
-    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<2048, int>, CertWarpSmem<2048, int>(), kBinW1000, sms * 3));
-  } else if (kCert) {
-    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<256, long long>, CertWarpSmem<256, long long>(), kBinW128, sms * 16));
-    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<512, long long>, CertWarpSmem<512, long long>(), kBinW256, sms * 8));
-    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<1024, long long>, CertWarpSmem<1024, long long>(), kBinW512, sms * 4));
-    PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<2048, long long>, CertWarpSmem<2048, long long>(), kBinW1000, sms * 2));
+  if constexpr (kCert) {
+    if (a.narrow) {
+      PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<256, int>, CertWarpSmem<256, int>(), kBinW128, sms * 16));
+      PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<512, int>, CertWarpSmem<512, int>(), kBinW256, sms * 8));
+      PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<1024, int>, CertWarpSmem<1024, int>(), kBinW512, sms * 6));
+      PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<2048, int>, CertWarpSmem<2048, int>(), kBinW1000, sms * 3));
+    } else {
+      PCC_RETURN_IF_ERROR(
+          warp_bin(CertWarpKernel<256, long long>, CertWarpSmem<256, long long>(), kBinW128, sms * 16));
+      PCC_RETURN_IF_ERROR(
+          warp_bin(CertWarpKernel<512, long long>, CertWarpSmem<512, long long>(), kBinW256, sms * 8));
+      PCC_RETURN_IF_ERROR(
+          warp_bin(CertWarpKernel<1024, long long>, CertWarpSmem<1024, long long>(), kBinW512, sms * 4));
+      PCC_RETURN_IF_ERROR(
+          warp_bin(CertWarpKernel<2048, long long>, CertWarpSmem<2048, long long>(), kBinW1000, sms * 2));
+    }
   } else {
     PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<256, kInt, kAsync>, WarpKernelSmem<256>(), kBinW128, sms * 16));
     PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<512, kInt, kAsync>, WarpKernelSmem<512>(), kBinW256, sms * 8));
