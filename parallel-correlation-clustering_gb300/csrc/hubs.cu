@@ -45,6 +45,28 @@ struct HubArgs {
   double* part_val;
   uint32_t* part_id;
   uint32_t* done;
+  // Global path (sync): tables, accumulators, plan (num_glob 0: none).
+  uint32_t num_glob;
+  uint32_t num_glob_items;
+  const uint32_t* glob_hub;
+  const unsigned long long* glob_base;
+  const uint32_t* glob_cap;
+  const uint32_t* glob_item;
+  const uint32_t* glob_item_start;
+  const uint32_t* big_glob;
+  uint32_t* gkeys;
+  unsigned long long* gvals;
+  long long* gt_int;
+  double* gt_dbl;
+  long long* gsmax;
+  uint32_t num_glob_slices;
+  const uint32_t* glob_nslices;
+  const uint32_t* glob_sbase;
+  const uint32_t* slice_hub;
+  const uint32_t* slice_start;
+  double* gpart_val;
+  uint32_t* gpart_id;
+  uint32_t* gdone;
 };
 
 // MurmurHash3's 32-bit finalizer (a bijection; every output bit depends on
@@ -556,6 +578,7 @@ __global__ void __launch_bounds__(kBigThreads) HubBigKernel(HubArgs h) {
     const uint32_t hb = h.item_hub[item];
     const uint32_t p = h.item_part[item];
     const uint32_t v = h.big_v[hb];
+    if (!kAsync && h.num_glob && h.big_glob[hb] != kNone) continue;  // global path
     if (!InFront(a, v)) continue;  // uniform over the CTA
     const VertexCtx x = LoadVertex<kAsync>(a, v);
     const uint32_t P = h.big_parts[hb];
@@ -634,6 +657,166 @@ __global__ void __launch_bounds__(kBigThreads) HubBigKernel(HubArgs h) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Global path: rows of the largest hubs split over many CTAs.
+// ---------------------------------------------------------------------------
+constexpr int kGlobThreads = 256;
+constexpr uint32_t kGlobChunk = 1024;  // row entries per work item (one pass of the CTA)
+
+// Accumulates row chunks into the hubs' HBM tables (warp-aggregated inserts
+// and adds), the together-sum and (INT) the largest running sum.
+template <bool kInt, typename V>
+__global__ void __launch_bounds__(kGlobThreads) HubGlobalAccumKernel(HubArgs h) {
+  constexpr int BT = kGlobThreads;
+  __shared__ HubShared<BT> sh;
+  const BMArgs& a = h.a;
+  const unsigned tid = threadIdx.x, lane = LaneId();
+  for (uint32_t item = blockIdx.x; item < h.num_glob_items; item += gridDim.x) {
+    const uint32_t gi = h.glob_item[item];
+    const uint32_t v = h.big_v[h.glob_hub[gi]];
+    if (!InFront(a, v)) continue;  // uniform over the CTA
+    const VertexCtx x = LoadVertex<false>(a, v);
+    const uint32_t e_begin = h.glob_item_start[item];
+    const uint32_t e_end = min(x.d, e_begin + kGlobChunk);
+    uint32_t* keys = h.gkeys + h.glob_base[gi];
+    V* vals = reinterpret_cast<V*>(h.gvals) + h.glob_base[gi];
+    const uint32_t cap = h.glob_cap[gi];
+    long long t_int = 0, smax = LLONG_MIN;
+    double t_dbl = 0.0;
+    for (uint32_t e0 = e_begin; e0 < e_end; e0 += BT * kHubUnroll) {
+      uint32_t uu[kHubUnroll], cc[kHubUnroll];
+      float ww[kHubUnroll];
+#pragma unroll
+      for (int k = 0; k < kHubUnroll; ++k) {
+        const uint32_t e = e0 + k * BT + tid;
+        uu[k] = v;
+        ww[k] = 0.f;
+        if (e < e_end) {
+          uu[k] = a.nbr[x.b + e];
+          ww[k] = a.w ? a.w[x.b + e] : 1.0f;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kHubUnroll; ++k) cc[k] = uu[k] != v ? __ldg(a.C + uu[k]) : kNone;
+#pragma unroll
+      for (int k = 0; k < kHubUnroll; ++k) {
+        if (e0 + k * BT >= e_end) break;  // uniform over the CTA
+        const bool cand = uu[k] != v;
+        const uint32_t cu = cc[k];
+        int xi = 0;
+        double xd = 0.0;
+        if (cand) EntryWeight<kInt>(a, ww[k], &xi, &xd);
+        if (cand && cu == x.c) {
+          if (kInt)
+            t_int += xi;
+          else
+            t_dbl = Dadd(t_dbl, xd);
+        }
+        const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane));
+        const bool leader = cand && int(lane) == __ffs(peers) - 1;
+        int Si = 0;
+        double Sd = 0.0;
+        GroupWeights<BT, kInt>(a, peers, leader, xi, xd, sh, &Si, &Sd);
+        if (leader) {
+          bool ins;
+          const uint32_t slot = HubInsert(keys, cap, SlotHash(cu), cu, &ins);
+          if (slot == kNone) {
+            atomicExch(&a.ctr->error, kErrHashFull);  // cannot happen: 2 * degree + 2 slots
+          } else if (kInt) {
+            const V old = AtomicAddV<V>(vals + slot, static_cast<V>(Si));
+            smax = max(smax, static_cast<long long>(old) + Si);
+          } else {
+            AtomicAddV<V>(vals + slot, static_cast<V>(Sd));
+          }
+        }
+      }
+    }
+    if (kInt) {
+      const long long t = BlockSum<BT, long long>(t_int, sh.red_ll);
+      const long long mx = BlockMaxLL<BT>(smax, sh.red_ll);
+      if (tid == 0) {
+        if (t) atomicAdd(reinterpret_cast<unsigned long long*>(h.gt_int + gi), static_cast<unsigned long long>(t));
+        atomicMax(h.gsmax + gi, mx);
+      }
+    } else {
+      const double t = BlockSum<BT, double>(t_dbl, sh.red_d);
+      if (tid == 0 && t != 0.0) atomicAdd(h.gt_dbl + gi, t);
+    }
+  }
+}
+
+// Evaluates the HBM tables of the frontier hubs, one slice per CTA (the
+// small-hub evaluation of the slice's keys: FP32 pre-filter, certified leading
+// class, FP64 survivors), clearing the slots (EvalTable).  The hub's last CTA
+// combines the slices' (value, id) bests, decides and resets the hub's
+// accumulators.
+template <bool kInt, typename V>
+__global__ void __launch_bounds__(kBigThreads) HubGlobalEvalKernel(HubArgs h) {
+  constexpr int BT = kBigThreads;
+  __shared__ HubShared<BT> sh;
+  const BMArgs& a = h.a;
+  const unsigned tid = threadIdx.x;
+  unsigned long long fam_e = 0, fam_v = 0;
+  for (uint32_t item = blockIdx.x; item < h.num_glob_slices; item += gridDim.x) {
+    const uint32_t gi = h.slice_hub[item];
+    const uint32_t v = h.big_v[h.glob_hub[gi]];
+    if (!InFront(a, v)) continue;  // uniform over the CTA
+    const VertexCtx x = LoadVertex<false>(a, v);
+    const uint32_t s0 = h.slice_start[item];
+    const uint32_t len = min(kHubGlobalSlice, h.glob_cap[gi] - s0);
+    const long long smax = __ldcg(h.gsmax + gi);
+    if (tid == 0) {
+      if (s0 == 0) {
+        fam_e += x.d;
+        fam_v += 1;
+      }
+      const double T = kInt ? static_cast<double>(__ldcg(h.gt_int + gi)) : __ldcg(h.gt_dbl + gi);
+      sh.change = ChangeOf(a, x, T);
+      sh.change32 = static_cast<float>(sh.change);
+    }
+    __syncthreads();
+    const double change = sh.change;
+    double bv;
+    uint32_t bi;
+    const unsigned long long base = h.glob_base[gi] + s0;
+    EvalTable<BT, kInt, false, V>(a, x, a.kf[v], change, smax, h.gkeys + base, reinterpret_cast<V*>(h.gvals) + base,
+                                  len, sh, &bv, &bi);
+    if (tid == 0) {
+      const uint32_t sb = h.glob_sbase[gi];
+      const uint32_t ns = h.glob_nslices[gi];
+      h.gpart_val[sb + s0 / kHubGlobalSlice] = bv;
+      h.gpart_id[sb + s0 / kHubGlobalSlice] = bi;
+      __threadfence();
+      if (atomicAdd(&h.gdone[gi], 1u) == ns - 1) {
+        __threadfence();
+        double cv = 0.0;
+        uint32_t ci = kNone;
+        for (uint32_t j = 0; j < ns; ++j) KeepBest(cv, ci, __ldcg(h.gpart_val + sb + j), __ldcg(h.gpart_id + sb + j));
+        HubDecide<false>(a, x, cv, ci, change);
+        h.gdone[gi] = 0;
+        h.gt_int[gi] = 0;
+        h.gt_dbl[gi] = 0.0;
+        h.gsmax[gi] = LLONG_MIN;
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0 && fam_v) {
+    atomicAdd(&a.ctr->fam_entries[kFamHubBig], fam_e);
+    atomicAdd(&a.ctr->fam_vertices[kFamHubBig], fam_v);
+  }
+}
+
+__global__ void GlobalStateInitKernel(uint32_t num, long long* gt_int, double* gt_dbl, long long* gsmax,
+                                      uint32_t* gdone) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < num; i += gridDim.x * blockDim.x) {
+    gt_int[i] = 0;
+    gt_dbl[i] = 0.0;
+    gsmax[i] = LLONG_MIN;
+    gdone[i] = 0;
+  }
+}
+
 __global__ void HubDegreesKernel(const uint32_t* list, uint32_t count, const uint64_t* off, uint32_t* deg) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
     deg[i] = static_cast<uint32_t>(off[list[i] + 1] - off[list[i]]);
@@ -691,7 +874,15 @@ Status LaunchHubT(Context* ctx, const HubArgs& h, uint32_t num_small, uint32_t n
     }
     FamEnd(ctx, kFamHubSmall, nl);
   }
+  const bool glob = !kAsync && h.num_glob;
   if (h.num_items) {
+    FamBegin(ctx, kFamHubBig);
+    if (glob) {
+      HubGlobalAccumKernel<kInt, V><<<std::min<unsigned>(h.num_glob_items, sms * 8), kGlobThreads, 0,
+                                      ctx->stream>>>(h);
+      PCC_COUNT(1);
+    }
+    FamEnd(ctx, kFamHubBig, glob ? 1 : 0);
     constexpr size_t smem = size_t(BigSlots<V>()) * (sizeof(V) + sizeof(uint32_t));
     auto k = HubBigKernel<kInt, kAsync, V>;
     const int per_sm = PrepareOnce(k, kBigThreads, smem);
@@ -701,6 +892,13 @@ Status LaunchHubT(Context* ctx, const HubArgs& h, uint32_t num_small, uint32_t n
     k<<<grid, kBigThreads, smem, ctx->stream>>>(h);
     FamEnd(ctx, kFamHubBig, 1);
     PCC_COUNT(1);
+    if (glob) {
+      FamBegin(ctx, kFamHubBig);
+      HubGlobalEvalKernel<kInt, V><<<std::min<unsigned>(h.num_glob_slices, 2 * sms), kBigThreads, 0,
+                                     ctx->stream>>>(h);
+      FamEnd(ctx, kFamHubBig, 1);
+      PCC_COUNT(1);
+    }
   }
   return LaunchCheck();
 }
@@ -730,6 +928,9 @@ Status BuildHubPlan(Context* ctx, const DevGraph& g, const BinSet& bins, HubPlan
   std::iota(order.begin(), order.end(), 0u);
   std::stable_sort(order.begin(), order.end(), [&](uint32_t i, uint32_t j) { return hd[i] > hd[j]; });
   std::vector<uint32_t> small_v, big_v, parts, pbase, item_hub, item_part;
+  std::vector<uint32_t> big_glob, glob_hub, glob_cap, glob_item, glob_item_start;
+  std::vector<uint32_t> glob_nslices, glob_sbase, slice_hub, slice_start;
+  std::vector<unsigned long long> glob_base;
   uint64_t total = 0;
   for (uint32_t r = 0; r < count; ++r) {
     const uint32_t i = order[r];
@@ -741,6 +942,27 @@ Status BuildHubPlan(Context* ctx, const DevGraph& g, const BinSet& bins, HubPlan
     const uint32_t P = std::max<uint32_t>(1, (hd[i] + kHubBigKeys - 1) / kHubBigKeys);
     const uint32_t hb = static_cast<uint32_t>(big_v.size());
     big_v.push_back(hv[i]);
+    if (P >= kHubGlobalParts) {
+      const uint32_t gi = static_cast<uint32_t>(glob_hub.size());
+      big_glob.push_back(gi);
+      glob_hub.push_back(hb);
+      glob_base.push_back(plan->glob_slots);
+      const uint32_t gcap = 2 * hd[i] + 2;
+      glob_cap.push_back(gcap);
+      plan->glob_slots += gcap;
+      glob_sbase.push_back(static_cast<uint32_t>(slice_hub.size()));
+      glob_nslices.push_back((gcap + kHubGlobalSlice - 1) / kHubGlobalSlice);
+      for (uint32_t s0 = 0; s0 < gcap; s0 += kHubGlobalSlice) {
+        slice_hub.push_back(gi);
+        slice_start.push_back(s0);
+      }
+      for (uint32_t e = 0; e < hd[i]; e += kGlobChunk) {
+        glob_item.push_back(gi);
+        glob_item_start.push_back(e);
+      }
+    } else {
+      big_glob.push_back(kNone);
+    }
     parts.push_back(P);
     pbase.push_back(static_cast<uint32_t>(total));
     total += P;
@@ -765,6 +987,22 @@ Status BuildHubPlan(Context* ctx, const DevGraph& g, const BinSet& bins, HubPlan
   PCC_RETURN_IF_ERROR(up(plan->big_pbase, pbase));
   PCC_RETURN_IF_ERROR(up(plan->item_hub, item_hub));
   PCC_RETURN_IF_ERROR(up(plan->item_part, item_part));
+  plan->num_glob = static_cast<uint32_t>(glob_hub.size());
+  plan->num_glob_items = static_cast<uint32_t>(glob_item.size());
+  if (plan->num_glob) {
+    PCC_RETURN_IF_ERROR(up(plan->big_glob, big_glob));
+    PCC_RETURN_IF_ERROR(up(plan->glob_hub, glob_hub));
+    PCC_RETURN_IF_ERROR(up(plan->glob_cap, glob_cap));
+    PCC_RETURN_IF_ERROR(up(plan->glob_item, glob_item));
+    PCC_RETURN_IF_ERROR(up(plan->glob_item_start, glob_item_start));
+    plan->num_glob_slices = static_cast<uint32_t>(slice_hub.size());
+    PCC_RETURN_IF_ERROR(up(plan->glob_nslices, glob_nslices));
+    PCC_RETURN_IF_ERROR(up(plan->glob_sbase, glob_sbase));
+    PCC_RETURN_IF_ERROR(up(plan->slice_hub, slice_hub));
+    PCC_RETURN_IF_ERROR(up(plan->slice_start, slice_start));
+    PCC_RETURN_IF_ERROR(plan->glob_base.Alloc(ctx, glob_base.size()));
+    PCC_RETURN_IF_ERROR(plan->glob_base.FromHost(glob_base.data(), glob_base.size()));
+  }
   return Sync(ctx);  // host vectors go out of scope
 }
 
@@ -776,6 +1014,29 @@ Status AllocHubState(Context* ctx, const HubPlan& plan, HubState* st) {
   }
   const uint64_t nh = std::max<uint32_t>(plan.num_big, 1);
   if (st->done.count < nh) PCC_RETURN_IF_ERROR(st->done.Alloc(ctx, nh));
+  if (plan.num_glob) {
+    // The rounds leave the tables clean; they are reset here all the same,
+    // at every level, so that a run cut short cannot leave keys behind.
+    if (st->gkeys.count < plan.glob_slots) {
+      PCC_RETURN_IF_ERROR(st->gkeys.Alloc(ctx, plan.glob_slots));
+      PCC_RETURN_IF_ERROR(st->gvals.Alloc(ctx, plan.glob_slots));
+    }
+    if (st->gt_int.count < plan.num_glob) {
+      PCC_RETURN_IF_ERROR(st->gt_int.Alloc(ctx, plan.num_glob));
+      PCC_RETURN_IF_ERROR(st->gt_dbl.Alloc(ctx, plan.num_glob));
+      PCC_RETURN_IF_ERROR(st->gsmax.Alloc(ctx, plan.num_glob));
+      PCC_RETURN_IF_ERROR(st->gdone.Alloc(ctx, plan.num_glob));
+    }
+    if (st->gpart_val.count < plan.num_glob_slices) {
+      PCC_RETURN_IF_ERROR(st->gpart_val.Alloc(ctx, plan.num_glob_slices));
+      PCC_RETURN_IF_ERROR(st->gpart_id.Alloc(ctx, plan.num_glob_slices));
+    }
+    PCC_CUDA(cudaMemsetAsync(st->gkeys.p, 0xFF, plan.glob_slots * sizeof(uint32_t), ctx->stream));  // kNone
+    PCC_CUDA(cudaMemsetAsync(st->gvals.p, 0, plan.glob_slots * sizeof(unsigned long long), ctx->stream));
+    GlobalStateInitKernel<<<Blocks(plan.num_glob, 256, 1024), 256, 0, ctx->stream>>>(
+        plan.num_glob, st->gt_int.p, st->gt_dbl.p, st->gsmax.p, st->gdone.p);
+    PCC_COUNT(1);
+  }
   return st->done.Zero();
 }
 
@@ -822,6 +1083,27 @@ Status LaunchHubBestMoves(Context* ctx, const BMArgs& a, const HubPlan& plan, Hu
   h.part_val = st.part_val.p;
   h.part_id = st.part_id.p;
   h.done = st.done.p;
+  h.num_glob = plan.num_glob;
+  h.num_glob_items = plan.num_glob_items;
+  h.glob_hub = plan.glob_hub.p;
+  h.glob_base = plan.glob_base.p;
+  h.glob_cap = plan.glob_cap.p;
+  h.glob_item = plan.glob_item.p;
+  h.glob_item_start = plan.glob_item_start.p;
+  h.big_glob = plan.big_glob.p;
+  h.gkeys = st.gkeys.p;
+  h.gvals = st.gvals.p;
+  h.gt_int = st.gt_int.p;
+  h.gt_dbl = st.gt_dbl.p;
+  h.gsmax = st.gsmax.p;
+  h.num_glob_slices = plan.num_glob_slices;
+  h.glob_nslices = plan.glob_nslices.p;
+  h.glob_sbase = plan.glob_sbase.p;
+  h.slice_hub = plan.slice_hub.p;
+  h.slice_start = plan.slice_start.p;
+  h.gpart_val = st.gpart_val.p;
+  h.gpart_id = st.gpart_id.p;
+  h.gdone = st.gdone.p;
   if (a.async) {
     if (!int_mode) return LaunchHubT<false, true, double>(ctx, h, plan.num_small, plan.num_small_wide);
     return narrow ? LaunchHubT<true, true, int>(ctx, h, plan.num_small, plan.num_small_wide) : LaunchHubT<true, true, long long>(ctx, h, plan.num_small, plan.num_small_wide);

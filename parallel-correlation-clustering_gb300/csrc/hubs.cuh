@@ -29,6 +29,8 @@ namespace pcc {
 constexpr uint32_t kHubMinDegree = 1000;  // hub = degree > 1000
 constexpr uint32_t kHubSmallMax = 4096;   // one-partition hubs
 constexpr uint32_t kHubBigKeys = 12288;   // expected distinct keys per big-hub partition
+constexpr uint32_t kHubGlobalParts = 4;    // big hubs with >= this many partitions take the global path
+constexpr uint32_t kHubGlobalSlice = 2048;   // table slots evaluated by one CTA
 
 // Static part (depends on the graph only).
 struct HubPlan {
@@ -44,6 +46,26 @@ struct HubPlan {
   DBuf<uint32_t> big_pbase;    // first partial of the big hub
   DBuf<uint32_t> item_hub;     // work items, largest hubs first
   DBuf<uint32_t> item_part;
+  // Big hubs with at least kHubGlobalParts partitions, synchronous rounds:
+  // many CTAs accumulate a row's chunks into one per-hub table in HBM, then
+  // one CTA per hub evaluates it (a row of millions of entries would
+  // otherwise keep a few CTAs busy while the rest of the GPU idles).
+  uint32_t num_glob = 0;
+  uint32_t num_glob_items = 0;
+  uint64_t glob_slots = 0;
+  DBuf<uint32_t> glob_hub;               // per global hub: its big-hub index
+  DBuf<unsigned long long> glob_base;    // first table slot
+  DBuf<uint32_t> glob_cap;               // table slots (2 * degree + 2: never full)
+  DBuf<uint32_t> glob_item;              // per work item: global hub index
+  DBuf<uint32_t> glob_item_start;        // first entry of the item's chunk
+  DBuf<uint32_t> big_glob;               // per big hub: global hub index or kNone
+  // Evaluation: the table is split into slices of kHubGlobalSlice slots, one
+  // CTA each; the hub's last CTA combines the slices' bests.
+  uint32_t num_glob_slices = 0;
+  DBuf<uint32_t> glob_nslices;           // per global hub
+  DBuf<uint32_t> glob_sbase;             // per global hub: first partial
+  DBuf<uint32_t> slice_hub;              // per slice: global hub index
+  DBuf<uint32_t> slice_start;            // per slice: first slot (within the hub's table)
 };
 
 // Per-context mutable state; counters are zero between rounds.
@@ -51,6 +73,16 @@ struct HubState {
   DBuf<double> part_val;
   DBuf<uint32_t> part_id;
   DBuf<uint32_t> done;
+  // Global-path tables (keys kNone / values 0 between rounds) and per-hub
+  // accumulators (reset by the evaluating CTA).
+  DBuf<uint32_t> gkeys;
+  DBuf<unsigned long long> gvals;
+  DBuf<long long> gt_int;
+  DBuf<double> gt_dbl;
+  DBuf<long long> gsmax;
+  DBuf<double> gpart_val;                // per slice: best (value, id)
+  DBuf<uint32_t> gpart_id;
+  DBuf<uint32_t> gdone;                  // per global hub: slices evaluated (0 between rounds)
 };
 
 Status BuildHubPlan(Context* ctx, const DevGraph& g, const BinSet& bins, HubPlan* plan);

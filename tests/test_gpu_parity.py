@@ -37,6 +37,16 @@ def _graphs():
     s, d = src[keep], gi.neighbors[keep].astype(np.int64)
     w = rng.integers(1, 6, size=s.size).astype(np.float32)
     out["sbm3k_int"] = P.CsrGraph.from_edges(gi.n, s, d, w)   # integer weights -> INT mode
+    # Two hubs of degree 100k and 60k on an SBM: 9 and 5 partitions, the
+    # global path (rows spread over many CTAs, per-hub HBM tables).
+    hb, _ = G.sbm(120000, 100, 0.004, 0.00002, 17)
+    src = np.repeat(np.arange(hb.n), np.diff(hb.offsets).astype(np.int64))
+    keep = src < hb.neighbors
+    s = np.concatenate([src[keep], np.zeros(100000, np.int64), np.ones(60000, np.int64)])
+    d = np.concatenate([hb.neighbors[keep].astype(np.int64), np.arange(1, 100001), np.arange(50000, 110000)])
+    out["hubs100k"] = P.CsrGraph.from_edges(hb.n, s, d)
+    wr = rng.uniform(0.5, 1.5, size=s.size).astype(np.float32)
+    out["hubs100k_real"] = P.CsrGraph.from_edges(hb.n, s, d, wr)
     return out
 
 
@@ -49,7 +59,7 @@ def _both(ctx, g):
     return ctx.upload(g), O.OracleGraph(g)
 
 
-@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "rmat16", "sbm3k_int", "lfr20k_real"])
+@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "rmat16", "sbm3k_int", "lfr20k_real", "hubs100k"])
 @pytest.mark.parametrize("nclusters_div", [1, 7, 300])
 def test_best_moves_replay(ctx, graphs, name, nclusters_div):
     """One sync best-move pass from a random state: GPU == oracle."""
@@ -104,7 +114,7 @@ CONFIGS = [
 ]
 
 
-@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "sbm3k_int"])
+@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "sbm3k_int", "hubs100k"])
 @pytest.mark.parametrize("ci", range(len(CONFIGS)))
 def test_correlation_cluster_bit_exact(ctx, graphs, name, ci):
     g = graphs[name]
@@ -120,7 +130,7 @@ def test_correlation_cluster_bit_exact(ctx, graphs, name, ci):
     assert st_g["objective"] == pytest.approx(st_o["objective"], rel=REL_TOL, abs=1e-9)
 
 
-@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "rmat16"])
+@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "rmat16", "hubs100k"])
 @pytest.mark.parametrize("move", [P.NBHR_MOVE, P.ALL_MOVE])
 def test_modularity_cluster_bit_exact(ctx, graphs, name, move):
     g = graphs[name]
@@ -134,9 +144,10 @@ def test_modularity_cluster_bit_exact(ctx, graphs, name, move):
     assert st_g["objective"] == pytest.approx(st_o["objective"], rel=REL_TOL, abs=1e-12)
 
 
-def test_real_weights_full_run(ctx, graphs):
+@pytest.mark.parametrize("name", ["lfr20k_real", "hubs100k_real"])
+def test_real_weights_full_run(ctx, graphs, name):
     """FP64 mode end to end: objective within 1e-9 relative of the oracle."""
-    g = graphs["lfr20k_real"]
+    g = graphs[name]
     dg, og = _both(ctx, g)
     cfg = P.make_config(resolution=0.1, refine=True, move_method=P.NBHR_CLUSTER_MOVE)
     lab_g, st_g = P.correlation_cluster(dg, cfg)
