@@ -218,6 +218,13 @@ struct BMArgs {
   double* K_mut;
   uint32_t* C_mut;
   uint32_t* moved_cluster_stamp;
+  // async mode: ids of empty clusters (at the start of the level, then as
+  // clusters empty), offered to vertices that found a new cluster
+  // (free_ctr[0] = pushed, [1] = taken; slots hold kNone until published
+  // and after being taken)
+  uint32_t* free_ids;
+  uint32_t* free_ctr;
+  uint32_t free_cap;
   // non-null: stamp and frontier come from here (front_stamp is the array)
   const RoundState* rs;
   // non-null: per-vertex resolution (graphs of a union with their own

@@ -223,6 +223,10 @@ struct ZeroSizeInput {
   const DevCounters* ctr;
   __device__ uint32_t operator()(uint64_t i) const { return ctr->new_movers && s[i] == 0u ? 1u : 0u; }
 };
+struct EmptyClusterInput {
+  const uint32_t* s;
+  __device__ uint32_t operator()(uint64_t i) const { return s[i] == 0u ? 1u : 0u; }
+};
 struct NewMoverInput {
   const uint32_t* st;
   uint32_t stamp;
@@ -604,6 +608,10 @@ class Engine {
     PCC_RETURN_IF_ERROR(zero_ids_.Alloc(ctx_, nn));
     PCC_RETURN_IF_ERROR(new_list_.Alloc(ctx_, nn));
 
+    if (cfg_.async) {
+      PCC_RETURN_IF_ERROR(free_ids_.Alloc(ctx_, nn));
+      PCC_RETURN_IF_ERROR(free_ctr_.Alloc(ctx_, 2));
+    }
     PCC_RETURN_IF_ERROR(ctr_.Alloc(ctx_, 1));
     PCC_RETURN_IF_ERROR(ctr_.Zero());
     PCC_RETURN_IF_ERROR(rs_.Alloc(ctx_, 1));
@@ -611,6 +619,16 @@ class Engine {
     PCC_RETURN_IF_ERROR(scan_tiles_.Reserve(ctx_, (nn + kScanTile - 1) / kScanTile + 1));
     (void)max_deg;
     return Status::Ok();
+  }
+
+  // Async mode: the free-id list of a level (or refinement pass) starts as
+  // the ids of its empty clusters (none from singletons).
+  Status SeedFreeIds(uint32_t n, const uint32_t* s) {
+    if (!cfg_.async || n == 0) return Status::Ok();
+    PCC_CUDA(cudaMemsetAsync(free_ids_.p, 0xFF, sizeof(uint32_t) * n, ctx_->stream));
+    PCC_RETURN_IF_ERROR(free_ctr_.Zero());
+    return ScanApply<uint32_t>(ctx_, n, EmptyClusterInput{s}, StoreIndexIfSet{free_ids_.p}, scan_tiles_,
+                               free_ctr_.p);
   }
 
   // Builds level state over graph g: singletons with node weights k (device,
@@ -647,6 +665,7 @@ class Engine {
       PCC_RETURN_IF_ERROR(LaunchCheck());
     }
     L->int_mode = IntModeFor(*g, cfg_.edge_weight_offset);
+    PCC_RETURN_IF_ERROR(SeedFreeIds(n, L->s.p));
     if (un_ && un_->d_res.p && n) {
       PCC_RETURN_IF_ERROR(L->vres.Alloc(ctx_, n));
       PCC_RETURN_IF_ERROR(L->vres32.Alloc(ctx_, n));
@@ -706,6 +725,11 @@ class Engine {
     a.K_mut = L->K.p;
     a.C_mut = L->C.p;
     a.moved_cluster_stamp = mod_stamp_.p;
+    if (cfg_.async) {
+      a.free_ids = free_ids_.p;
+      a.free_ctr = free_ctr_.p;
+      a.free_cap = n;
+    }
     a.rs = rs;
     a.vres = L->vres.p;
     a.vres32 = L->vres32.p;
@@ -1030,6 +1054,7 @@ class Engine {
           RefreshKfKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->K.p, Li->Kf.p, nullptr, 0, nullptr);
           PCC_COUNT(1);
           PCC_RETURN_IF_ERROR(LaunchCheck());
+          PCC_RETURN_IF_ERROR(SeedFreeIds(ni, Li->s.p));
         }
         bool moved = false;
         PCC_RETURN_IF_ERROR(Iterate(Li, num_inner, &moved));
@@ -1329,6 +1354,7 @@ class Engine {
   uint32_t stamp_ = 0;
   DBuf<uint32_t> moves_, movers_, moved_stamp_, mod_stamp_, next_stamp_, new_stamp_, aux_stamp_;
   DBuf<uint32_t> zero_ids_, new_list_;
+  DBuf<uint32_t> free_ids_, free_ctr_;  // async: ids of clusters emptied during the level
   DBuf<uint32_t> scan_tiles_;
   HubState hub_state_;
   DBuf<DevCounters> ctr_;

@@ -152,19 +152,44 @@ __device__ __forceinline__ bool Decide(const BMArgs& a, const VertexCtx& x, doub
     // AsyncMove (internal.cc:371-403): apply immediately.
     if (!(value > 0)) return false;
     const uint32_t cur = x.c;
-    atomicSub(&a.s_mut[cur], 1u);
+    const uint32_t left = atomicSub(&a.s_mut[cur], 1u);
     atomicAdd(&a.K_mut[cur], -1 * x.kv);
+    if (left == 1u && a.free_ids) {  // cur emptied: offer its id to new clusters
+      const uint32_t pos = atomicAdd(&a.free_ctr[0], 1u);
+      if (pos < a.free_cap) atomicExch(&a.free_ids[pos], cur);
+    }
     uint32_t dest = target;
     if (target != a.n) {
       atomicAdd(&a.s_mut[target], 1u);
       atomicAdd(&a.K_mut[target], x.kv);
     } else {
-      // Claim an empty id by CAS, probing linearly from the vertex's own id.
-      // Bounded: after 4n probes the kernel records an error and leaves the
-      // vertex where it was (its leave is undone).
+      // Claim an empty id by CAS.  The reference probes linearly from the
+      // vertex's own id (internal.cc:390-401); any empty id gives the same
+      // clustering up to renaming, and on graphs with long runs of occupied
+      // ids (isolated vertices of RMAT) that probe can walk a million ids
+      // while the rest of the kernel waits on one thread.  So the ids empty
+      // at the start of the level and those of clusters emptied during it
+      // are tried first (a taken or re-occupied one fails the CAS), then the
+      // linear probe.  Bounded:
+      // after 4n probes the kernel records an error and leaves the vertex
+      // where it was (its leave is undone).
       uint64_t i = x.v;
-      const uint64_t limit = 4ull * a.n + 64;
       bool got = false;
+      if (a.free_ids) {
+        for (int t = 0; t < 16; ++t) {
+          const uint32_t pushed = min(__ldcg(&a.free_ctr[0]), a.free_cap);
+          if (__ldcg(&a.free_ctr[1]) >= pushed) break;
+          const uint32_t pos = atomicAdd(&a.free_ctr[1], 1u);
+          if (pos >= pushed) break;
+          const uint32_t id = atomicExch(&a.free_ids[pos], kNone);
+          if (id != kNone && atomicCAS(&a.s_mut[id], 0u, 1u) == 0u) {
+            i = id;
+            got = true;
+            break;
+          }
+        }
+      }
+      const uint64_t limit = got ? 0 : 4ull * a.n + 64;
       for (uint64_t p = 0; p < limit; ++p) {
         if (__ldcg(&a.s_mut[i]) == 0u && atomicCAS(&a.s_mut[i], 0u, 1u) == 0u) {
           got = true;
