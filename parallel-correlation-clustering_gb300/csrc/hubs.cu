@@ -21,6 +21,7 @@ namespace {
 constexpr int kHubUnroll = 4;              // entries per thread in flight
 constexpr uint32_t kHubMaxSub = 1u << 12;  // sub-partitions before giving up
 constexpr uint32_t kMaxCont = 256;         // contender list per CTA
+constexpr int kEvalBatch = 4;              // table slots per thread in flight (EvalTable)
 
 constexpr int kSmallThreads = 256;         // small hubs: CTA size, table slots
 constexpr uint32_t kSmallSlots = 2 * kHubSmallMax;
@@ -125,6 +126,7 @@ struct HubShared {
   uint32_t ncont;
   uint32_t overflow;
   uint32_t nkeys;
+  uint32_t last;  // global path: this CTA evaluated the hub's last slice
   double change;
   float change32;
 };
@@ -333,37 +335,74 @@ __device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double
   constexpr bool kFilter = kInt && !kAsync;
   double lv = 0.0;
   uint32_t lid = kNone;
+  // Slots are read kEvalBatch at a time per thread, so that the gathers of
+  // their cluster weights are in flight together.
+  constexpr int kB = kEvalBatch;
   if (kFilter) {
     const I smax = static_cast<I>(smax_ll);
     const float c32 = sh.change32;
+    const float r32 = Res32Of(a, x.v);
     float U = -CUDART_INF_F;
-    for (uint32_t s = tid; s < cap; s += BT) {
-      const uint32_t key = skeys[s];
-      if (key == kNone) continue;
-      const FilterVal f = FilterOf<I>(Res32Of(a, x.v), k32, a.Kf[key], static_cast<I>(svals[s]), smax, c32);
-      if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
+    for (uint32_t s0 = tid; s0 < cap; s0 += BT * kB) {
+      uint32_t kk[kB];
+      I ss[kB];
+      float kf[kB];
+#pragma unroll
+      for (int j = 0; j < kB; ++j) {
+        const uint32_t s = s0 + j * BT;
+        kk[j] = s < cap ? skeys[s] : kNone;
+        ss[j] = s < cap ? static_cast<I>(svals[s]) : I(0);
+      }
+#pragma unroll
+      for (int j = 0; j < kB; ++j) kf[j] = kk[j] != kNone ? a.Kf[kk[j]] : 0.f;
+#pragma unroll
+      for (int j = 0; j < kB; ++j) {
+        if (kk[j] == kNone) continue;
+        const FilterVal f = FilterOf<I>(r32, k32, kf[j], ss[j], smax, c32);
+        if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
+      }
     }
     if (tid == 0) sh.ncont = 0;
     U = BlockMaxF<BT>(U, sh.red_f);
     LexKeyT<I> lead, tail;
-    for (uint32_t s = tid; s < cap; s += BT) {
-      const uint32_t key = skeys[s];
-      if (key == kNone) continue;
-      const I S = static_cast<I>(svals[s]);
-      skeys[s] = kNone;
-      svals[s] = V(0);
-      const FilterVal f = FilterOf<I>(Res32Of(a, x.v), k32, a.Kf[key], S, smax, c32);
-      if (f.sane && __fadd_rn(f.Y, f.e) < U) continue;
-      const double KD = a.K[key];
-      const unsigned long long ko = KOrder(KD);
-      lead.Keep(S, ko, key);
-      tail.Keep(-S, ~ko, key);
-      const uint32_t pos = atomicAdd(&sh.ncont, 1u);
-      if (pos < kMaxCont) {
-        sh.cont_key[pos] = key;
-        sh.cont_S[pos] = S;
-      } else {
-        KeepBest(lv, lid, ValOf(a, x, change, static_cast<double>(S), KD), key);  // list full: now
+    for (uint32_t s0 = tid; s0 < cap; s0 += BT * kB) {
+      uint32_t kk[kB];
+      I ss[kB];
+      float kf[kB];
+#pragma unroll
+      for (int j = 0; j < kB; ++j) {
+        const uint32_t s = s0 + j * BT;
+        kk[j] = kNone;
+        ss[j] = I(0);
+        if (s < cap) {
+          kk[j] = skeys[s];
+          if (kk[j] != kNone) {
+            ss[j] = static_cast<I>(svals[s]);
+            skeys[s] = kNone;
+            svals[s] = V(0);
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kB; ++j) kf[j] = kk[j] != kNone ? a.Kf[kk[j]] : 0.f;
+#pragma unroll
+      for (int j = 0; j < kB; ++j) {
+        const uint32_t key = kk[j];
+        if (key == kNone) continue;
+        const I S = ss[j];
+        const FilterVal f = FilterOf<I>(r32, k32, kf[j], S, smax, c32);
+        if (f.sane && __fadd_rn(f.Y, f.e) < U) continue;
+        const double KD = a.K[key];
+        const unsigned long long ko = KOrder(KD);
+        lead.Keep(S, ko, key);
+        tail.Keep(-S, ~ko, key);
+        const uint32_t pos = atomicAdd(&sh.ncont, 1u);
+        if (pos < kMaxCont) {
+          sh.cont_key[pos] = key;
+          sh.cont_S[pos] = S;
+        } else {
+          KeepBest(lv, lid, ValOf(a, x, change, static_cast<double>(S), KD), key);  // list full: now
+        }
       }
     }
     bool single;
@@ -387,13 +426,29 @@ __device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double
     if (tid == 0 && lead.id != kNone)
       KeepBest(lv, lid, ValOf(a, x, change, static_cast<double>(lead.S), a.K[lead.id]), lead.id);
   } else {
-    for (uint32_t s = tid; s < cap; s += BT) {
-      const uint32_t key = skeys[s];
-      if (key == kNone) continue;
-      const V sv = svals[s];
-      skeys[s] = kNone;
-      svals[s] = V(0);
-      KeepBest(lv, lid, ValOf(a, x, change, static_cast<double>(sv), LdK<kAsync>(a.K + key)), key);
+    for (uint32_t s0 = tid; s0 < cap; s0 += BT * kB) {
+      uint32_t kk[kB];
+      V sv[kB];
+      double kd[kB];
+#pragma unroll
+      for (int j = 0; j < kB; ++j) {
+        const uint32_t s = s0 + j * BT;
+        kk[j] = kNone;
+        sv[j] = V(0);
+        if (s < cap) {
+          kk[j] = skeys[s];
+          if (kk[j] != kNone) {
+            sv[j] = svals[s];
+            skeys[s] = kNone;
+            svals[s] = V(0);
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kB; ++j) kd[j] = kk[j] != kNone ? LdK<kAsync>(a.K + kk[j]) : 0.0;
+#pragma unroll
+      for (int j = 0; j < kB; ++j)
+        if (kk[j] != kNone) KeepBest(lv, lid, ValOf(a, x, change, static_cast<double>(sv[j]), kd[j]), kk[j]);
     }
   }
   BlockArgmax<BT>(lv, lid, sh.red_k, sh.red_i);
@@ -661,7 +716,7 @@ __global__ void __launch_bounds__(kBigThreads) HubBigKernel(HubArgs h) {
 // Global path: rows of the largest hubs split over many CTAs.
 // ---------------------------------------------------------------------------
 constexpr int kGlobThreads = 256;
-constexpr uint32_t kGlobChunk = 1024;  // row entries per work item (one pass of the CTA)
+constexpr uint32_t kGlobChunk = kGlobThreads;  // row entries per work item: one per thread
 
 // Accumulates row chunks into the hubs' HBM tables (warp-aggregated inserts
 // and adds), the together-sum and (INT) the largest running sum.
@@ -751,8 +806,8 @@ __global__ void __launch_bounds__(kGlobThreads) HubGlobalAccumKernel(HubArgs h) 
 // combines the slices' (value, id) bests, decides and resets the hub's
 // accumulators.
 template <bool kInt, typename V>
-__global__ void __launch_bounds__(kBigThreads) HubGlobalEvalKernel(HubArgs h) {
-  constexpr int BT = kBigThreads;
+__global__ void __launch_bounds__(kGlobThreads) HubGlobalEvalKernel(HubArgs h) {
+  constexpr int BT = kGlobThreads;
   __shared__ HubShared<BT> sh;
   const BMArgs& a = h.a;
   const unsigned tid = threadIdx.x;
@@ -781,17 +836,22 @@ __global__ void __launch_bounds__(kBigThreads) HubGlobalEvalKernel(HubArgs h) {
     const unsigned long long base = h.glob_base[gi] + s0;
     EvalTable<BT, kInt, false, V>(a, x, a.kf[v], change, smax, h.gkeys + base, reinterpret_cast<V*>(h.gvals) + base,
                                   len, sh, &bv, &bi);
+    const uint32_t sb = h.glob_sbase[gi];
+    const uint32_t ns = h.glob_nslices[gi];
     if (tid == 0) {
-      const uint32_t sb = h.glob_sbase[gi];
-      const uint32_t ns = h.glob_nslices[gi];
       h.gpart_val[sb + s0 / kHubGlobalSlice] = bv;
       h.gpart_id[sb + s0 / kHubGlobalSlice] = bi;
       __threadfence();
-      if (atomicAdd(&h.gdone[gi], 1u) == ns - 1) {
-        __threadfence();
-        double cv = 0.0;
-        uint32_t ci = kNone;
-        for (uint32_t j = 0; j < ns; ++j) KeepBest(cv, ci, __ldcg(h.gpart_val + sb + j), __ldcg(h.gpart_id + sb + j));
+      sh.last = atomicAdd(&h.gdone[gi], 1u) == ns - 1 ? 1u : 0u;
+    }
+    __syncthreads();
+    if (sh.last) {  // uniform: the whole CTA combines the slices' bests
+      __threadfence();
+      double cv = 0.0;
+      uint32_t ci = kNone;
+      for (uint32_t j = tid; j < ns; j += BT) KeepBest(cv, ci, __ldcg(h.gpart_val + sb + j), __ldcg(h.gpart_id + sb + j));
+      BlockArgmax<BT>(cv, ci, sh.red_k, sh.red_i);
+      if (tid == 0) {
         HubDecide<false>(a, x, cv, ci, change);
         h.gdone[gi] = 0;
         h.gt_int[gi] = 0;
@@ -894,7 +954,7 @@ Status LaunchHubT(Context* ctx, const HubArgs& h, uint32_t num_small, uint32_t n
     PCC_COUNT(1);
     if (glob) {
       FamBegin(ctx, kFamHubBig);
-      HubGlobalEvalKernel<kInt, V><<<std::min<unsigned>(h.num_glob_slices, 2 * sms), kBigThreads, 0,
+      HubGlobalEvalKernel<kInt, V><<<std::min<unsigned>(h.num_glob_slices, 8 * sms), kGlobThreads, 0,
                                      ctx->stream>>>(h);
       FamEnd(ctx, kFamHubBig, 1);
       PCC_COUNT(1);

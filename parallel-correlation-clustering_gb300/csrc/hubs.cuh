@@ -30,7 +30,7 @@ constexpr uint32_t kHubMinDegree = 1000;  // hub = degree > 1000
 constexpr uint32_t kHubSmallMax = 4096;   // one-partition hubs
 constexpr uint32_t kHubBigKeys = 12288;   // expected distinct keys per big-hub partition
 constexpr uint32_t kHubGlobalParts = 4;    // big hubs with >= this many partitions take the global path
-constexpr uint32_t kHubGlobalSlice = 2048;   // table slots evaluated by one CTA
+constexpr uint32_t kHubGlobalSlice = 1024;   // table slots evaluated by one CTA
 
 // Static part (depends on the graph only).
 struct HubPlan {
