@@ -320,6 +320,7 @@ struct Options {
   double res = 0;
   double offset = 0;
   int move_method = PCC_NBHR_CLUSTER_MOVE;
+  bool whole_clusters = false;  // DEFAULT_CLUSTER_MOVES
   bool async = false;
   bool permute = false;
   uint64_t seed = 0;
@@ -416,6 +417,66 @@ bool AsyncMove(const Graph& g, Helper& h, uint32_t v, const Options& o,
   }
 }
 
+// Whole-cluster moves of one synchronous round: the DEFAULT_CLUSTER_MOVES
+// block of BestMovesForVertexSubset (parallel-correlation-clusterer.cc:
+// 167-297, subclustering NONE), with ClusteringHelper::BestMove(moving_nodes)
+// (internal.cc:644-707) and BestMoveFromStats (correlation-clusterer-util.h:
+// 70-113).  Every cluster (OutputIndicesById groups: members ascending) is a
+// moving set whose members are exactly the vertices of that cluster, so
+// class-2 entries (both ends moving) never cross clusters and class-1 entries
+// never stay inside.  Returns the clusters MoveNodesToCluster modified.
+std::vector<uint8_t> ClusterMoves(const Graph& g, Helper& h, const Options& o,
+                                  uint64_t* moved_count) {
+  const uint32_t n = g.n;
+  const std::vector<std::vector<uint32_t>> groups = GroupsById(h.C);
+  std::vector<uint32_t> moves(n, kNone);
+  const int64_t ng = static_cast<int64_t>(groups.size());
+#pragma omp parallel num_threads(NumThreads())
+  {
+    SumTable after;  // class_1_together_after: cluster -> EdgeSum
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t gi = 0; gi < ng; ++gi) {
+      const std::vector<uint32_t>& members = groups[gi];
+      const uint32_t c = h.C[members[0]];
+      uint64_t deg = 0;
+      for (uint32_t v : members) deg += g.degree(v);
+      after.Reset(deg);
+      double weight = 0;    // moving_nodes_weight
+      double weight_c = 0;  // cluster_moving_weights[c]
+      for (uint32_t v : members) {
+        weight_c += h.k[v];
+        weight += h.k[v];
+        for (uint64_t j = g.off[v]; j < g.off[v + 1]; ++j) {
+          const uint32_t cu = h.C[g.nbr[j]];
+          if (cu == c) continue;  // both ends moving
+          // `float weight; weight -= offset;` then EdgeSum::Add(double).
+          const float wf = static_cast<float>(static_cast<double>(g.weight(j)) - o.offset);
+          after.Add(cu, static_cast<double>(wf));
+        }
+      }
+      auto half_square = [](double x) { return x * x / 2; };
+      double change = 0;
+      change += 0.0 / 2 - o.res * (half_square(weight) - half_square(weight_c));
+      change -= 0.0 - o.res * (weight_c * (h.K[c] - weight_c));
+      uint32_t best = kNone;
+      double best_val = change;
+      for (uint32_t slot : after.used) {
+        const uint32_t d = after.keys[slot];
+        const double val = change + (after.vals[slot] - o.res * (weight * (h.K[d] - 0.0)));
+        if (val > best_val || (val == best_val && best != kNone && d < best)) {
+          best = d;
+          best_val = val;
+        }
+      }
+      const uint32_t target = best != kNone ? best : n;
+      if (target < n && c >= target) best_val = 0;  // only towards a higher id
+      if (best_val > 0)
+        for (uint32_t v : members) moves[v] = target;
+    }
+  }
+  return MoveNodesToCluster(h, moves, moved_count);
+}
+
 // N(marked) via gbbs::edgeMap with the always-true functor
 // (parallel-correlation-clusterer.cc:46-55, 312-331): every neighbour of a
 // marked vertex, as an ascending list.
@@ -441,8 +502,9 @@ std::vector<uint32_t> AllVertices(uint32_t n) {
   return out;
 }
 
-// BestMovesForVertexSubset (parallel-correlation-clusterer.cc:115-338),
-// LOUVAIN vertex moves only.  Returns the next frontier.
+// BestMovesForVertexSubset (parallel-correlation-clusterer.cc:115-338):
+// vertex moves, then (DEFAULT_CLUSTER_MOVES, synchronous) whole-cluster
+// moves.  Returns the next frontier.
 std::vector<uint32_t> BestMovesForVertexSubset(const Graph& g, Helper& h,
                                                const std::vector<uint32_t>& frontier,
                                                Options& o, Counters& ctr) {
@@ -504,6 +566,10 @@ std::vector<uint32_t> BestMovesForVertexSubset(const Graph& g, Helper& h,
       }
     }
     moved_clusters = MoveNodesToCluster(h, moves, &ctr.moves);
+    if (o.whole_clusters) {
+      const std::vector<uint8_t> extra = ClusterMoves(g, h, o, &ctr.moves);
+      for (uint32_t i = 0; i < n; ++i) moved_clusters[i] |= extra[i];
+    }
   }
 
   if (o.move_method == PCC_ALL_MOVE) return AllVertices(n);
@@ -684,7 +750,11 @@ int RefineClustersSubroutine(const Graph& graph, const pcc_config& cfg,
     num_iterations = cfg.louvain_num_iterations > 0 ? cfg.louvain_num_iterations : 10;
     num_inner = cfg.louvain_num_inner_iterations > 0 ? cfg.louvain_num_inner_iterations : 10;
   } else if (cfg.clustering_moves_method == PCC_DEFAULT_CLUSTER_MOVES) {
-    return PCC_UNIMPLEMENTED;  // whole-cluster moves are not restated yet
+    // One level of up to num_iterations rounds (:487-492).  The async
+    // variant (AsyncMove(moving_nodes), internal.cc:405-446) is not restated.
+    if (cfg.async) return PCC_UNIMPLEMENTED;
+    num_iterations = 1;
+    num_inner = cfg.num_iterations > 0 ? cfg.num_iterations : 20;
   } else {
     return PCC_UNIMPLEMENTED;
   }
@@ -694,6 +764,7 @@ int RefineClustersSubroutine(const Graph& graph, const pcc_config& cfg,
   o.res = cfg.resolution;
   o.offset = cfg.edge_weight_offset;
   o.move_method = cfg.move_method;
+  o.whole_clusters = cfg.clustering_moves_method == PCC_DEFAULT_CLUSTER_MOVES;
   o.async = cfg.async != 0;
   o.permute = cfg.permute != 0;
   o.seed = cfg.random_seed;

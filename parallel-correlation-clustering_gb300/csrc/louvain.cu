@@ -24,6 +24,9 @@ namespace pcc {
 
 Status CompressGraph(Context* ctx, const DevGraph& g, const uint32_t* C, const double* k,
                      std::unique_ptr<DevGraph>* out);
+Status FindClusterMoves(Context* ctx, const DevGraph& g, const uint32_t* C, const double* k, const double* K,
+                        double res, double offset, bool exact_sums, uint32_t* moves, uint32_t* movers,
+                        DevCounters* ctr);
 
 namespace {
 
@@ -776,6 +779,7 @@ class Engine {
         PCC_COUNT(1);
       }
       PCC_RETURN_IF_ERROR(LaunchCheck());
+      if (cfg_.clustering_moves_method == PCC_DEFAULT_CLUSTER_MOVES) PCC_RETURN_IF_ERROR(WholeClusterMoves(L));
     }
     timer_.End(kPhaseApply);
     if (cfg_.move_method == PCC_ALL_MOVE) return Status::Ok();
@@ -805,6 +809,45 @@ class Engine {
     PCC_RETURN_IF_ERROR(LaunchCheck());
     timer_.End(kPhaseFrontier);
     return Status::Ok();
+  }
+
+  // Whole-cluster moves after the round's vertex moves (DEFAULT_CLUSTER_MOVES,
+  // parallel-correlation-clusterer.cc:167-297): the moving clusters'
+  // members go through the same apply as vertex movers, and the clusters it
+  // modifies carry this round's stamp, so the NBHR_CLUSTER_MOVE frontier
+  // sees them (moved_clusters |= additional_moved_clusters).  Host-driven
+  // rounds only (the step reads sizes on the host).
+  Status WholeClusterMoves(Level* L) {
+    const DevGraph& g = *L->g;
+    const uint32_t n = g.n;
+    DevCounters hc;
+    PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
+    PCC_RETURN_IF_ERROR(Sync(ctx_));
+    res_.moves += hc.movers;  // the vertex movers; the caller adds the cluster movers
+    PCC_CUDA(cudaMemsetAsync(&ctr_.p->movers, 0, sizeof(uint32_t), ctx_->stream));
+    PCC_CUDA(cudaMemsetAsync(&ctr_.p->new_movers, 0, sizeof(uint32_t), ctx_->stream));
+    // The vertex movers' new-cluster marks of this round are spent (0 is no stamp).
+    PCC_CUDA(cudaMemsetAsync(new_stamp_.p, 0, sizeof(uint32_t) * n, ctx_->stream));
+    // Integral entry values whose every partial sum stays below 2^53 sum
+    // exactly in any order.
+    const bool exact = L->int_mode && static_cast<double>(g.m) * (g.max_abs_w + std::fabs(cfg_.edge_weight_offset)) <
+                                          9007199254740992.0;
+    PCC_RETURN_IF_ERROR(FindClusterMoves(ctx_, g, L->C.p, L->k.p, L->K.p, cfg_.resolution, cfg_.edge_weight_offset,
+                                         exact, moves_.p, movers_.p, ctr_.p));
+    ApplyArgs ap{n, L->C.p, L->s.p, L->k.p, L->K.p, moves_.p, movers_.p, mod_stamp_.p, new_stamp_.p, stamp_,
+                 ctr_.p, nullptr};
+    const unsigned grid = GridFor(ctx_, n);
+    ApplyLeaveKernel<<<grid, kT, 0, ctx_->stream>>>(ap); PCC_COUNT(1);
+    ApplyJoinKernel<<<grid, kT, 0, ctx_->stream>>>(ap); PCC_COUNT(1);
+    PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, ZeroSizeInput{L->s.p, ctr_.p}, StoreIndexIfSet{zero_ids_.p},
+                                            scan_tiles_, static_cast<uint32_t*>(nullptr)));
+    PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, NewMoverInput{new_stamp_.p, stamp_, ctr_.p, nullptr},
+                                            StoreIndexIfSet{new_list_.p}, scan_tiles_,
+                                            static_cast<uint32_t*>(nullptr)));
+    AssignNewKernel<<<grid, kT, 0, ctx_->stream>>>(ap, zero_ids_.p, new_list_.p); PCC_COUNT(1);
+    RefreshKfKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->K.p, L->Kf.p, mod_stamp_.p, stamp_, nullptr);
+    PCC_COUNT(1);
+    return LaunchCheck();
   }
 
   // One best-move round over `front` (host_counts known), driven from the
@@ -953,7 +996,7 @@ class Engine {
   // moves, one graph, no detailed timing), else driven from the host.
   Status Iterate(Level* L, int64_t num_inner, bool* moved_out) {
     if (!cfg_.async && !un_ && !ctx_->detailed_timing && !ctx_->graphs_failed &&
-        L->g->m >= ctx_->device_loop_min_entries)
+        cfg_.clustering_moves_method == PCC_LOUVAIN && L->g->m >= ctx_->device_loop_min_entries)
       return IterateDevice(L, num_inner, moved_out);
     return IterateBestMoves(L, num_inner, moved_out);
   }
@@ -984,7 +1027,12 @@ class Engine {
       num_iterations = cfg_.louvain_num_iterations > 0 ? cfg_.louvain_num_iterations : 10;
       num_inner = cfg_.louvain_num_inner_iterations > 0 ? cfg_.louvain_num_inner_iterations : 10;
     } else if (cfg_.clustering_moves_method == PCC_DEFAULT_CLUSTER_MOVES) {
-      return MakeError(PCC_UNIMPLEMENTED, "DEFAULT_CLUSTER_MOVES (whole-cluster moves) is not available on GB300 yet");
+      // One level of up to num_iterations rounds (:487-492), each with
+      // whole-cluster moves after the vertex moves.
+      if (cfg_.async)
+        return MakeError(PCC_UNIMPLEMENTED, "DEFAULT_CLUSTER_MOVES with async moves is not available");
+      num_iterations = 1;
+      num_inner = cfg_.num_iterations > 0 ? cfg_.num_iterations : 20;
     } else {
       return MakeError(PCC_UNIMPLEMENTED,
                        "Correlation clustering moves must be DEFAULT_CLUSTER_MOVES or LOUVAIN.");

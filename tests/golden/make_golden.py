@@ -3,9 +3,10 @@
 An independent pure-Python restatement of the reference's parallel
 correlation / modularity clustering path (loops over dicts and sorted lists,
 no shared code with oracle/pcc_oracle.cc), written from:
-  parallel-correlation-clusterer.cc:115-365, 476-653   (rounds, levels, refine)
-  parallel-correlation-clusterer-internal.cc:50-149, 256-369, 448-583, 709-782
-  correlation-clusterer-util.h:26-43
+  parallel-correlation-clusterer.cc:115-365, 476-653   (rounds, levels, refine,
+                                                        whole-cluster moves)
+  parallel-correlation-clusterer-internal.cc:50-149, 256-369, 448-583, 644-782
+  correlation-clusterer-util.h:26-113
   parallel/parallel-graph-utils.cc:33-243, parallel-sequence-ops.h:161-209
   parallel-modularity-clusterer.cc:36-111
 The fixtures pin the C++ oracle (tests/test_oracle.py).  The reference
@@ -129,7 +130,45 @@ def move_nodes(C, s, k, K, n, moves):
     return modified
 
 
-def best_moves_round(g, C, s, k, K, frontier, res, off, move_method):
+def cluster_moves(g, C, s, k, K, res, off):
+    """Whole-cluster moves of one synchronous round (DEFAULT_CLUSTER_MOVES,
+    subclustering NONE): parallel-correlation-clusterer.cc:167-297 with
+    BestMove(moving_nodes) (internal.cc:644-707) and BestMoveFromStats
+    (correlation-clusterer-util.h:70-113).  Returns the modified clusters."""
+    n = g.n
+    moves = [None] * n
+    for members in groups_by_id(C):
+        c = C[members[0]]
+        inside = set(members)
+        weight, weight_c = 0.0, 0.0       # moving_nodes_weight, cluster_moving_weights[c]
+        after = {}                        # class_1_together_after: cluster -> sum
+        for v in members:
+            weight_c += k[v]
+            weight += k[v]
+            for (u, w) in g.adj[v]:
+                wf = f32(w - off)         # float weight -= double offset
+                if u in inside:
+                    continue              # class 2, both ends in c: not separate
+                after[C[u]] = after.get(C[u], 0.0) + wf
+        half_square = lambda x: x * x / 2
+        change = 0.0
+        change += 0.0 / 2 - res * (half_square(weight) - half_square(weight_c))
+        change -= 0.0 - res * (weight_c * (K[c] - weight_c))
+        best_id, best_val = None, change
+        for d, total in after.items():
+            val = change + (total - res * (weight * (K[d] - 0.0)))
+            if val > best_val or (val == best_val and best_id is not None and d < best_id):
+                best_id, best_val = d, val
+        target = best_id if best_id is not None else n
+        if target < n and c >= target:
+            best_val = 0.0
+        if best_val > 0:
+            for v in members:
+                moves[v] = target
+    return move_nodes(C, s, k, K, n, moves)
+
+
+def best_moves_round(g, C, s, k, K, frontier, res, off, move_method, whole_clusters=False):
     n = g.n
     moves = [None] * n
     moved_vertex = [False] * n
@@ -142,6 +181,9 @@ def best_moves_round(g, C, s, k, K, frontier, res, off, move_method):
             moves[v] = t
             moved_vertex[v] = True
     modified = move_nodes(C, s, k, K, n, moves)
+    if whole_clusters:
+        extra = cluster_moves(g, C, s, k, K, res, off)
+        modified = [a or b for a, b in zip(modified, extra)]
     if move_method == 1:  # ALL_MOVE
         return list(range(n))
     if move_method == 0:
@@ -156,7 +198,7 @@ def best_moves_round(g, C, s, k, K, frontier, res, off, move_method):
     return sorted(nxt)
 
 
-def iterate(g, C, s, k, K, inner, res, off, mm, ctr):
+def iterate(g, C, s, k, K, inner, res, off, mm, ctr, whole_clusters=False):
     frontier = list(range(g.n))
     moved = False
     local = True
@@ -164,7 +206,7 @@ def iterate(g, C, s, k, K, inner, res, off, mm, ctr):
     while it < inner and local:
         ctr["ev"] += sum(len(g.adj[v]) for v in frontier)
         ctr["rounds"] += 1
-        frontier = best_moves_round(g, C, s, k, K, frontier, res, off, mm)
+        frontier = best_moves_round(g, C, s, k, K, frontier, res, off, mm, whole_clusters)
         local = len(frontier) > 0
         moved |= local
         it += 1
@@ -209,8 +251,13 @@ def groups_by_id(ids):
 
 def cluster(g, cfg, node_weights=None):
     res, off = cfg["resolution"], cfg.get("edge_weight_offset", 0.0)
-    iters = cfg.get("louvain_num_iterations", 0) or 10
-    inner = cfg.get("louvain_num_inner_iterations", 0) or 10
+    whole = cfg.get("clustering_moves_method", 1) == 0  # DEFAULT_CLUSTER_MOVES
+    if whole:   # one level, num_iterations rounds (:487-492)
+        iters = 1
+        inner = cfg.get("num_iterations", 0) or 20
+    else:
+        iters = cfg.get("louvain_num_iterations", 0) or 10
+        inner = cfg.get("louvain_num_inner_iterations", 0) or 10
     refine = cfg.get("refine", False)
     mm = cfg.get("move_method", 0)
     n = g.n
@@ -224,7 +271,7 @@ def cluster(g, cfg, node_weights=None):
     ctr = {"ev": 0, "rounds": 0}
     it = 0
     while it < iters:
-        moved = iterate(cur, C, s, hk, K, inner, res, off, mm, ctr)
+        moved = iterate(cur, C, s, hk, K, inner, res, off, mm, ctr, whole)
         if not moved:
             it -= 1
             break
@@ -256,7 +303,7 @@ def cluster(g, cfg, node_weights=None):
                 for j in members:
                     Ci[j] = gi
                     Ki[gi] += ki[j]
-            iterate(graphs[i], Ci, si, ki, Ki, inner, res, off, mm, ctr)
+            iterate(graphs[i], Ci, si, ki, Ki, inner, res, off, mm, ctr, whole)
         ids = helpers[0][0]
     grps = groups_by_id(ids)
     labels = [0] * n
@@ -333,6 +380,16 @@ CONFIGS = [
     {"kind": "correlation", "resolution": 0.05, "edge_weight_offset": 0.5, "refine": True, "move_method": 2},
     {"kind": "modularity", "resolution": 1.0, "refine": True, "move_method": 2},
     {"kind": "modularity", "resolution": 0.5, "refine": False, "move_method": 0},
+    # Whole-cluster moves (one level).  With refine the reference's level loop
+    # returns the identity clustering (refinement needs a second level).
+    {"kind": "correlation", "resolution": 0.05, "refine": False, "move_method": 1,
+     "clustering_moves_method": 0},
+    {"kind": "correlation", "resolution": 0.2, "edge_weight_offset": 0.5, "refine": False, "move_method": 0,
+     "clustering_moves_method": 0, "num_iterations": 6},
+    {"kind": "correlation", "resolution": 0.01, "refine": True, "move_method": 2,
+     "clustering_moves_method": 0},
+    {"kind": "modularity", "resolution": 1.0, "refine": False, "move_method": 2,
+     "clustering_moves_method": 0},
 ]
 
 

@@ -199,6 +199,57 @@ def test_edge_cases(ctx):
     assert lab.tolist() == [0] and st["num_clusters"] == 1
 
 
+# Whole-cluster moves (DEFAULT_CLUSTER_MOVES): one level of num_iterations
+# rounds, each with vertex moves then whole-cluster moves.  With refine the
+# reference's level loop returns the identity clustering (a single level has
+# nothing to refine into).
+CM_CONFIGS = [
+    dict(resolution=0.05, move_method=P.ALL_MOVE, num_iterations=8),
+    dict(resolution=0.1, move_method=P.NBHR_CLUSTER_MOVE),
+    dict(resolution=0.02, edge_weight_offset=0.5, move_method=P.NBHR_MOVE, num_iterations=12),
+    dict(resolution=0.01, move_method=P.NBHR_CLUSTER_MOVE, refine=True),
+]
+
+
+@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "sbm3k_int", "hubs100k"])
+@pytest.mark.parametrize("ci", range(len(CM_CONFIGS)))
+def test_cluster_moves_bit_exact(ctx, graphs, name, ci):
+    g = graphs[name]
+    dg, og = _both(ctx, g)
+    cfg = P.make_config(clustering_moves_method=P.DEFAULT_CLUSTER_MOVES, **CM_CONFIGS[ci])
+    lab_g, st_g = P.correlation_cluster(dg, cfg)
+    lab_o, st_o = O.correlation_cluster(og, cfg)
+    np.testing.assert_array_equal(lab_g, lab_o)
+    assert st_g["edge_visits"] == st_o["edge_visits"]
+    assert st_g["rounds"] == st_o["rounds"]
+    assert st_g["levels"] == st_o["levels"]
+    assert st_g["objective"] == pytest.approx(st_o["objective"], rel=REL_TOL, abs=1e-9)
+
+
+@pytest.mark.parametrize("name", ["sbm2k", "rmat16"])
+@pytest.mark.parametrize("move", [P.NBHR_MOVE, P.NBHR_CLUSTER_MOVE])
+def test_modularity_cluster_moves_bit_exact(ctx, graphs, name, move):
+    g = graphs[name]
+    dg, og = _both(ctx, g)
+    cfg = P.make_config(resolution=1.0, move_method=move, clustering_moves_method=P.DEFAULT_CLUSTER_MOVES)
+    lab_g, st_g = P.modularity_cluster(dg, cfg)
+    lab_o, st_o = O.modularity_cluster(og, cfg)
+    np.testing.assert_array_equal(lab_g, lab_o)
+    assert st_g["rounds"] == st_o["rounds"]
+    assert st_g["modularity"] == pytest.approx(st_o["modularity"], rel=REL_TOL, abs=1e-12)
+
+
+def test_cluster_moves_real_weights(ctx, graphs):
+    """FP64 mode with whole-cluster moves: objective within 1e-9 relative."""
+    g = graphs["lfr20k_real"]
+    dg, og = _both(ctx, g)
+    cfg = P.make_config(resolution=0.1, move_method=P.NBHR_CLUSTER_MOVE,
+                        clustering_moves_method=P.DEFAULT_CLUSTER_MOVES)
+    _, st_g = P.correlation_cluster(dg, cfg)
+    _, st_o = O.correlation_cluster(og, cfg)
+    assert st_g["objective"] == pytest.approx(st_o["objective"], rel=REL_TOL)
+
+
 def test_errors_are_status_codes(ctx, graphs):
     g = graphs["sbm2k"]
     dg = ctx.upload(g)
@@ -207,6 +258,9 @@ def test_errors_are_status_codes(ctx, graphs):
     assert e.value.code == 12  # UNIMPLEMENTED, as the reference
     with pytest.raises(P.PccError) as e:
         P.correlation_cluster(dg, P.make_config(subclustering_method=1))
+    assert e.value.code == 12
+    with pytest.raises(P.PccError) as e:  # async whole-cluster moves are not built
+        P.correlation_cluster(dg, P.make_config(clustering_moves_method=P.DEFAULT_CLUSTER_MOVES, async_=True))
     assert e.value.code == 12
     bad = np.full(g.n, g.n + 5, np.uint32)
     with pytest.raises(P.PccError) as e:

@@ -42,14 +42,16 @@ def _cfg(d):
     return P.make_config(resolution=d["resolution"], edge_weight_offset=d.get("edge_weight_offset", 0.0),
                          refine=d.get("refine", False), move_method=d.get("move_method", 0),
                          louvain_num_iterations=d.get("louvain_num_iterations", 0),
-                         louvain_num_inner_iterations=d.get("louvain_num_inner_iterations", 0))
+                         louvain_num_inner_iterations=d.get("louvain_num_inner_iterations", 0),
+                         clustering_moves_method=d.get("clustering_moves_method", P.LOUVAIN),
+                         num_iterations=d.get("num_iterations", 0))
 
 
 with open(os.path.join(HERE, "golden", "golden_clusterings.json")) as _f:
     GOLDEN = json.load(_f)
 
 
-@pytest.mark.parametrize("fx", GOLDEN, ids=[f"{g['graph']}-{i % 6}" for i, g in enumerate(GOLDEN)])
+@pytest.mark.parametrize("fx", GOLDEN, ids=[f"{g['graph']}-{i % 10}" for i, g in enumerate(GOLDEN)])
 def test_oracle_matches_golden(fx):
     g = _csr(fx["n"], fx["edges"], fx["weights"])
     og = O.OracleGraph(g)
@@ -201,3 +203,14 @@ def test_move_nodes_new_cluster_ids():
     assert C2.tolist() == [0, 0, 1, 3, 2, 0]
     assert s2.tolist() == [3, 1, 1, 1, 0, 0]
     assert mod.tolist() == [1, 1, 1, 1, 0, 1]
+
+
+def test_oracle_async_cluster_moves_unimplemented():
+    """DEFAULT_CLUSTER_MOVES with async moves (AsyncMove(moving_nodes)) is not
+    restated; the oracle answers UNIMPLEMENTED like the GPU library."""
+    g = _csr(6, [(0, 1), (1, 2), (0, 2), (3, 4), (4, 5), (3, 5), (2, 3)])
+    og = O.OracleGraph(g)
+    cfg = P.make_config(resolution=0.1, clustering_moves_method=P.DEFAULT_CLUSTER_MOVES, async_=True)
+    with pytest.raises(Exception) as e:
+        O.correlation_cluster(og, cfg)
+    assert "12" in str(e.value) or "UNIMPLEMENTED" in str(e.value)
