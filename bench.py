@@ -514,6 +514,18 @@ def main():
         a_mod.append(st["modularity"])
     barrier()
 
+    # Whole-cluster moves (DEFAULT_CLUSTER_MOVES): one level of up to 20
+    # rounds, each with vertex moves then whole-cluster moves.
+    ccfg = P.make_config(resolution=1.0, move_method=P.NBHR_MOVE, clustering_moves_method=P.DEFAULT_CLUSTER_MOVES)
+    P.modularity_cluster(dg, ccfg)
+    c_ev, c_ms, c_mod, c_steps = 0, 0.0, None, min(args.steps, 3)
+    for _ in range(c_steps):
+        _, st = P.modularity_cluster(dg, ccfg)
+        c_ev += st["edge_visits"]
+        c_ms += st["ms_total"]
+        c_mod = st["modularity"]
+    barrier()
+
     # Batched and serving workloads (rank 0; one GPU each).
     batched = serving = lfr = None
     if rank == 0 and args.lfr_n > 0:
@@ -583,7 +595,12 @@ def main():
             "quality": quality,
             "modes": {"async": {"value": a_ev / (a_ms / 1000.0) if a_ms > 0 else None, "unit": UNIT,
                                 "ms_per_step": a_ms / args.steps, "modularity_mean": sum(a_mod) / len(a_mod),
-                                "note": "same graph and config with async=true, 16 waves per round"}},
+                                "note": "same graph and config with async=true, 16 waves per round"},
+                      "cluster_moves": {"value": c_ev / (c_ms / 1000.0) if c_ms > 0 else None, "unit": UNIT,
+                                        "ms_per_step": c_ms / c_steps if c_steps else None, "modularity": c_mod,
+                                        "note": "same graph, clustering_moves_method DEFAULT_CLUSTER_MOVES "
+                                                "(one level, 20 rounds, whole-cluster moves after each "
+                                                "round's vertex moves), no refine"}},
             "lfr": lfr,
             "batched": batched,
             "serving": serving,
