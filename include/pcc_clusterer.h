@@ -261,6 +261,11 @@ struct CommunityScores {
 };
 CommunityScores CompareCommunities(const std::vector<std::vector<uint32_t>>& communities,
                                    const InMemoryClusterer::Clustering& clustering);
+// The same scores computed on the device (pcc_compare_communities) on GPU
+// `device`; what the CLI's --input_communities step runs.
+Status CompareCommunitiesOnDevice(const std::vector<std::vector<uint32_t>>& communities,
+                                  const InMemoryClusterer::Clustering& clustering, int device,
+                                  CommunityScores* out);
 
 }  // namespace pcc_gb300
 

@@ -226,6 +226,40 @@ pcc_status pcc_modularity(pcc_context* ctx, const pcc_graph* graph,
                           double* out_modularity);
 
 /*
+ * Ground-truth scoring on the device: CompareCommunities
+ * (clustering/cluster-in-memory_main.cc:172-225), the CLI's
+ * --input_communities step.  Replaces the host loops the reference runs
+ * after Cluster() returns.
+ *
+ * labels[n] (< n) is a clustering: cluster i is the i-th distinct label in
+ * ascending order, as OutputIndicesById lists the clustering.  Community j
+ * is members[offsets[j] .. offsets[j+1]) (order and repeats as read from
+ * the file, see ReadCommunities :155-170; an id >= n meets no cluster but
+ * counts in the community's size).  For each
+ * community: the cluster with the largest intersection (the first such
+ * cluster on ties; cluster 0 when every intersection is empty), precision
+ * = intersection / that cluster's size, recall = intersection / community
+ * size (0 for an empty community).  Averages use pbbs::reduce_add order.
+ * precision / recall (num_communities each) may be NULL.
+ */
+typedef struct pcc_community_scores {
+  double avg_precision;
+  double avg_recall;
+  uint64_t num_clusters;  /* "Num communities" of the reference's report */
+  uint64_t min_size;      /* UINT32_MAX (UINT_E_MAX) when there is no cluster */
+  uint64_t max_size;
+  double avg_size;
+} pcc_community_scores;
+
+pcc_status pcc_compare_communities(pcc_context* ctx, uint32_t n,
+                                   const uint32_t* labels,
+                                   uint32_t num_communities,
+                                   const uint64_t* offsets,
+                                   const uint32_t* members,
+                                   double* precision, double* recall,
+                                   pcc_community_scores* out);
+
+/*
  * One synchronous best-move pass over ALL vertices from a given state:
  * ClusteringHelper::EfficientBestMove plus the sync decision of
  * BestMovesForVertexSubset (parallel-correlation-clusterer-internal.cc:

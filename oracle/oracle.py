@@ -77,6 +77,9 @@ def lib():
                                       P(ctypes.c_double), P(ctypes.c_uint32),
                                       P(ctypes.c_uint8)]
         L.pcco_compress.argtypes = [vp, P(ctypes.c_uint32), P(ctypes.c_double)]
+        L.pcco_compare_communities.argtypes = [ctypes.c_uint32, P(ctypes.c_uint32), ctypes.c_uint32,
+                                               P(ctypes.c_uint64), P(ctypes.c_uint32),
+                                               P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]
         L.pcco_compress.restype = vp
         _lib = L
     return _lib
@@ -213,3 +216,25 @@ def compress(g: OracleGraph, C, node_weights=None):
     h = lib().pcco_compress(g.h, _p(C, ctypes.c_uint32), _p(k, ctypes.c_double))
     og = OracleGraph(handle=h)
     return og.to_csr()
+
+
+def compare_communities(labels, communities):
+    """CompareCommunities on host lists; returns (scores dict, precision,
+    recall).  communities: a list of vertex-id sequences."""
+    labels = np.ascontiguousarray(labels, np.uint32)
+    sizes = [len(c) for c in communities]
+    off = np.zeros(len(communities) + 1, np.uint64)
+    off[1:] = np.cumsum(sizes, dtype=np.uint64)
+    mem = (np.concatenate([np.asarray(c, np.uint32) for c in communities]) if sum(sizes)
+           else np.zeros(1, np.uint32))
+    mem = np.ascontiguousarray(mem, np.uint32)
+    prec = np.zeros(max(len(communities), 1), np.float64)
+    rec = np.zeros(max(len(communities), 1), np.float64)
+    out = np.zeros(6, np.float64)
+    _check(lib().pcco_compare_communities(labels.size, _p(labels, ctypes.c_uint32), len(communities),
+                                          _p(off, ctypes.c_uint64), _p(mem, ctypes.c_uint32),
+                                          _p(prec, ctypes.c_double), _p(rec, ctypes.c_double),
+                                          _p(out, ctypes.c_double)))
+    scores = {"avg_precision": out[0], "avg_recall": out[1], "num_clusters": int(out[2]),
+              "min_size": int(out[3]), "max_size": int(out[4]), "avg_size": out[5]}
+    return scores, prec[:len(communities)], rec[:len(communities)]

@@ -1037,6 +1037,61 @@ int pcco_move_nodes(uint32_t n, uint32_t* C, uint32_t* s, const double* k,
   return PCC_OK;
 }
 
+// CompareCommunities (clustering/cluster-in-memory_main.cc:172-225), read
+// literally: the clustering is OutputIndicesById of the labels (groups in
+// ascending label order, members ascending), each community is sorted
+// (ReadCommunities, :155-170), std::set_intersection against every cluster
+// in order keeps the first largest, and the averages are pbbs::reduce_add
+// over the per-community vectors divided by their count.  out[6] =
+// {avg_precision, avg_recall, num_clusters, min_size, max_size, avg_size}.
+int pcco_compare_communities(uint32_t n, const uint32_t* labels, uint32_t num_comm,
+                             const uint64_t* off, const uint32_t* members,
+                             double* precision, double* recall, double* out) {
+  const std::vector<uint32_t> ids(labels, labels + n);
+  const std::vector<std::vector<uint32_t>> clustering = GroupsById(ids);
+  std::vector<double> prec(num_comm, 0.0), rec(num_comm, 0.0);
+  for (uint32_t j = 0; j < num_comm; ++j) {
+    std::vector<uint32_t> community(members + off[j], members + off[j + 1]);
+    std::sort(community.begin(), community.end());
+    std::vector<uint32_t> intersect(community.size());
+    size_t max_intersect = 0, max_idx = 0;
+    for (size_t i = 0; i < clustering.size(); ++i) {
+      const std::vector<uint32_t>& cluster = clustering[i];
+      auto it = std::set_intersection(cluster.begin(), cluster.end(), community.begin(),
+                                      community.end(), intersect.begin());
+      const size_t sz = static_cast<size_t>(it - intersect.begin());
+      if (sz > max_intersect) {
+        max_intersect = sz;
+        max_idx = i;
+      }
+    }
+    const size_t csize = clustering.empty() ? 0 : clustering[max_idx].size();
+    prec[j] = csize ? static_cast<double>(max_intersect) / static_cast<double>(csize) : 0.0;
+    rec[j] = community.empty() ? 0.0
+                               : static_cast<double>(max_intersect) / static_cast<double>(community.size());
+  }
+  auto add = [](double a, double b) { return a + b; };
+  const double sp = num_comm ? BlockedReduce(prec.data(), num_comm, add) : 0.0;
+  const double sr = num_comm ? BlockedReduce(rec.data(), num_comm, add) : 0.0;
+  out[0] = sp / static_cast<double>(num_comm);
+  out[1] = sr / static_cast<double>(num_comm);
+  size_t min_size = 0xFFFFFFFFu, max_size = 0;  // UINT_E_MAX
+  double avg_size = 0;
+  for (const auto& c : clustering) {
+    min_size = std::min(min_size, c.size());
+    max_size = std::max(max_size, c.size());
+    avg_size += static_cast<double>(c.size());
+  }
+  avg_size /= static_cast<double>(clustering.size());
+  out[2] = static_cast<double>(clustering.size());
+  out[3] = static_cast<double>(min_size);
+  out[4] = static_cast<double>(max_size);
+  out[5] = avg_size;
+  if (precision) std::copy(prec.begin(), prec.end(), precision);
+  if (recall) std::copy(rec.begin(), rec.end(), recall);
+  return PCC_OK;
+}
+
 pcco_graph* pcco_compress(const pcco_graph* g, const uint32_t* C,
                           const double* k) {
   std::vector<uint32_t> c(C, C + g->g.n);

@@ -129,7 +129,9 @@ Status Main(int argc, char** argv) {
     std::vector<std::vector<uint32_t>> comm;
     s = pcc_gb300::ReadCommunities(communities, &comm);
     if (!s.ok()) return s;
-    const auto r = pcc_gb300::CompareCommunities(comm, *clustering);
+    pcc_gb300::CommunityScores r;  // scored on the device
+    s = pcc_gb300::CompareCommunitiesOnDevice(comm, *clustering, 0, &r);
+    if (!s.ok()) return s;
     std::cout << "Avg precision: " << std::setprecision(17) << r.avg_precision << std::endl;
     std::cout << "Avg recall: " << std::setprecision(17) << r.avg_recall << std::endl;
     std::cout << "Num communities: " << r.num_clusters << std::endl;

@@ -777,6 +777,25 @@ Status ReadCommunities(const std::string& path, std::vector<std::vector<uint32_t
   return Status::Ok();
 }
 
+// pbbs::reduce_add order: a serial fold of <= 1024 items, else serial folds
+// of 1024-item blocks followed by the same reduce over the block sums.
+static double BlockedSum(const std::vector<double>& a) {
+  if (a.empty()) return 0.0;
+  if (a.size() <= 1024) {
+    double r = a[0];
+    for (size_t j = 1; j < a.size(); ++j) r += a[j];
+    return r;
+  }
+  std::vector<double> sums((a.size() + 1023) / 1024);
+  for (size_t b = 0; b < sums.size(); ++b) {
+    const size_t s = b * 1024, e = std::min(a.size(), s + 1024);
+    double r = a[s];
+    for (size_t j = s + 1; j < e; ++j) r += a[j];
+    sums[b] = r;
+  }
+  return BlockedSum(sums);
+}
+
 CommunityScores CompareCommunities(const std::vector<std::vector<uint32_t>>& communities,
                                    const InMemoryClusterer::Clustering& clustering) {
   CommunityScores out;
@@ -789,11 +808,18 @@ CommunityScores CompareCommunities(const std::vector<std::vector<uint32_t>>& com
   std::vector<uint32_t> owner(max_node, 0xFFFFFFFFu);
   for (size_t i = 0; i < sorted.size(); ++i)
     for (uint32_t v : sorted[i]) owner[v] = static_cast<uint32_t>(i);
-  double sum_p = 0, sum_r = 0;
+  std::vector<double> prec(communities.size(), 0.0), rec(communities.size(), 0.0);
   std::map<uint32_t, size_t> count;
-  for (const auto& community : communities) {
+  std::vector<uint32_t> distinct;
+  for (size_t j = 0; j < communities.size(); ++j) {
+    const std::vector<uint32_t>& community = communities[j];
+    // std::set_intersection counts a repeated member once: the cluster
+    // holds it once.
+    distinct.assign(community.begin(), community.end());
+    std::sort(distinct.begin(), distinct.end());
+    distinct.erase(std::unique(distinct.begin(), distinct.end()), distinct.end());
     count.clear();
-    for (uint32_t v : community)
+    for (uint32_t v : distinct)
       if (v < max_node && owner[v] != 0xFFFFFFFFu) ++count[owner[v]];
     // The largest intersection, the first cluster (lowest index) on ties;
     // cluster 0 when nothing intersects.
@@ -805,13 +831,13 @@ CommunityScores CompareCommunities(const std::vector<std::vector<uint32_t>>& com
       }
     }
     const double denom = sorted.empty() ? 0.0 : static_cast<double>(sorted[best_idx].size());
-    sum_p += denom > 0 ? static_cast<double>(best) / denom : 0.0;
-    sum_r += community.empty() ? 0.0 : static_cast<double>(best) / static_cast<double>(community.size());
+    prec[j] = denom > 0 ? static_cast<double>(best) / denom : 0.0;
+    rec[j] = community.empty() ? 0.0 : static_cast<double>(best) / static_cast<double>(community.size());
   }
-  out.avg_precision = sum_p / static_cast<double>(communities.size());
-  out.avg_recall = sum_r / static_cast<double>(communities.size());
+  out.avg_precision = BlockedSum(prec) / static_cast<double>(communities.size());
+  out.avg_recall = BlockedSum(rec) / static_cast<double>(communities.size());
   out.num_clusters = sorted.size();
-  out.min_size = sorted.empty() ? 0 : SIZE_MAX;
+  out.min_size = 0xFFFFFFFFu;  // UINT_E_MAX, the reference's start value
   for (const auto& c : sorted) {
     out.min_size = std::min(out.min_size, c.size());
     out.max_size = std::max(out.max_size, c.size());
@@ -819,6 +845,45 @@ CommunityScores CompareCommunities(const std::vector<std::vector<uint32_t>>& com
   }
   out.avg_size /= static_cast<double>(sorted.size());
   return out;
+}
+
+Status CompareCommunitiesOnDevice(const std::vector<std::vector<uint32_t>>& communities,
+                                  const InMemoryClusterer::Clustering& clustering, int device,
+                                  CommunityScores* out) {
+  // Labels: cluster i of the clustering is label i (OutputIndicesById order).
+  uint64_t n64 = 0;
+  for (const auto& c : clustering) n64 += c.size();
+  if (n64 > 0xFFFFFFFFull) return Status(PCC_INVALID_ARGUMENT, "clustering too large");
+  const uint32_t n = static_cast<uint32_t>(n64);
+  std::vector<uint32_t> labels(n, 0xFFFFFFFFu);
+  for (size_t i = 0; i < clustering.size(); ++i)
+    for (uint32_t v : clustering[i]) {
+      if (v >= n || labels[v] != 0xFFFFFFFFu)
+        return Status(PCC_INVALID_ARGUMENT, "the clustering must cover nodes 0..n-1 once");
+      labels[v] = static_cast<uint32_t>(i);
+    }
+  std::vector<uint64_t> offsets(communities.size() + 1, 0);
+  std::vector<uint32_t> members;
+  for (size_t j = 0; j < communities.size(); ++j) {
+    members.insert(members.end(), communities[j].begin(), communities[j].end());
+    offsets[j + 1] = members.size();
+  }
+  pcc_context* ctx = nullptr;
+  pcc_status st = pcc_create(&ctx, device, 0);
+  if (st != PCC_OK) return Status(st, "pcc_create failed (no usable GPU)");
+  pcc_community_scores r{};
+  st = pcc_compare_communities(ctx, n, labels.data(), static_cast<uint32_t>(communities.size()), offsets.data(),
+                               members.empty() ? nullptr : members.data(), nullptr, nullptr, &r);
+  const std::string msg = st == PCC_OK ? std::string() : std::string(pcc_last_error(ctx));
+  pcc_destroy(ctx);
+  if (st != PCC_OK) return Status(st, msg);
+  out->avg_precision = r.avg_precision;
+  out->avg_recall = r.avg_recall;
+  out->num_clusters = static_cast<size_t>(r.num_clusters);
+  out->min_size = static_cast<size_t>(r.min_size);
+  out->max_size = static_cast<size_t>(r.max_size);
+  out->avg_size = r.avg_size;
+  return Status::Ok();
 }
 
 }  // namespace pcc_gb300
@@ -885,6 +950,9 @@ int32_t pcch_compare_communities(const char* communities_path, uint32_t n, const
   for (uint32_t v = 0; v < n; ++v) k = std::max(k, labels[v] + 1);
   pcc_gb300::InMemoryClusterer::Clustering cl(k);
   for (uint32_t v = 0; v < n; ++v) cl[labels[v]].push_back(v);
+  // OutputIndicesById lists only the labels in use, in ascending order.
+  cl.erase(std::remove_if(cl.begin(), cl.end(), [](const std::vector<uint32_t>& c) { return c.empty(); }),
+           cl.end());
   const pcc_gb300::CommunityScores r = pcc_gb300::CompareCommunities(comm, cl);
   out6[0] = r.avg_precision;
   out6[1] = r.avg_recall;

@@ -69,6 +69,12 @@ class PccConfig(ctypes.Structure):
     ]
 
 
+class PccCommunityScores(ctypes.Structure):
+    _fields_ = [("avg_precision", ctypes.c_double), ("avg_recall", ctypes.c_double),
+                ("num_clusters", ctypes.c_uint64), ("min_size", ctypes.c_uint64),
+                ("max_size", ctypes.c_uint64), ("avg_size", ctypes.c_double)]
+
+
 class PccStats(ctypes.Structure):
     _fields_ = [
         ("edge_visits", ctypes.c_uint64),
@@ -273,6 +279,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.pcc_modularity.argtypes = [vp, vp, ctypes.c_double, P(ctypes.c_uint32),
                                    P(ctypes.c_double)]
     lib.pcc_modularity.restype = ctypes.c_int
+    lib.pcc_compare_communities.argtypes = [vp, ctypes.c_uint32, P(ctypes.c_uint32), ctypes.c_uint32,
+                                            P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_double),
+                                            P(ctypes.c_double), P(PccCommunityScores)]
+    lib.pcc_compare_communities.restype = ctypes.c_int
     lib.pcc_best_moves.argtypes = [vp, vp, P(PccConfig), P(ctypes.c_uint32),
                                    P(ctypes.c_uint32), P(ctypes.c_double),
                                    P(ctypes.c_double), P(ctypes.c_uint32),
@@ -455,6 +465,28 @@ def modularity(g: DeviceGraph, resolution: float, labels) -> float:
     g.ctx.check(g.ctx.lib.pcc_modularity(g.ctx.handle, g.handle, resolution,
                                          _ptr(lab, ctypes.c_uint32), ctypes.byref(out)))
     return float(out.value)
+
+
+def compare_communities(ctx: "Context", labels, communities):
+    """Ground-truth scoring (CompareCommunities, cluster-in-memory_main.cc:
+    172-225) on the device.  communities: a list of vertex-id sequences.
+    Returns (scores dict, precision per community, recall per community)."""
+    lab = _u32(labels)
+    sizes = [len(c) for c in communities]
+    off = np.zeros(len(communities) + 1, np.uint64)
+    off[1:] = np.cumsum(sizes, dtype=np.uint64)
+    mem = (np.concatenate([np.asarray(c, np.uint32) for c in communities]) if sum(sizes)
+           else np.zeros(1, np.uint32))
+    mem = np.ascontiguousarray(mem, np.uint32)
+    prec = np.zeros(max(len(communities), 1), np.float64)
+    rec = np.zeros(max(len(communities), 1), np.float64)
+    out = PccCommunityScores()
+    ctx.check(ctx.lib.pcc_compare_communities(ctx.handle, lab.size, _ptr(lab, ctypes.c_uint32), len(communities),
+                                              _ptr(off, ctypes.c_uint64), _ptr(mem, ctypes.c_uint32),
+                                              _ptr(prec, ctypes.c_double), _ptr(rec, ctypes.c_double),
+                                              ctypes.byref(out)))
+    scores = {name: getattr(out, name) for name, _ in out._fields_}
+    return scores, prec[:len(communities)], rec[:len(communities)]
 
 
 def best_moves(g: DeviceGraph, config: PccConfig, cluster_ids, cluster_sizes, node_weights,

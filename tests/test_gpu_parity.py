@@ -250,6 +250,49 @@ def test_cluster_moves_real_weights(ctx, graphs):
     assert st_g["objective"] == pytest.approx(st_o["objective"], rel=REL_TOL)
 
 
+def _same(a, b):
+    return a == b or (isinstance(a, float) and isinstance(b, float) and np.isnan(a) and np.isnan(b))
+
+
+@pytest.mark.parametrize("ci", range(3))
+def test_compare_communities_device(ctx, ci):
+    """Device CompareCommunities equals the oracle bit for bit: repeats, ids
+    outside the graph, empty communities, sparse labels, > 1024 communities."""
+    from test_oracle import community_cases
+    labels, comms = community_cases()[ci]
+    got, gp, gr = P.compare_communities(ctx, labels, comms)
+    want, wp, wr = O.compare_communities(labels, comms)
+    np.testing.assert_array_equal(gp, wp)
+    np.testing.assert_array_equal(gr, wr)
+    for key, val in want.items():
+        assert _same(float(got[key]), float(val)), key
+
+
+def test_compare_communities_planted(ctx, graphs):
+    """A GPU clustering of an SBM scored against its planted blocks."""
+    g, blocks = G.sbm(3000, 30, 0.05, 0.001, 21)
+    dg = ctx.upload(g)
+    labels, _ = P.correlation_cluster(dg, P.make_config(resolution=0.02, refine=True))
+    comms = [np.flatnonzero(blocks == b).tolist() for b in range(int(blocks.max()) + 1)]
+    got, gp, gr = P.compare_communities(ctx, labels, comms)
+    want, wp, wr = O.compare_communities(labels, comms)
+    np.testing.assert_array_equal(gp, wp)
+    np.testing.assert_array_equal(gr, wr)
+    for key, val in want.items():
+        assert _same(float(got[key]), float(val)), key
+    assert got["avg_precision"] > 0.5 and got["avg_recall"] > 0.5
+    # No graph: every member is outside it; sizes report the reference's
+    # start values.
+    got0, gp0, _ = P.compare_communities(ctx, np.zeros(0, np.uint32), [[0, 1], []])
+    want0, wp0, _ = O.compare_communities(np.zeros(0, np.uint32), [[0, 1], []])
+    np.testing.assert_array_equal(gp0, wp0)
+    for key, val in want0.items():
+        assert _same(float(got0[key]), float(val)), key
+    with pytest.raises(P.PccError) as e:  # labels must be below n
+        P.compare_communities(ctx, np.array([0, 5], np.uint32), [[0]])
+    assert e.value.code == 3
+
+
 def test_errors_are_status_codes(ctx, graphs):
     g = graphs["sbm2k"]
     dg = ctx.upload(g)

@@ -166,3 +166,18 @@ def test_cli_error_paths(built, tmp_path):
         r = _cli("--clusterer_name=ParallelModularityClusterer",
                  "--clusterer_config=correlation_clusterer_config { resolution: 1 }", "--input_graph", path)
         assert r.returncode != 0 and "UNAVAILABLE" in r.stderr
+
+
+def test_compare_communities_matches_oracle(built, tmp_path):
+    """The host library's CompareCommunities (CPU path of the CLI) equals the
+    oracle's reading of the reference bit for bit, repeats and ids outside
+    the graph included."""
+    from test_oracle import community_cases
+    import oracle as O
+    for labels, comms in community_cases():
+        path = tmp_path / "comm.txt"
+        path.write_text("".join("".join(f"{v}\t" for v in c) + "\n" for c in comms))
+        got = G.compare_communities(str(path), labels)
+        want, _, _ = O.compare_communities(labels, [sorted(c) for c in comms])
+        for key in ("avg_precision", "avg_recall", "num_clusters", "min_size", "max_size", "avg_size"):
+            assert got[key] == want[key], key

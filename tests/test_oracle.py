@@ -214,3 +214,72 @@ def test_oracle_async_cluster_moves_unimplemented():
     with pytest.raises(Exception) as e:
         O.correlation_cluster(og, cfg)
     assert "12" in str(e.value) or "UNIMPLEMENTED" in str(e.value)
+
+
+def _blocked_sum(xs):
+    """pbbs::reduce_add order: serial fold of <= 1024 items, else folds of
+    1024-item blocks and the same reduce over the block sums."""
+    if not xs:
+        return 0.0
+    if len(xs) <= 1024:
+        r = xs[0]
+        for x in xs[1:]:
+            r += x
+        return r
+    return _blocked_sum([_blocked_sum(xs[i:i + 1024]) for i in range(0, len(xs), 1024)])
+
+
+def _compare_brute(labels, communities):
+    """CompareCommunities (cluster-in-memory_main.cc:172-225) by definition:
+    intersections as Python sets, first largest in cluster order."""
+    clusters = {}
+    for v, c in enumerate(labels):
+        clusters.setdefault(int(c), set()).add(v)
+    order = [clusters[c] for c in sorted(clusters)]
+    prec, rec = [], []
+    for comm in communities:
+        cs = set(int(v) for v in comm)
+        best, idx = 0, 0
+        for i, cl in enumerate(order):
+            k = len(cl & cs)
+            if k > best:
+                best, idx = k, i
+        prec.append(best / len(order[idx]) if order else 0.0)
+        rec.append(best / len(comm) if len(comm) else 0.0)
+    nc = len(communities)
+    sizes = [len(c) for c in order]
+    return ({"avg_precision": _blocked_sum(prec) / nc if nc else float("nan"),
+             "avg_recall": _blocked_sum(rec) / nc if nc else float("nan"),
+             "num_clusters": len(order), "min_size": min(sizes) if sizes else 0xFFFFFFFF,
+             "max_size": max(sizes) if sizes else 0,
+             "avg_size": sum(sizes) / len(sizes) if sizes else float("nan")}, prec, rec)
+
+
+def community_cases():
+    """Seeded (labels, communities) cases: repeated members, ids no cluster
+    holds, empty communities, labels that are not dense, ties, and more
+    than 1024 communities (the blocked reduce)."""
+    rng = np.random.default_rng(11)
+    out = []
+    for n, k, nc in ((40, 7, 9), (300, 25, 40), (2000, 300, 2500)):
+        labels = rng.choice(rng.permutation(n)[:k], size=n)            # sparse label values
+        comms = []
+        for j in range(nc):
+            size = int(rng.integers(0, 12))
+            c = rng.integers(0, n + 5, size=size).tolist()             # ids >= n too
+            if size and rng.random() < 0.3:
+                c += c[:2]                                              # repeats
+            comms.append(c)
+        comms.append([])
+        out.append((labels.astype(np.uint32), comms))
+    return out
+
+
+@pytest.mark.parametrize("ci", range(3))
+def test_oracle_compare_communities_brute_force(ci):
+    labels, comms = community_cases()[ci]
+    got, gp, gr = O.compare_communities(labels, comms)
+    want, wp, wr = _compare_brute(labels, comms)
+    assert gp.tolist() == wp and gr.tolist() == wr
+    for key, val in want.items():
+        assert got[key] == val, key
