@@ -231,17 +231,27 @@ def lfr_leg(args, P, G, ctx, dist_steps: int = 2):
     correlation, resolution 0.1, refine, NBHR_CLUSTER_MOVE, permute, sync.
     Graph resident in HBM; the oracle runs the same config on a 1M-vertex
     graph of the same distribution (bounded CPU sample)."""
-    g, _ = G.lfr(args.lfr_n, mean_degree=20, dmax=2000, seed=6)
+    import numpy as np
+    g, planted = G.lfr(args.lfr_n, mean_degree=20, dmax=2000, seed=6)
     cfg = P.make_config(resolution=0.1, refine=True, move_method=P.NBHR_CLUSTER_MOVE, permute=True, random_seed=1)
     dg = ctx.upload(g)
     P.correlation_cluster(dg, cfg)
     ev, ms = 0, 0.0
-    st = None
+    st = labels = None
     for _ in range(dist_steps):
-        _, st = P.correlation_cluster(dg, cfg)
+        labels, st = P.correlation_cluster(dg, cfg)
         ev += st["edge_visits"]
         ms += st["ms_total"]
     dg.free()
+    # Ground-truth scoring (CompareCommunities) of the clustering against the
+    # planted communities, on the device; host arrays in, report out.
+    order = np.argsort(planted, kind="stable").astype(np.uint32)
+    comm_off = np.zeros(int(planted.max()) + 2, np.uint64)
+    comm_off[1:] = np.cumsum(np.bincount(planted), dtype=np.uint64)
+    P.compare_communities(ctx, labels, offsets=comm_off, members=order)
+    t = time.perf_counter()
+    score, _, _ = P.compare_communities(ctx, labels, offsets=comm_off, members=order)
+    score_ms = (time.perf_counter() - t) * 1000.0
     out = {
         "workload": "lfr_like_real_weights_correlation_refine_nbhr_cluster_sync",
         "n": g.n, "m_entries": g.m, "dtype": "f64 (real weights: FP64 best moves)",
@@ -250,6 +260,10 @@ def lfr_leg(args, P, G, ctx, dist_steps: int = 2):
         "rounds": st["rounds"],
         "phases_ms_per_step": {"best_moves": st["ms_best_moves"], "compress": st["ms_compress"],
                                "apply": st["ms_apply"], "frontier": st["ms_frontier"]},
+        "scoring": {"what": "CompareCommunities on the device against the planted communities "
+                            "(pcc_compare_communities, host arrays in and out)",
+                    "communities": int(comm_off.size - 1), "ms": score_ms,
+                    "avg_precision": score["avg_precision"], "avg_recall": score["avg_recall"]},
     }
     if not args.no_cpu_baseline:
         sys.path.insert(0, ORACLE_DIR)

@@ -467,26 +467,30 @@ def modularity(g: DeviceGraph, resolution: float, labels) -> float:
     return float(out.value)
 
 
-def compare_communities(ctx: "Context", labels, communities):
+def compare_communities(ctx: "Context", labels, communities=None, offsets=None, members=None):
     """Ground-truth scoring (CompareCommunities, cluster-in-memory_main.cc:
-    172-225) on the device.  communities: a list of vertex-id sequences.
-    Returns (scores dict, precision per community, recall per community)."""
+    172-225) on the device.  communities: a list of vertex-id sequences, or
+    offsets (uint64[C+1]) and members (uint32) in CSR form.  Returns (scores
+    dict, precision per community, recall per community)."""
     lab = _u32(labels)
-    sizes = [len(c) for c in communities]
-    off = np.zeros(len(communities) + 1, np.uint64)
-    off[1:] = np.cumsum(sizes, dtype=np.uint64)
-    mem = (np.concatenate([np.asarray(c, np.uint32) for c in communities]) if sum(sizes)
-           else np.zeros(1, np.uint32))
-    mem = np.ascontiguousarray(mem, np.uint32)
-    prec = np.zeros(max(len(communities), 1), np.float64)
-    rec = np.zeros(max(len(communities), 1), np.float64)
+    if communities is not None:
+        sizes = [len(c) for c in communities]
+        offsets = np.zeros(len(communities) + 1, np.uint64)
+        offsets[1:] = np.cumsum(sizes, dtype=np.uint64)
+        members = (np.concatenate([np.asarray(c, np.uint32) for c in communities]) if sum(sizes)
+                   else np.zeros(1, np.uint32))
+    off = np.ascontiguousarray(offsets, np.uint64)
+    mem = np.ascontiguousarray(members if len(members) else np.zeros(1, np.uint32), np.uint32)
+    nc = off.size - 1
+    prec = np.zeros(max(nc, 1), np.float64)
+    rec = np.zeros(max(nc, 1), np.float64)
     out = PccCommunityScores()
-    ctx.check(ctx.lib.pcc_compare_communities(ctx.handle, lab.size, _ptr(lab, ctypes.c_uint32), len(communities),
+    ctx.check(ctx.lib.pcc_compare_communities(ctx.handle, lab.size, _ptr(lab, ctypes.c_uint32), nc,
                                               _ptr(off, ctypes.c_uint64), _ptr(mem, ctypes.c_uint32),
                                               _ptr(prec, ctypes.c_double), _ptr(rec, ctypes.c_double),
                                               ctypes.byref(out)))
     scores = {name: getattr(out, name) for name, _ in out._fields_}
-    return scores, prec[:len(communities)], rec[:len(communities)]
+    return scores, prec[:nc], rec[:nc]
 
 
 def best_moves(g: DeviceGraph, config: PccConfig, cluster_ids, cluster_sizes, node_weights,
