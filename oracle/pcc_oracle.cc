@@ -477,6 +477,104 @@ std::vector<uint8_t> ClusterMoves(const Graph& g, Helper& h, const Options& o,
   return MoveNodesToCluster(h, moves, moved_count);
 }
 
+// ClusteringHelper::BestMove(moving_nodes) (internal.cc:644-707) with
+// BestMoveFromStats (correlation-clusterer-util.h:70-113) on live state, for
+// a moving set whose members share one cluster c (the async cluster-move
+// step): class-2 entries (both ends moving) never cross clusters; class-1
+// entries to c itself count as currently together.  Returns (target, value)
+// with target == n for "no cluster" (nullopt).
+Move BestMoveSet(const Graph& g, const Helper& h, const std::vector<uint32_t>& members,
+                 const std::vector<uint8_t>& moving, const Options& o, SumTable& after) {
+  const uint32_t c = h.C[members[0]];
+  uint64_t deg = 0;
+  for (uint32_t v : members) deg += g.degree(v);
+  after.Reset(deg);
+  double weight = 0, weight_c = 0, together = 0;
+  for (uint32_t v : members) {
+    weight_c += h.k[v];
+    weight += h.k[v];
+    for (uint64_t j = g.off[v]; j < g.off[v + 1]; ++j) {
+      const uint32_t u = g.nbr[j];
+      const float wf = static_cast<float>(static_cast<double>(g.weight(j)) - o.offset);
+      if (moving[u]) continue;  // class 2: both ends in c
+      const uint32_t cu = h.C[u];
+      if (cu == c) together += static_cast<double>(wf);
+      after.Add(cu, static_cast<double>(wf));
+    }
+  }
+  auto half_square = [](double x) { return x * x / 2; };
+  double change = 0;
+  change += 0.0 / 2 - o.res * (half_square(weight) - half_square(weight_c));
+  change -= together - o.res * (weight_c * (h.K[c] - weight_c));
+  Move best{g.n, change};
+  uint32_t best_id = kNone;
+  for (uint32_t slot : after.used) {
+    const uint32_t d = after.keys[slot];
+    const double moving_d = d == c ? weight_c : 0.0;  // cluster_moving_weights[d]
+    const double val = change + (after.vals[slot] - o.res * (weight * (h.K[d] - moving_d)));
+    if (val > best.value || (val == best.value && best_id != kNone && d < best_id)) {
+      best_id = d;
+      best.value = val;
+    }
+  }
+  if (best_id != kNone) best.target = best_id;
+  return best;
+}
+
+// The async branch of the DEFAULT_CLUSTER_MOVES block (parallel-correlation-
+// clusterer.cc:255-268): AsyncMove(moving_nodes) (internal.cc:405-446) for
+// every cluster of the clustering after the round's vertex moves, restated
+// sequentially in cluster order (each move sees the ones before it).  A
+// one-member set takes the vertex AsyncMove; a larger one moves whole when
+// its value is positive, with the moving weight summed in FP32 (the
+// reference's delayed_seq<float>), to a new cluster by the linear probe
+// from its own id.  The moved flags are set at the members' vertex ids, as
+// the reference does.
+void AsyncClusterMoves(const Graph& g, Helper& h, const Options& o,
+                       std::vector<uint8_t>& moved_clusters, Counters& ctr) {
+  const uint32_t n = g.n;
+  const std::vector<std::vector<uint32_t>> groups = GroupsById(h.C);
+  std::vector<uint8_t> additional(n, 0), moving(n, 0);
+  Scratch sc;
+  for (const std::vector<uint32_t>& members : groups) {
+    bool moved = false;
+    if (members.size() == 1) {
+      moved = AsyncMove(g, h, members[0], o, sc);
+    } else {
+      for (uint32_t v : members) moving[v] = 1;
+      const Move mv = BestMoveSet(g, h, members, moving, o, sc.table);
+      for (uint32_t v : members) moving[v] = 0;
+      if (mv.value > 0) {
+        const uint32_t cur = h.C[members[0]];
+        const uint32_t size = static_cast<uint32_t>(members.size());
+        std::vector<float> wts(members.size());
+        for (size_t i = 0; i < members.size(); ++i) wts[i] = static_cast<float>(h.k[members[i]]);
+        const float total = BlockedReduce(wts.data(), wts.size(), [](float a, float b) { return a + b; });
+        h.s[cur] -= size;
+        h.K[cur] += -1 * total;
+        uint32_t dest = mv.target;
+        if (dest != n) {
+          h.s[dest] += size;
+          h.K[dest] += total;
+        } else {
+          uint64_t i = cur;
+          while (h.s[i] != 0) i = (i + 1) % n;
+          dest = static_cast<uint32_t>(i);
+          h.s[dest] = size;
+          h.K[dest] += total;
+        }
+        for (uint32_t v : members) h.C[v] = dest;
+        moved = true;
+      }
+    }
+    if (moved) {
+      ctr.moves += members.size();
+      for (uint32_t v : members) additional[v] = 1;
+    }
+  }
+  for (uint32_t i = 0; i < n; ++i) moved_clusters[i] |= additional[i];
+}
+
 // N(marked) via gbbs::edgeMap with the always-true functor
 // (parallel-correlation-clusterer.cc:46-55, 312-331): every neighbour of a
 // marked vertex, as an ascending list.
@@ -543,6 +641,7 @@ std::vector<uint32_t> BestMovesForVertexSubset(const Graph& g, Helper& h,
       moved_count += local;
     }
     ctr.moves += moved_count.load();
+    if (o.whole_clusters) AsyncClusterMoves(g, h, o, moved_clusters, ctr);
   } else {
     std::vector<uint32_t> moves(n, kNone);
 #pragma omp parallel num_threads(NumThreads())
@@ -750,9 +849,7 @@ int RefineClustersSubroutine(const Graph& graph, const pcc_config& cfg,
     num_iterations = cfg.louvain_num_iterations > 0 ? cfg.louvain_num_iterations : 10;
     num_inner = cfg.louvain_num_inner_iterations > 0 ? cfg.louvain_num_inner_iterations : 10;
   } else if (cfg.clustering_moves_method == PCC_DEFAULT_CLUSTER_MOVES) {
-    // One level of up to num_iterations rounds (:487-492).  The async
-    // variant (AsyncMove(moving_nodes), internal.cc:405-446) is not restated.
-    if (cfg.async) return PCC_UNIMPLEMENTED;
+    // One level of up to num_iterations rounds (:487-492).
     num_iterations = 1;
     num_inner = cfg.num_iterations > 0 ? cfg.num_iterations : 20;
   } else {

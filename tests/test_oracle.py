@@ -205,15 +205,16 @@ def test_move_nodes_new_cluster_ids():
     assert mod.tolist() == [1, 1, 1, 1, 0, 1]
 
 
-def test_oracle_async_cluster_moves_unimplemented():
-    """DEFAULT_CLUSTER_MOVES with async moves (AsyncMove(moving_nodes)) is not
-    restated; the oracle answers UNIMPLEMENTED like the GPU library."""
+def test_oracle_async_cluster_moves():
+    """Async whole-cluster moves: two triangles joined by an edge end as the
+    two triangles (the vertex moves form them; no whole-cluster move pays)."""
     g = _csr(6, [(0, 1), (1, 2), (0, 2), (3, 4), (4, 5), (3, 5), (2, 3)])
     og = O.OracleGraph(g)
-    cfg = P.make_config(resolution=0.1, clustering_moves_method=P.DEFAULT_CLUSTER_MOVES, async_=True)
-    with pytest.raises(Exception) as e:
-        O.correlation_cluster(og, cfg)
-    assert "12" in str(e.value) or "UNIMPLEMENTED" in str(e.value)
+    for seed in range(3):
+        cfg = P.make_config(resolution=0.3, clustering_moves_method=P.DEFAULT_CLUSTER_MOVES, async_=True,
+                            random_seed=seed + 1)
+        lab, st = O.correlation_cluster(og, cfg)
+        assert lab[0] == lab[1] == lab[2] and lab[3] == lab[4] == lab[5] and lab[0] != lab[3], lab
 
 
 def _blocked_sum(xs):
