@@ -199,6 +199,24 @@ def test_edge_cases(ctx):
     assert lab.tolist() == [0] and st["num_clusters"] == 1
 
 
+def test_c1_sbm10k_config_bit_exact(ctx):
+    """The CPU-runnable config exactly: SBM n = 10,000, 50 blocks of
+    uniform-multinomial sizes, p_in 0.05, p_out 0.0005, unit weights (mean
+    degree 14.9); correlation, resolution 0.01, refine, sync, ALL_MOVE, 10 x 10
+    iterations.  Labels, counters and objective equal the oracle's."""
+    g, _ = G.sbm(10000, 50, 0.05, 0.0005, 1)
+    dg, og = _both(ctx, g)
+    cfg = P.make_config(resolution=0.01, refine=True, move_method=P.ALL_MOVE, louvain_num_iterations=10,
+                        louvain_num_inner_iterations=10)
+    lab_g, st_g = P.correlation_cluster(dg, cfg)
+    lab_o, st_o = O.correlation_cluster(og, cfg)
+    np.testing.assert_array_equal(lab_g, lab_o)
+    assert st_g["edge_visits"] == st_o["edge_visits"]
+    assert st_g["rounds"] == st_o["rounds"]
+    assert st_g["levels"] == st_o["levels"]
+    assert st_g["objective"] == pytest.approx(st_o["objective"], rel=REL_TOL, abs=1e-9)
+
+
 # Whole-cluster moves (DEFAULT_CLUSTER_MOVES): one level of num_iterations
 # rounds, each with vertex moves then whole-cluster moves.  With refine the
 # reference's level loop returns the identity clustering (a single level has
