@@ -46,6 +46,16 @@ def test_parse_full_config(built):
     assert cfg.move_method == P.ALL_MOVE
 
 
+def test_parse_whole_cluster_moves(built):
+    """DEFAULT_CLUSTER_MOVES with its round count (num_iterations) reaches the
+    library config as the engine reads it."""
+    cfg, _ = G.parse_config("correlation_clusterer_config { resolution: 0.2 "
+                            "clustering_moves_method: DEFAULT_CLUSTER_MOVES num_iterations: 6 "
+                            "move_method: NBHR_MOVE }")
+    assert cfg.clustering_moves_method == P.DEFAULT_CLUSTER_MOVES
+    assert cfg.num_iterations == 6 and cfg.move_method == P.NBHR_MOVE and cfg.resolution == 0.2
+
+
 def test_parse_defaults_and_numbers(built):
     cfg, case = G.parse_config("")
     assert case == 0
