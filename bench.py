@@ -14,8 +14,12 @@ round, level and refinement pass, identically to the oracle.
           HBM (CUDA events on the library's stream, summed over the steps)
   e2e     the same metric through pcc_cluster_host_csr on pinned host
           buffers: upload + cluster + label download every step
-  --impl reference   the oracle (the CPU restatement of the reference
-          clusterer) on the host cores, same config, bounded sample
+  cpu_baseline   the oracle (the CPU restatement of the reference
+          clusterer) on all host cores: one clustering of the same graph
+          with the same config; its labels pin the GPU's (quality.oracle)
+  --impl reference   the same oracle timed per step on the same graph and
+          config; it generates the graph itself and loads no library of the
+          GPU package
 
 Three more workloads ride on the same JSON line (rank 0, one GPU each):
   lfr       LFR-like graph, 8M vertices, real weights (FP64 mode), in the
@@ -67,7 +71,7 @@ def parse_args():
     ap.add_argument("--scale", type=int, default=22)
     ap.add_argument("--async", dest="async_", action="store_true")
     ap.add_argument("--cpu-scale", type=int, default=20,
-                    help="RMAT scale of the bounded CPU-baseline sample")
+                    help="RMAT scale of the async-quality comparison with the oracle (5 seeds each)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-graphs", type=int, default=4096,
                     help="graphs of the batched SBM leg (0 = skip the leg)")
@@ -167,25 +171,103 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_baseline(args, P, G):
-    """The oracle on the host cores, bounded sample: the same config on an
-    RMAT graph of scale --cpu-scale (edge visits/s is size-normalised)."""
+def phases(st, bpe):
+    """Per-phase device time of one clustering run with detailed timing, with
+    the algorithmic GB/s of best moves, compression and the frontier push."""
+    peak, _ = measured_peak()
+
+    def rate(byts, ms):
+        if not byts or not ms:
+            return None, None
+        gbs = byts / (ms / 1000.0) / 1e9
+        return gbs, gbs / peak
+
+    out = {"note": "one clustering with detailed timing (host-driven rounds, CUDA events per phase)",
+           "total": st["ms_total"]}
+    for name, key, byts in (("best_moves", "ms_best_moves", st["algo_bytes_best_moves"]),
+                            ("compress", "ms_compress", st["algo_bytes_compress"]),
+                            ("apply", "ms_apply", None),
+                            ("frontier", "ms_frontier", st["algo_bytes_frontier"])):
+        gbs, frac = rate(byts, st[key])
+        out[name] = {"ms": st[key], "algo_bytes": byts, "achieved_gbs": gbs, "frac": frac}
+    out["bytes_rule"] = {"best_moves": f"{bpe} B per entry + 40 B per vertex evaluated",
+                         "compress": "(12 or 8) m + 8 m' + 20 n + 16 n' per contraction",
+                         "frontier": "4 B per entry of each expanded row + 4 B per expanded row"}
+    return out
+
+
+def families(P, st, bpe, peak):
+    """Best-move kernel families of one detailed-timing run: device time,
+    launches and algorithmic GB/s ({bpe} B per entry + 40 B per vertex)."""
+    out = {}
+    for f, name in enumerate(P.PccStats.FAMILIES):
+        ms, nl = st["family_ms"][f], st["family_launches"][f]
+        if ms <= 0 or nl == 0:
+            continue
+        byts = bpe * st["family_entries"][f] + 40 * st["family_vertices"][f]
+        gbs = byts / (ms / 1000.0) / 1e9
+        out[name] = {"ms_per_step": ms, "launches_per_step": nl, "entries_per_step": st["family_entries"][f],
+                     "achieved_gbs": gbs, "frac": gbs / peak}
+    return out
+
+
+def cpu_baseline(args, P, g, gpu_labels, gpu_stats):
+    """The oracle on all host cores: one full clustering of the bench's own
+    graph with the same config (about 15-20 s of CPU work on 16 cores).  Its
+    labels and modularity also pin the GPU result of the timed steps: sync
+    moves on a unit-weight graph must give identical labels."""
+    import numpy as np
     sys.path.insert(0, ORACLE_DIR)
     import oracle as O
     O.set_threads(0)
     threads = O.get_threads()
-    g = G.rmat(args.cpu_scale, 16, seed=1)
     og = O.OracleGraph(g)
     cfg = make_cfg(P, args)
     t = time.perf_counter()
-    _, st = O.modularity_cluster(og, cfg)
+    labels, st = O.modularity_cluster(og, cfg)
     dt = time.perf_counter() - t
-    return {
+    cpu = {
         "value": st["edge_visits"] / dt, "unit": UNIT, "cores": threads, "kind": "port",
-        "sample": f"one full clustering of RMAT scale {args.cpu_scale} (n={g.n}, m={g.m}) with the same "
-                  f"config; {st['edge_visits']} edge visits in {dt:.2f} s",
-        "modularity": st["modularity"],
+        "sample": f"one full clustering of the bench graph (RMAT scale {args.scale}, n={g.n}, m={g.m}) with the "
+                  f"same config; {st['edge_visits']} edge visits in {dt:.2f} s",
     }
+    same = bool(np.array_equal(labels, gpu_labels))
+    parity = {
+        "oracle_modularity": st["modularity"], "gpu_modularity": gpu_stats["modularity"],
+        "labels_identical": same,
+        "differing_labels": int((labels != gpu_labels).sum()),
+        "edge_visits_equal": st["edge_visits"] == gpu_stats["edge_visits"],
+        "rounds_equal": st["rounds"] == gpu_stats["rounds"],
+        "levels_equal": st["levels"] == gpu_stats["levels"],
+    }
+    return cpu, parity
+
+
+def async_quality(args, P, G, ctx, seeds: int = 5):
+    """Async mode is nondeterministic (in the reference too): the GPU's mean
+    modularity over seeds beside the oracle's, on RMAT scale --cpu-scale with
+    the headline config in async mode.  Each GPU modularity is recomputed by
+    the oracle from the GPU's labels."""
+    import numpy as np
+    sys.path.insert(0, ORACLE_DIR)
+    import oracle as O
+    O.set_threads(0)
+    g = G.rmat(args.cpu_scale, 16, seed=1)
+    og = O.OracleGraph(g)
+    dg = ctx.upload(g)
+    gpu, cpu = [], []
+    for seed in range(1, seeds + 1):
+        cfg = P.make_config(resolution=1.0, refine=True, move_method=P.NBHR_MOVE, async_=True, random_seed=seed)
+        lab, _ = P.modularity_cluster(dg, cfg)
+        gpu.append(O.modularity(og, 1.0, lab))
+        _, so = O.modularity_cluster(og, cfg)
+        cpu.append(so["modularity"])
+    dg.free()
+    mg, mc = float(np.mean(gpu)), float(np.mean(cpu))
+    return {"graph": f"RMAT scale {args.cpu_scale} (n={g.n}, m={g.m})", "seeds": seeds,
+            "gpu_mean_modularity": mg, "oracle_mean_modularity": mc,
+            "relative_difference": (mg - mc) / abs(mc) if mc else None,
+            "gpu": gpu, "oracle": cpu}
 
 
 def batched_leg(args, P, G, ctx):
@@ -242,6 +324,11 @@ def lfr_leg(args, P, G, ctx, dist_steps: int = 2):
         labels, st = P.correlation_cluster(dg, cfg)
         ev += st["edge_visits"]
         ms += st["ms_total"]
+    # One more clustering with detailed timing: the phase and family split.
+    detailed = ctx.detailed_timing
+    ctx.set_detailed_timing(True)
+    _, sd = P.correlation_cluster(dg, cfg)
+    ctx.set_detailed_timing(detailed)
     dg.free()
     # Ground-truth scoring (CompareCommunities) of the clustering against the
     # planted communities, on the device; host arrays in, report out.
@@ -257,9 +344,9 @@ def lfr_leg(args, P, G, ctx, dist_steps: int = 2):
         "n": g.n, "m_entries": g.m, "dtype": "f64 (real weights: FP64 best moves)",
         "value": ev / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / dist_steps,
         "objective": st["objective"], "num_clusters": st["num_clusters"], "levels": st["levels"],
-        "rounds": st["rounds"],
-        "phases_ms_per_step": {"best_moves": st["ms_best_moves"], "compress": st["ms_compress"],
-                               "apply": st["ms_apply"], "frontier": st["ms_frontier"]},
+        "rounds": st["rounds"], "mean_degree": g.m / g.n,
+        "phases_ms_per_step": phases(sd, bpe=12),
+        "kernel_families": families(P, sd, 12, measured_peak()[0]),
         "scoring": {"what": "CompareCommunities on the device against the planted communities "
                             "(pcc_compare_communities, host arrays in and out)",
                     "communities": int(comm_off.size - 1), "ms": score_ms,
@@ -374,21 +461,25 @@ def reduce_over_ranks(dist, to_max, to_sum, device):
 
 
 def run_reference(args):
-    """--impl reference: the oracle port on all host threads; rank 0 only."""
+    """--impl reference: the oracle (the CPU restatement of the reference
+    clusterer) on all host threads, rank 0 only.  Each step is one full
+    clustering of the GPU arm's graph (RMAT scale --scale) with the GPU arm's
+    config.  The graph comes from the oracle's own generator, so this process
+    loads no library of the GPU package (the package's Python module is
+    imported for its ctypes struct definitions only)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import pcc_gb300 as P
-    import pcc_graphs as G
     sys.path.insert(0, ORACLE_DIR)
     import oracle as O
-    import build_native
-    build_native.build_host()
+    import pcc_gb300 as P
     O.build()
     O.set_threads(0)
     threads = O.get_threads()
-    g = G.rmat(args.cpu_scale, 16, seed=1)
-    og = O.OracleGraph(g)
+    t = time.perf_counter()
+    og = O.rmat(args.scale, 16, seed=1)
+    gen_s = time.perf_counter() - t
+    n, m = og.info()
     cfg = make_cfg(P, args)
     for _ in range(args.warmup):
         O.modularity_cluster(og, cfg)
@@ -402,16 +493,17 @@ def run_reference(args):
         total_ev += st["edge_visits"]
         mod = st["modularity"]
     value = total_ev / total_t
-    sample = (f"each step one full clustering of RMAT scale {args.cpu_scale} (n={g.n}, m={g.m}), "
-              f"same config as the GPU arm (scale {args.scale})")
+    sample = (f"each step one full clustering of RMAT scale {args.scale} (n={n}, m={m}), the GPU arm's graph "
+              f"and config, generated by the oracle in {gen_s:.1f} s (not timed)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total_t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded RMAT generator)", "config": config_dict(args, g.n, g.m),
+        "data": "synthetic (seeded RMAT generator)", "config": config_dict(args, n, m),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "quality": {"modularity": mod},
+        "quality": {"modularity": mod, "edge_visits_per_step": total_ev // max(args.steps, 1)},
+        "parity": "unpinned-vs-binary (the reference cannot be built here); this arm is the oracle restatement",
     }
     print(json.dumps(line), flush=True)
 
@@ -461,10 +553,8 @@ def main():
     vv = 0
     dev_ms = 0.0
     bm_ms = 0.0
-    comp_ms = 0.0
-    apply_ms = 0.0
-    front_ms = 0.0
     algo_bytes = 0
+    labels = last_stats = None
     launches = 0
     fam_ms = [0.0] * 4
     fam_launch = [0] * 4
@@ -473,6 +563,7 @@ def main():
     quality = {}
     for _ in range(args.steps):
         labels, st = P.modularity_cluster(dg, cfg)
+        last_stats = st
         ev += st["edge_visits"]
         vv += st["vertex_visits"]
         dev_ms += st["ms_total"]
@@ -488,13 +579,10 @@ def main():
     # every phase and best-move kernel family) gives the breakdown and the
     # per-launch figures of the roofline.
     ctx.set_detailed_timing(True)
-    _, st = P.modularity_cluster(dg, cfg)
+    _, st_detail = P.modularity_cluster(dg, cfg)
     ctx.set_detailed_timing(args.detailed_timing)
-    detailed_ms = st["ms_total"]
+    st = st_detail
     bm_ms = st["ms_best_moves"]
-    comp_ms = st["ms_compress"]
-    apply_ms = st["ms_apply"]
-    front_ms = st["ms_frontier"]
     algo_bytes = st["algo_bytes_best_moves"]
     for f in range(4):
         fam_ms[f] = st["family_ms"][f]
@@ -540,6 +628,11 @@ def main():
         c_mod = st["modularity"]
     barrier()
 
+    # Async quality against the oracle (rank 0; RMAT scale --cpu-scale).
+    async_check = None
+    if rank == 0 and not args.no_cpu_baseline:
+        async_check = async_quality(args, P, G, ctx)
+
     # Batched and serving workloads (rank 0; one GPU each).
     batched = serving = lfr = None
     if rank == 0 and args.lfr_n > 0:
@@ -579,11 +672,13 @@ def main():
         traffic_per_entry = TRAFFIC_BYTES_PER_ENTRY.get(names[top])
         traffic = (traffic_per_entry * fam_e[top] / max(fam_launch[top], 1)) if traffic_per_entry else None
         cpu = None
+        pinning = None
         if not args.no_cpu_baseline:
             try:
-                cpu = cpu_baseline(args, P, G)
+                cpu, pinning = cpu_baseline(args, P, g, labels, last_stats)
             except Exception as e:  # the baseline is reported, never required
                 cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {e}"}
+
         line = {
             "metric": METRIC, "value": ev_all / dev_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
@@ -602,14 +697,17 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clocks,
             "gpu_launches": launches,
-            "phases_ms_per_step": {"note": "one clustering with detailed timing (host-driven rounds)",
-                                   "total": detailed_ms, "best_moves": bm_ms,
-                                   "compress": comp_ms, "apply": apply_ms, "frontier": front_ms},
+            "phases_ms_per_step": phases(st_detail, bpe),
             "wall_s": wall,
-            "quality": quality,
+            "quality": dict(quality, **({"oracle": pinning} if pinning else {})),
+            "parity": "unpinned-vs-binary (the reference cannot be built here), "
+                      + ("bit-exact-vs-oracle on this graph" if pinning and pinning["labels_identical"]
+                         else "checked against the oracle on this graph: see quality.oracle"
+                         if pinning else "not checked in this run"),
             "modes": {"async": {"value": a_ev / (a_ms / 1000.0) if a_ms > 0 else None, "unit": UNIT,
                                 "ms_per_step": a_ms / args.steps, "modularity_mean": sum(a_mod) / len(a_mod),
                                 "note": "same graph and config with async=true, 16 waves per round"},
+                      "async_quality": async_check,
                       "cluster_moves": {"value": c_ev / (c_ms / 1000.0) if c_ms > 0 else None, "unit": UNIT,
                                         "ms_per_step": c_ms / c_steps if c_steps else None, "modularity": c_mod,
                                         "note": "same graph, clustering_moves_method DEFAULT_CLUSTER_MOVES "

@@ -112,6 +112,13 @@ typedef struct pcc_stats {
   uint64_t family_launches[4];
   uint64_t family_entries[4];
   uint64_t family_vertices[4];
+  /* Algorithmic bytes of graph compression: (12, or 8 without weights) per
+     input entry + 8 per output entry + 20 per input vertex + 16 per output
+     vertex, summed over the contractions. */
+  uint64_t algo_bytes_compress;
+  /* Algorithmic bytes of the frontier push with detailed timing on (0 off):
+     4 per entry of every expanded row + 4 per expanded row. */
+  uint64_t algo_bytes_frontier;
 } pcc_stats;
 
 void pcc_config_default(pcc_config* config);
@@ -424,8 +431,9 @@ void pcc_server_destroy(pcc_server* server);
  *   stream        cudaStream_t (NULL = default stream) of the current device
  *
  * Runs on the current device.  The first call on a device resolves the
- * scratch address and must come before any stream capture.  The call
- * synchronises `stream` to read its status.  Calls that overlap in time on
+ * scratch address (cudaGetSymbolAddress); make that first call before any
+ * stream capture begins.  Every call synchronises `stream` and copies a
+ * status word to the host before it returns.  Calls that overlap in time on
  * one device share the scratch and race: serialise them.  Sums use FP64
  * atomics: equal to pcc_best_moves on integer weights, within rounding on
  * real weights.

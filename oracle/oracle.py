@@ -81,6 +81,9 @@ def lib():
                                                P(ctypes.c_uint64), P(ctypes.c_uint32),
                                                P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]
         L.pcco_compress.restype = vp
+        L.pcco_gen_rmat.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_double, ctypes.c_uint64]
+        L.pcco_gen_rmat.restype = vp
         _lib = L
     return _lib
 
@@ -216,6 +219,14 @@ def compress(g: OracleGraph, C, node_weights=None):
     h = lib().pcco_compress(g.h, _p(C, ctypes.c_uint32), _p(k, ctypes.c_double))
     og = OracleGraph(handle=h)
     return og.to_csr()
+
+
+def rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+         seed: int = 1) -> OracleGraph:
+    """Seeded RMAT graph built inside the oracle (symmetrised, deduplicated,
+    no self-loops, unit weights): the same graph as the package's generator
+    for the same arguments, without loading any library of the package."""
+    return OracleGraph(handle=lib().pcco_gen_rmat(scale, edge_factor, a, b, c, seed))
 
 
 def compare_communities(labels, communities):

@@ -981,6 +981,92 @@ void FillStats(const ClusterResult& r, pcc_stats* st) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// Seeded RMAT input for the CPU baseline.  Input generation, not part of the
+// restated algorithm: it yields the same graph as the package's host
+// generator (pcch_gen_rmat) from the same seed, written independently so a
+// process that times the oracle loads no library of the GPU package.  The
+// sample stream is a counter-based SplitMix64 hash of (seed, sample, level
+// pair); each level picks a quadrant with probabilities a, b, c, 1-a-b-c.
+// The CSR is symmetrised, self-loops dropped, rows sorted by neighbour id
+// and deduplicated.  A CPU test checks the two generators agree entry for
+// entry.
+// ---------------------------------------------------------------------------
+namespace {
+
+inline uint64_t Mix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+inline uint64_t SampleHash(uint64_t seed, uint64_t sample, uint64_t level) {
+  return Mix64(Mix64(seed ^ Mix64(sample)) ^ (level * 0xD6E8FEB86659FD93ull));
+}
+
+Graph RmatGraph(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                uint64_t seed) {
+  Graph g;
+  g.n = scale >= 32 ? 0xFFFFFFFFu : (1u << scale);
+  const uint64_t samples = uint64_t(edge_factor) << scale;
+  const double ab = a + b, abc = a + b + c;
+  std::vector<uint32_t> su(samples), sv(samples);
+#pragma omp parallel for schedule(static) num_threads(NumThreads())
+  for (int64_t e = 0; e < int64_t(samples); ++e) {
+    uint32_t u = 0, v = 0;
+    uint64_t h = 0;
+    for (uint32_t l = 0; l < scale; ++l) {
+      if (l % 2 == 0) h = SampleHash(seed, uint64_t(e), l);
+      const uint32_t word = l % 2 ? uint32_t(h >> 32) : uint32_t(h & 0xFFFFFFFFu);
+      const double x = double(word) / 4294967296.0;
+      const uint32_t qu = x < ab ? 0u : 1u;
+      const uint32_t qv = (x < a || (x >= ab && x < abc)) ? 0u : 1u;
+      u = 2 * u + qu;
+      v = 2 * v + qv;
+    }
+    su[e] = u;
+    sv[e] = v;
+  }
+  // Both directions of every non-loop sample, bucketed by source row.
+  std::vector<uint64_t> cnt(size_t(g.n) + 1, 0);
+#pragma omp parallel for schedule(static) num_threads(NumThreads())
+  for (int64_t e = 0; e < int64_t(samples); ++e) {
+    if (su[e] == sv[e]) continue;
+    __atomic_fetch_add(&cnt[su[e]], 1, __ATOMIC_RELAXED);
+    __atomic_fetch_add(&cnt[sv[e]], 1, __ATOMIC_RELAXED);
+  }
+  std::vector<uint64_t> start(size_t(g.n) + 1, 0);
+  for (uint32_t i = 0; i < g.n; ++i) start[i + 1] = start[i] + cnt[i];
+  std::vector<uint32_t> bucket(start[g.n]);
+  std::vector<uint64_t> fill(start.begin(), start.end() - 1);
+#pragma omp parallel for schedule(static) num_threads(NumThreads())
+  for (int64_t e = 0; e < int64_t(samples); ++e) {
+    if (su[e] == sv[e]) continue;
+    bucket[__atomic_fetch_add(&fill[su[e]], 1, __ATOMIC_RELAXED)] = sv[e];
+    bucket[__atomic_fetch_add(&fill[sv[e]], 1, __ATOMIC_RELAXED)] = su[e];
+  }
+  // Sort and deduplicate each row in place; then pack the rows.
+  std::vector<uint64_t> deg(g.n, 0);
+#pragma omp parallel for schedule(dynamic, 512) num_threads(NumThreads())
+  for (int64_t i = 0; i < int64_t(g.n); ++i) {
+    uint32_t* r = bucket.data() + start[i];
+    const size_t len = start[i + 1] - start[i];
+    std::sort(r, r + len);
+    deg[i] = size_t(std::unique(r, r + len) - r);
+  }
+  g.off.assign(size_t(g.n) + 1, 0);
+  for (uint32_t i = 0; i < g.n; ++i) g.off[i + 1] = g.off[i] + deg[i];
+  g.m = g.off[g.n];
+  g.nbr.resize(g.m);
+#pragma omp parallel for schedule(dynamic, 512) num_threads(NumThreads())
+  for (int64_t i = 0; i < int64_t(g.n); ++i)
+    std::copy(bucket.begin() + start[i], bucket.begin() + start[i] + deg[i], g.nbr.begin() + g.off[i]);
+  return g;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
 // C ABI of the oracle (ctypes from tests/ and bench.py).
 // ---------------------------------------------------------------------------
 extern "C" {
@@ -1196,6 +1282,13 @@ pcco_graph* pcco_compress(const pcco_graph* g, const uint32_t* C,
   if (k) kk.assign(k, k + g->g.n);
   auto* out = new pcco_graph;
   out->g = CompressGraph(g->g, c, kk);
+  return out;
+}
+
+pcco_graph* pcco_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                          uint64_t seed) {
+  auto* out = new pcco_graph;
+  out->g = RmatGraph(scale, edge_factor, a, b, c, seed);
   return out;
 }
 

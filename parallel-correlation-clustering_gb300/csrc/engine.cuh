@@ -148,6 +148,10 @@ struct DevCounters {
   // Accumulated by the device-side round loop (sync mode).
   unsigned long long sync_moves;     // real movers over the loop's rounds
   unsigned long long visited;        // vertices evaluated over the loop's rounds
+  // Detailed timing only: rows the frontier push expanded and their entries,
+  // over the call (algorithmic bytes of the push).
+  unsigned long long push_entries;
+  unsigned long long push_rows;
 };
 
 constexpr int kErrProbeLimit = 1;   // async new-cluster probe exceeded its bound

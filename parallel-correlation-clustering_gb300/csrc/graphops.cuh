@@ -207,11 +207,11 @@ __global__ void __launch_bounds__(256) BinCountKernel(uint32_t n, const uint64_t
 }
 
 // Number and degree sum of the vertices satisfying pred (one pass over n).
-template <class P>
+template <class P, class CountT = uint32_t>
 __global__ void __launch_bounds__(256) CountDegreesKernel(uint32_t n, const uint64_t* __restrict__ off, P pred,
-                                                          unsigned long long* deg_sum, uint32_t* vcount) {
+                                                          unsigned long long* deg_sum, CountT* vcount) {
   unsigned long long dacc = 0;
-  uint32_t cnt = 0;
+  CountT cnt = 0;
   for (uint64_t v = uint64_t(blockIdx.x) * 256 + threadIdx.x; v < n; v += uint64_t(gridDim.x) * 256) {
     if (!pred(static_cast<uint32_t>(v))) continue;
     dacc += off[v + 1] - off[v];
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(256) CountDegreesKernel(uint32_t n, const uint
     cnt += __shfl_xor_sync(kFull, cnt, o);
   }
   __shared__ unsigned long long sd[8];
-  __shared__ uint32_t sc[8];
+  __shared__ CountT sc[8];
   if (LaneId() == 0) {
     sd[threadIdx.x >> 5] = dacc;
     sc[threadIdx.x >> 5] = cnt;
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(256) CountDegreesKernel(uint32_t n, const uint
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long t = 0;
-    uint32_t c = 0;
+    CountT c = 0;
     for (int w = 0; w < 8; ++w) {
       t += sd[w];
       c += sc[w];

@@ -419,6 +419,14 @@ struct PredModifiedCluster {  // NBHR_CLUSTER_MOVE: vertices of modified cluster
   __device__ bool operator()(uint32_t v) const { return mod_stamp[C[v]] == StampIn(rs, stamp); }
 };
 
+// Rows the frontier push expands: marked (pred) and not empty.
+template <class P>
+struct PredMarkedRow {
+  const uint64_t* off;
+  P pred;
+  __device__ bool operator()(uint32_t v) const { return off[v + 1] > off[v] && pred(v); }
+};
+
 // ---------------------------------------------------------------------------
 // Objective / modularity.
 // ---------------------------------------------------------------------------
@@ -562,6 +570,8 @@ struct RunResult {
   int32_t rounds = 0;
   int32_t refine_passes = 0;
   uint64_t algo_bytes = 0;
+  // CompressGraph: (12 or 8) m + 8 m' + 20 n + 16 n' per contraction.
+  uint64_t algo_bytes_compress = 0;
 };
 
 // INT mode with every neighbour-cluster sum below 2^30 in magnitude (so
@@ -575,6 +585,14 @@ bool NarrowSums(const DevGraph& g, double offset) {
 // over seeds within 0.15% of the reference restatement on SBM, RMAT and
 // LFR-like graphs, where one wave loses up to 1.6%.
 constexpr uint32_t kAsyncWaves = 16;
+
+// Algorithmic bytes of one contraction (CompressGraph): read the CSR and
+// gather C per entry ((4 + 4) or (4 + 4 + 4) B), write CSR' (8 B per entry),
+// read C and k per vertex (12 B) plus the offsets (8 B), write the offsets'
+// and k' (16 B per new vertex).
+uint64_t CompressBytes(const DevGraph& in, const DevGraph& out) {
+  return (in.w.p ? 12ull : 8ull) * in.m + 8ull * out.m + 20ull * in.n + 16ull * out.n;
+}
 
 bool IntModeFor(const DevGraph& g, double offset) {
   if (!g.integral) return false;
@@ -808,6 +826,21 @@ class Engine {
     }
     PCC_RETURN_IF_ERROR(LaunchCheck());
     timer_.End(kPhaseFrontier);
+    if (ctx_->detailed_timing && !rs && n) {
+      // Untimed: the rows the push expanded and their entries, for the
+      // frontier phase's algorithmic bytes.
+      if (cfg_.move_method == PCC_NBHR_CLUSTER_MOVE) {
+        const PredMarkedRow<PredModifiedCluster> pred{g.off.p, PredModifiedCluster{L->C.p, mod_stamp_.p, stamp_, rs}};
+        CountDegreesKernel<PredMarkedRow<PredModifiedCluster>, unsigned long long>
+            <<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g.off.p, pred, &ctr_.p->push_entries, &ctr_.p->push_rows);
+      } else {
+        const PredMarkedRow<PredStamp> pred{g.off.p, PredStamp{moved_stamp_.p, stamp_, rs}};
+        CountDegreesKernel<PredMarkedRow<PredStamp>, unsigned long long>
+            <<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g.off.p, pred, &ctr_.p->push_entries, &ctr_.p->push_rows);
+      }
+      PCC_COUNT(1);
+      PCC_RETURN_IF_ERROR(LaunchCheck());
+    }
     return Status::Ok();
   }
 
@@ -1070,6 +1103,7 @@ class Engine {
       timer_.Begin(kPhaseCompress);
       PCC_RETURN_IF_ERROR(CompressGraph(ctx_, *helper->g, helper->C.p, helper->k.p, &next));
       timer_.End(kPhaseCompress);
+      res_.algo_bytes_compress += CompressBytes(*helper->g, *next);
       DevGraph* ng = next.get();
       std::unique_ptr<Level> nl;
       PCC_RETURN_IF_ERROR(MakeLevel(ng, std::move(next), ng->node_w.p, false, nullptr, &nl));
@@ -1295,6 +1329,7 @@ class Engine {
       timer_.Begin(kPhaseCompress);
       PCC_RETURN_IF_ERROR(CompressGraph(ctx_, *helper->g, helper->C.p, helper->k.p, &next));
       timer_.End(kPhaseCompress);
+      res_.algo_bytes_compress += CompressBytes(*helper->g, *next);
       DevGraph* ng = next.get();
       if (ng->n <= u.vbase[B - 1]) return MakeError(PCC_INTERNAL, "union contraction lost a graph's range");
       std::unique_ptr<Level> nl;
@@ -1382,6 +1417,15 @@ class Engine {
   double PhaseMs(int k) const { return timer_.TotalMs(k); }
   double FamilyMs(int f) const { return fam_timer_.TotalMs(f); }
   // Family counters of the call (reads the device counters).
+  // Rows the frontier push expanded and their entries (detailed timing).
+  Status PushCounts(uint64_t* entries, uint64_t* rows) {
+    DevCounters hc;
+    PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
+    PCC_RETURN_IF_ERROR(Sync(ctx_));
+    *entries = hc.push_entries;
+    *rows = hc.push_rows;
+    return Status::Ok();
+  }
   Status FamilyCounts(uint64_t* entries, uint64_t* vertices) {
     DevCounters hc;
     PCC_RETURN_IF_ERROR(ctr_.ToHost(&hc, 1));
@@ -1600,6 +1644,10 @@ Status ClusterImpl(pcc_context* pctx, const pcc_graph* graph, const pcc_config* 
     stats->ms_frontier = eng.PhaseMs(kPhaseFrontier);
     stats->kernel_launches = LaunchCounter() - launches0;
     stats->algo_bytes_best_moves = eng.result().algo_bytes;
+    stats->algo_bytes_compress = eng.result().algo_bytes_compress;
+    uint64_t pe = 0, pr = 0;
+    PCC_RETURN_IF_ERROR(eng.PushCounts(&pe, &pr));
+    stats->algo_bytes_frontier = 4 * pe + 4 * pr;
     uint64_t fe[kNumFamilies], fv[kNumFamilies];
     PCC_RETURN_IF_ERROR(eng.FamilyCounts(fe, fv));
     for (int f = 0; f < kNumFamilies; ++f) {
@@ -1778,6 +1826,10 @@ Status UnionChunk(Context* ctx, const pcc_config& cfg, const std::vector<const p
     tot->ms_frontier += eng.PhaseMs(kPhaseFrontier);
     tot->kernel_launches += LaunchCounter() - launches0;
     tot->algo_bytes_best_moves += r.algo_bytes;
+    tot->algo_bytes_compress += r.algo_bytes_compress;
+    uint64_t pe = 0, pr = 0;
+    PCC_RETURN_IF_ERROR(eng.PushCounts(&pe, &pr));
+    tot->algo_bytes_frontier += 4 * pe + 4 * pr;
     uint64_t fe[kNumFamilies], fv[kNumFamilies];
     PCC_RETURN_IF_ERROR(eng.FamilyCounts(fe, fv));
     for (int f = 0; f < kNumFamilies; ++f) {

@@ -266,7 +266,9 @@ struct pcc_server {
   std::unique_ptr<Pool> pool;
   std::mutex mu;
   uint64_t next_ticket = 1;
-  std::unordered_map<uint64_t, std::unique_ptr<Request>> requests;
+  // Shared so that a waiter keeps its request alive after another waiter of
+  // the same ticket has collected and erased it.
+  std::unordered_map<uint64_t, std::shared_ptr<Request>> requests;
 };
 
 extern "C" {
@@ -374,7 +376,7 @@ pcc_status pcc_server_submit(pcc_server* server, uint32_t n, uint64_t m, const u
                              const pcc_config* config, int32_t objective, uint64_t* ticket) {
   if (!server || !offsets || (m && !neighbors) || !config || !ticket || (objective != 0 && objective != 1))
     return PCC_INVALID_ARGUMENT;
-  auto r = std::make_unique<Request>();
+  auto r = std::make_shared<Request>();
   r->n = n;
   r->m = m;
   r->off_own.assign(offsets, offsets + uint64_t(n) + 1);
@@ -393,7 +395,7 @@ pcc_status pcc_server_submit(pcc_server* server, uint32_t n, uint64_t m, const u
     std::lock_guard<std::mutex> lk(server->mu);
     r->ticket = server->next_ticket++;
     *ticket = r->ticket;
-    server->requests[r->ticket] = std::move(r);
+    server->requests[r->ticket] = r;
   }
   const pcc_status s = server->pool->Submit(raw);
   if (s != PCC_OK) {
@@ -407,14 +409,14 @@ pcc_status pcc_server_submit(pcc_server* server, uint32_t n, uint64_t m, const u
 pcc_status pcc_server_wait(pcc_server* server, uint64_t ticket, int32_t wait_ms, uint32_t* out_labels,
                            pcc_stats* stats, double* latency_ms, double* queue_ms) {
   if (!server) return PCC_INVALID_ARGUMENT;
-  Request* r = nullptr;
+  std::shared_ptr<Request> r;
   {
     std::lock_guard<std::mutex> lk(server->mu);
     auto it = server->requests.find(ticket);
     if (it == server->requests.end()) return PCC_NOT_FOUND;
-    r = it->second.get();
+    r = it->second;
   }
-  if (!server->pool->Wait(r, wait_ms)) return PCC_DEADLINE_EXCEEDED;
+  if (!server->pool->Wait(r.get(), wait_ms)) return PCC_DEADLINE_EXCEEDED;
   const pcc_status s = r->status;
   if (s == PCC_OK && out_labels && r->n) std::memcpy(out_labels, r->labels.data(), sizeof(uint32_t) * r->n);
   if (stats) *stats = r->stats;

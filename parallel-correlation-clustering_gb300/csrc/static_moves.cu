@@ -25,9 +25,10 @@
 // Scratch: kStaticSlots slots of (uint32 key, double sum), key = cluster + 1
 // (0 = empty), all zero between calls, plus one error word.  The first call
 // on a device resolves the array's address (cudaGetSymbolAddress) with that
-// device current and must come before any stream capture on it.  Calls that
-// overlap in time on one device (two host threads, two streams) share the
-// scratch and race; callers serialise them.
+// device current; make that first call before any stream capture begins.
+// Every call synchronises its stream and copies the error word to the host
+// before it returns.  Calls that overlap in time on one device (two host
+// threads, two streams) share the scratch and race; callers serialise them.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -227,12 +228,28 @@ __global__ void __launch_bounds__(kThreads) StaticBestMoveKernel(StaticArgs a) {
   }
 }
 
+// The scratch array's device address, per device.  Only a successful
+// lookup is recorded: a lookup that failed (for example while another
+// stream was capturing in global mode) is retried by the next call.
 struct DeviceScratch {
-  std::once_flag once;
-  cudaError_t err = cudaSuccess;
+  std::mutex mu;
   unsigned char* base = nullptr;
 };
 DeviceScratch g_devices[kMaxDevices];
+
+unsigned char* ScratchBase(int dev) {
+  DeviceScratch& ds = g_devices[dev];
+  std::lock_guard<std::mutex> lk(ds.mu);
+  if (!ds.base) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    ds.base = static_cast<unsigned char*>(p);
+  }
+  return ds.base;
+}
 
 }  // namespace
 
@@ -249,16 +266,11 @@ extern "C" pcc_status pcc_best_moves_static(
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return PCC_UNAVAILABLE;
   if (dev < 0 || dev >= kMaxDevices) return PCC_OUT_OF_RANGE;
-  DeviceScratch& ds = g_devices[dev];
-  std::call_once(ds.once, [&ds]() {
-    void* p = nullptr;
-    ds.err = cudaGetSymbolAddress(&p, g_static_scratch);
-    ds.base = static_cast<unsigned char*>(p);
-  });
-  if (ds.err != cudaSuccess || !ds.base) return PCC_INTERNAL;
+  unsigned char* const base = ScratchBase(dev);
+  if (!base) return PCC_INTERNAL;
   if (num_vertices == 0) return PCC_OK;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  uint32_t* error = reinterpret_cast<uint32_t*>(ds.base + kKeysBytes + size_t(kStaticSlots) * 8);
+  uint32_t* error = reinterpret_cast<uint32_t*>(base + kKeysBytes + size_t(kStaticSlots) * 8);
   if (cudaMemsetAsync(error, 0, sizeof(uint32_t), st) != cudaSuccess) return PCC_INTERNAL;
   uint32_t region = 32;
   while (region < 2ull * max_degree + 2) region <<= 1;
@@ -284,8 +296,8 @@ extern "C" pcc_status pcc_best_moves_static(
   a.region = region;
   a.out_t = d_out_targets;
   a.out_v = d_out_values;
-  a.keys = reinterpret_cast<uint32_t*>(ds.base);
-  a.sums = reinterpret_cast<double*>(ds.base + kKeysBytes);
+  a.keys = reinterpret_cast<uint32_t*>(base);
+  a.sums = reinterpret_cast<double*>(base + kKeysBytes);
   a.error = error;
   StaticBestMoveKernel<<<static_cast<unsigned>(grid), kThreads, 0, st>>>(a);
   if (cudaGetLastError() != cudaSuccess) return PCC_INTERNAL;

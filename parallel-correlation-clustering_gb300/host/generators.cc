@@ -245,15 +245,16 @@ pcch_graph* pcch_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double
 }
 
 // LFR-like planted partition.  Degrees follow a discrete power law
-// (exponent tau1) on [dmin, dmax] with dmin chosen so the mean is close to
-// `mean_degree`; community sizes follow a power law (exponent tau2) on
+// (exponent tau1) on [dmin, dmax]; a fraction q of the draws comes from
+// [dmin + 1, dmax] instead, with dmin and q chosen so the sequence's mean is
+// the target.  Community sizes follow a power law (exponent tau2) on
 // [cmin, cmax].  Each vertex sends round((1 - mu) d) stubs inside its
 // community and the rest outside; stubs are paired uniformly at random
 // (configuration model) within each community and globally.  Self-loops and
 // duplicates are dropped.  Weights are Uniform[w_lo, w_hi] per undirected
 // edge (0 / 0 for unit weights).  truth[i] is the community of vertex i.
-pcch_graph* pcch_gen_lfr(uint32_t n, double mean_degree, uint32_t dmax, double tau1, uint32_t cmin, uint32_t cmax,
-                         double tau2, double mu, double w_lo, double w_hi, uint64_t seed) {
+static pcch_graph* LfrOnce(uint32_t n, double mean_degree, uint32_t dmax, double tau1, uint32_t cmin, uint32_t cmax,
+                    double tau2, double mu, double w_lo, double w_hi, uint64_t seed) {
   // Degree distribution.
   auto pl_mean = [&](uint32_t dmin) {
     double num = 0, den = 0;
@@ -266,17 +267,28 @@ pcch_graph* pcch_gen_lfr(uint32_t n, double mean_degree, uint32_t dmax, double t
   };
   uint32_t dmin = 1;
   while (dmin < dmax && pl_mean(dmin + 1) <= mean_degree) ++dmin;
-  std::vector<double> cdf;
-  for (uint32_t d = dmin; d <= dmax; ++d) cdf.push_back(std::pow(double(d), -tau1));
-  for (size_t i = 1; i < cdf.size(); ++i) cdf[i] += cdf[i - 1];
-  for (auto& x : cdf) x /= cdf.back();
-  // Mix dmin and dmin+1 so the mean matches: fraction q of draws shifted up.
+  auto make_cdf = [&](uint32_t lo) {
+    std::vector<double> cdf;
+    for (uint32_t d = lo; d <= dmax; ++d) cdf.push_back(std::pow(double(d), -tau1));
+    for (size_t i = 1; i < cdf.size(); ++i) cdf[i] += cdf[i - 1];
+    for (auto& x : cdf) x /= cdf.back();
+    return cdf;
+  };
+  const std::vector<double> cdf = make_cdf(dmin);
+  const std::vector<double> cdf_up = make_cdf(dmin < dmax ? dmin + 1 : dmin);
+  const uint32_t dmin_up = dmin < dmax ? dmin + 1 : dmin;
+  // Mix the laws from dmin and dmin + 1: fraction q from the upper one, so
+  // (1 - q) mean(dmin) + q mean(dmin + 1) equals the target.
+  const double m_lo = pl_mean(dmin), m_hi = pl_mean(dmin_up);
+  const double q = m_hi > m_lo ? std::min(1.0, std::max(0.0, (mean_degree - m_lo) / (m_hi - m_lo))) : 0.0;
   std::vector<uint32_t> deg(n);
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < int64_t(n); ++i) {
     const double u = U01(Hash3(seed, 11, uint64_t(i)));
-    const size_t k = std::lower_bound(cdf.begin(), cdf.end(), u) - cdf.begin();
-    deg[i] = dmin + static_cast<uint32_t>(std::min(k, cdf.size() - 1));
+    const bool up = U01(Hash3(seed, 16, uint64_t(i))) < q;
+    const std::vector<double>& c = up ? cdf_up : cdf;
+    const size_t k = std::lower_bound(c.begin(), c.end(), u) - c.begin();
+    deg[i] = (up ? dmin_up : dmin) + static_cast<uint32_t>(std::min(k, c.size() - 1));
   }
   // Community sizes.
   std::vector<double> ccdf;
@@ -343,6 +355,22 @@ pcch_graph* pcch_gen_lfr(uint32_t n, double mean_degree, uint32_t dmax, double t
   g->truth = static_cast<uint32_t*>(std::malloc(sizeof(uint32_t) * std::max<uint32_t>(n, 1)));
   std::copy(comm.begin(), comm.end(), g->truth);
   return g;
+}
+
+// The realised mean degree falls short of the degree sequence's mean by the
+// self-loops and duplicates dropped after pairing (small communities pair
+// many stubs among few vertices).  One measured pass gives the shortfall; a
+// second pass from the same seed asks for a mean raised by it, so that the
+// realised mean lands on the configured one.
+pcch_graph* pcch_gen_lfr(uint32_t n, double mean_degree, uint32_t dmax, double tau1, uint32_t cmin, uint32_t cmax,
+                         double tau2, double mu, double w_lo, double w_hi, uint64_t seed) {
+  pcch_graph* g = LfrOnce(n, mean_degree, dmax, tau1, cmin, cmax, tau2, mu, w_lo, w_hi, seed);
+  if (!g || n == 0 || g->m == 0) return g;
+  const double realised = double(g->m) / double(n);
+  if (realised >= 0.998 * mean_degree) return g;
+  const double target = std::min(double(dmax), mean_degree * mean_degree / realised);
+  pcch_graph_free(g);
+  return LfrOnce(n, target, dmax, tau1, cmin, cmax, tau2, mu, w_lo, w_hi, seed);
 }
 
 }  // extern "C"

@@ -97,6 +97,8 @@ class PccStats(ctypes.Structure):
         ("family_launches", ctypes.c_uint64 * 4),
         ("family_entries", ctypes.c_uint64 * 4),
         ("family_vertices", ctypes.c_uint64 * 4),
+        ("algo_bytes_compress", ctypes.c_uint64),
+        ("algo_bytes_frontier", ctypes.c_uint64),
     ]
 
     FAMILIES = ("groups", "warps", "small_hubs", "big_hubs")
@@ -300,6 +302,7 @@ class Context:
     def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
         self.lib = load_library()
         self._h = ctypes.c_void_p()
+        self.detailed_timing = False
         st = self.lib.pcc_create(ctypes.byref(self._h), device, hbm_budget_bytes)
         if st != 0:
             raise PccError(st, "pcc_create failed (no usable GPU?)")
@@ -335,6 +338,7 @@ class Context:
         per-kernel-family CUDA events (on), or the device-side round loop
         (off, the default)."""
         self.lib.pcc_set_detailed_timing(self._h, 1 if on else 0)
+        self.detailed_timing = bool(on)
 
     def bytes_in_use(self) -> int:
         return int(self.lib.pcc_device_bytes_in_use(self._h))
