@@ -55,11 +55,11 @@ METRIC = "best-move edge-visits/s"
 UNIT = "edge-visits/s"
 
 # DRAM bytes (read + write) per evaluated entry of each best-move kernel
-# family, from ncu captures of RMAT scale 20, level 0, round 1 (the whole
-# frontier); the summary and command are in profiles/.  Traffic scales with
-# the entries evaluated, so the per-launch figure at the bench's size is this
-# times the entries of a launch.
-TRAFFIC_BYTES_PER_ENTRY = {"groups": 51.9, "warps": 8.84, "small_hubs": 5.38, "big_hubs": 7.64}
+# family, from ncu captures of RMAT scale 20, level 0, first round (the whole
+# frontier; cold L2); the summary and command are in profiles/.  Traffic
+# scales with the entries evaluated, so the per-launch figure at the bench's
+# size is this times the entries of a launch.
+TRAFFIC_BYTES_PER_ENTRY = {"groups": 52.0, "warps": 8.84, "small_hubs": 6.22, "big_hubs": 9.92}
 
 
 def parse_args():
@@ -246,12 +246,14 @@ def cpu_baseline(args, P, g, gpu_labels, gpu_stats):
 def async_quality(args, P, G, ctx, seeds: int = 5):
     """Async mode is nondeterministic (in the reference too): the GPU's mean
     modularity over seeds beside the oracle's, on RMAT scale --cpu-scale with
-    the headline config in async mode.  Each GPU modularity is recomputed by
-    the oracle from the GPU's labels."""
+    the headline config in async mode.  The oracle runs on one worker (the
+    reference's async result also moves with its worker count; one worker
+    is deterministic per seed).  Each GPU modularity is recomputed by the
+    oracle from the GPU's labels."""
     import numpy as np
     sys.path.insert(0, ORACLE_DIR)
     import oracle as O
-    O.set_threads(0)
+    O.set_threads(1)
     g = G.rmat(args.cpu_scale, 16, seed=1)
     og = O.OracleGraph(g)
     dg = ctx.upload(g)
@@ -263,8 +265,9 @@ def async_quality(args, P, G, ctx, seeds: int = 5):
         _, so = O.modularity_cluster(og, cfg)
         cpu.append(so["modularity"])
     dg.free()
+    O.set_threads(0)
     mg, mc = float(np.mean(gpu)), float(np.mean(cpu))
-    return {"graph": f"RMAT scale {args.cpu_scale} (n={g.n}, m={g.m})", "seeds": seeds,
+    return {"graph": f"RMAT scale {args.cpu_scale} (n={g.n}, m={g.m})", "seeds": seeds, "oracle_workers": 1,
             "gpu_mean_modularity": mg, "oracle_mean_modularity": mc,
             "relative_difference": (mg - mc) / abs(mc) if mc else None,
             "gpu": gpu, "oracle": cpu}
@@ -295,6 +298,28 @@ def batched_leg(args, P, G, ctx):
                     for lab, st, r in zip(labels, stats, ref))
     value = len(graphs) / batch_s
     plain = len(sample) / plain_s
+    # Breakdown: the same graphs as disjoint unions on one context with
+    # detailed timing (CUDA events per phase); wall minus device time is the
+    # host side (upload, union build, per-round flag reads, download).
+    detailed = ctx.detailed_timing
+    ctx.set_detailed_timing(True)
+    t = time.perf_counter()
+    _, ustats, tot = P.cluster_union(ctx, graphs, cfg)
+    union_wall_ms = (time.perf_counter() - t) * 1000.0
+    ctx.set_detailed_timing(detailed)
+    dev_ms = tot["ms_total"]
+    breakdown = {
+        "note": "one more run of the same graphs as unions on one context with detailed timing",
+        "wall_ms": union_wall_ms, "device_ms": dev_ms,
+        "best_moves_ms": tot["ms_best_moves"], "compress_ms": tot["ms_compress"],
+        "apply_ms": tot["ms_apply"], "frontier_ms": tot["ms_frontier"],
+        "other_device_ms": dev_ms - tot["ms_best_moves"] - tot["ms_compress"] - tot["ms_apply"] - tot["ms_frontier"],
+        "host_side_ms": union_wall_ms - dev_ms,
+        "union_rounds": tot["rounds"], "kernel_launches": tot["kernel_launches"],
+        "edge_visits": tot["edge_visits"],
+        "best_move_edge_visits_per_s": tot["edge_visits"] / (tot["ms_best_moves"] / 1000.0)
+        if tot["ms_best_moves"] > 0 else None,
+    }
     return {
         "workload": "batched_sbm_correlation_refine",
         "graphs": len(graphs), "n_total": int(sum(g.n for g in graphs)), "m_total": int(sum(g.m for g in graphs)),
@@ -303,6 +328,7 @@ def batched_leg(args, P, G, ctx):
         "speedup_vs_per_graph_calls": value / plain,
         "identical_to_per_graph_calls": bool(identical),
         "path": "pcc_cluster_batch -> disjoint unions (pcc_cluster_union), host buffers in and out",
+        "breakdown": breakdown,
     }
 
 

@@ -203,12 +203,19 @@ class ParallelCorrelationClustererGB300 : public InMemoryClusterer {
   Status RefineClusters(const ClustererConfig& config, Clustering* clustering) const override;
   // Statistics of the last call (edge visits, rounds, timings).
   const pcc_stats& last_stats() const { return stats_; }
+  // The CLI's graph read (cluster-in-memory_main.cc:285-306) on the device:
+  // the GBBS adjacency file is parsed straight into the resident graph
+  // (pcc_graph_read_gbbs) and replaces whatever MutableGraph() holds for
+  // the following Cluster / RefineClusters calls.
+  Status ReadGraphOnDevice(const std::string& path, bool float_weighted);
 
  protected:
   virtual int objective() const { return 0; }
   Status Run(const ClustererConfig& config, const std::vector<uint32_t>* initial,
              Clustering* out) const;
   Status EnsureDevice() const;
+  Status EnsureContext() const;
+  uint32_t num_nodes() const { return device_graph_only_ ? device_nodes_ : graph_.num_nodes(); }
 
   GpuOptions options_;
   CsrGraph graph_;
@@ -217,6 +224,8 @@ class ParallelCorrelationClustererGB300 : public InMemoryClusterer {
   mutable uint64_t uploaded_entries_ = 0;
   mutable uint32_t uploaded_nodes_ = 0;
   mutable pcc_stats stats_{};
+  bool device_graph_only_ = false;  // dgraph_ came from ReadGraphOnDevice
+  uint32_t device_nodes_ = 0;
 };
 
 // ParallelModularityClusterer: node weight = degree, resolution / total
@@ -244,6 +253,9 @@ Status WriteGbbsAdjacencyGraph(const std::string& path, const CsrGraph& graph);
 // One cluster per line, node ids each followed by a tab
 // (cluster-in-memory_main.cc:131-144).
 Status WriteClustering(const std::string& path, const InMemoryClusterer::Clustering& clustering);
+// The same file formatted on GPU `device` (pcc_write_clustering).
+Status WriteClusteringOnDevice(const std::string& path, const InMemoryClusterer::Clustering& clustering,
+                               int device);
 Status ReadCommunities(const std::string& path, std::vector<std::vector<uint32_t>>* communities);
 
 // Ground-truth scoring of CompareCommunities (cluster-in-memory_main.cc:

@@ -176,6 +176,46 @@ pcc_status pcc_graph_download(pcc_context* ctx, const pcc_graph* graph,
                               float* weights);
 
 /*
+ * GBBS adjacency text parsed on the device into a resident graph, in place
+ * of gbbs_io::read_unweighted_symmetric_graph /
+ * read_weighted_symmetric_graph<float> + CopyGraph
+ * (clustering/cluster-in-memory_main.cc:285-306).  The text is
+ * "AdjacencyGraph" or "WeightedAdjacencyGraph", n, m, n offsets, m neighbour
+ * ids and, when weighted, m weights, separated by whitespace; float_weighted
+ * must match the header.  Results and errors equal the host reader's
+ * (pcch_read_gbbs): offsets and ids are decimal digits; weights round as
+ * strtof (nearest float, ties to even); all-one weights give a unit-weight
+ * graph; tokens after the last one needed are ignored.  Hexadecimal floats,
+ * nan(...) payloads and weights of more than 200 significant digits are
+ * INVALID_ARGUMENT here.  Bad or missing tokens are INVALID_ARGUMENT (the
+ * first in file order is named), n > 2^32 - 1 is OUT_OF_RANGE.
+ *   text / size   the file's bytes in host memory
+ */
+pcc_status pcc_graph_parse_gbbs(pcc_context* ctx, const char* text, uint64_t size,
+                                int32_t float_weighted, pcc_graph** out);
+/* Reads the file at `path` into pinned host memory, then parses it on the
+ * device as pcc_graph_parse_gbbs.  NOT_FOUND if it cannot be opened. */
+pcc_status pcc_graph_read_gbbs(pcc_context* ctx, const char* path,
+                               int32_t float_weighted, pcc_graph** out);
+
+/*
+ * WriteClustering (clustering/cluster-in-memory_main.cc:132-145) formatted
+ * on the device.  labels[n] (host) gives each node's cluster index; cluster
+ * i is the set of nodes labelled i, for i up to the largest label.  The text
+ * has one line per cluster in index order, each member id (ascending)
+ * followed by a tab, then a newline (an empty line for an empty cluster).
+ * pcc_format_clustering stores the length in *length and, when out is not
+ * NULL, the text in out[0..length) (RESOURCE_EXHAUSTED if capacity is
+ * smaller; call with out = NULL to size the buffer).  pcc_write_clustering
+ * writes the text to the file at `path` (NOT_FOUND if it cannot be opened).
+ */
+pcc_status pcc_format_clustering(pcc_context* ctx, uint32_t n,
+                                 const uint32_t* labels, char* out,
+                                 uint64_t capacity, uint64_t* length);
+pcc_status pcc_write_clustering(pcc_context* ctx, const char* path, uint32_t n,
+                                const uint32_t* labels);
+
+/*
  * ParallelCorrelationClusterer::RefineClusters / Cluster
  * (clustering/clusterers/parallel-correlation-clusterer.cc:392-653).
  *   node_weights    host double[n] or NULL (all 1, parallel-correlation-

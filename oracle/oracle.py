@@ -84,6 +84,8 @@ def lib():
         L.pcco_gen_rmat.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_double, ctypes.c_uint64]
         L.pcco_gen_rmat.restype = vp
+        L.pcco_subclusters.argtypes = [vp, P(ctypes.c_uint32), ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                       P(ctypes.c_uint32), P(ctypes.c_uint64), P(ctypes.c_uint32)]
         _lib = L
     return _lib
 
@@ -227,6 +229,19 @@ def rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c:
     no self-loops, unit weights): the same graph as the package's generator
     for the same arguments, without loading any library of the package."""
     return OracleGraph(handle=lib().pcco_gen_rmat(scale, edge_factor, a, b, c, seed))
+
+
+def subclusters(g: OracleGraph, C, method: int, resolution: float = 0.0, edge_weight_offset: float = 0.0):
+    """Subcluster ids of clustering C on g (one level of the subclustering
+    before compression); returns (ids, block starts + total)."""
+    n, _ = g.info()
+    C = np.ascontiguousarray(C, np.uint32)
+    ids = np.empty(n, np.uint32)
+    nxt = np.empty(n + 1, np.uint64)
+    G = ctypes.c_uint32()
+    _check(lib().pcco_subclusters(g.h, _p(C, ctypes.c_uint32), method, resolution, edge_weight_offset,
+                                  _p(ids, ctypes.c_uint32), _p(nxt, ctypes.c_uint64), ctypes.byref(G)))
+    return ids, nxt[:G.value + 1].copy()
 
 
 def compare_communities(labels, communities):

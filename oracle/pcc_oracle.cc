@@ -829,6 +829,245 @@ void HelperFromLabels(Helper& h, uint32_t n, const std::vector<double>& k,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Subclustering before compression: CompressSubclusters (parallel-
+// correlation-clusterer.cc:436-474) with ComputeSubcluster and its three
+// methods (parallel-correlation-clusterer-internal.cc:784-1120).
+//
+// Every cluster (OutputIndicesById order: ids ascending, members ascending)
+// is split into subclusters; cluster i owns the subcluster ids
+// [next_i, next_i + B_i) (B_i = the method's block size, next = the
+// exclusive scan of the blocks), and the graph is compressed by subcluster
+// id.  The next level starts from the clustering "subclusters of one
+// cluster together": compressed vertex j is in cluster i for j in i's block,
+// and cluster i's size is its block size B_i (ids of the block that no
+// vertex took included, as the reference's group sizes).
+//
+// Labels inside a cluster (local index x = rank of the member among the
+// cluster's members):
+//  * CONNECTIVITY: components of the member pairs joined by an entry, each
+//    labelled by its smallest member's local index (union by the smaller
+//    root, as GBBS's asynchronous union-find links a larger root to a
+//    smaller one); B = the cluster size.
+//  * TRIANGLE: components of the entries (v, u), C(u) = C(v), whose
+//    triangle ratio |N(v) & N(u)| / (deg v + deg u) (a sorted-merge
+//    intersection of the two rows) exceeds 0.25; B = 1 + the largest label.
+//    The reference labels components with GBBS's work-efficient CC (LDD
+//    centres); here a component is labelled by its smallest member, which
+//    gives the same components under other ids.
+//  * SLOW_CONNECTIVITY: the reference's sequential merge loop, step by step;
+//    B = 1 + the largest label.
+//
+// Where this deliberately differs from the reference: its level loop keeps
+// flattening through the level's cluster ids while the compressed graph is
+// indexed by subcluster ids, and its next-level clustering names subcluster
+// ids beyond the compressed graph (reads and writes outside the helper's
+// vectors whenever a cluster's largest component label is below its block
+// end).  Those are index confusions with undefined behaviour, so a
+// level-i vertex maps to its subcluster id on level i + 1 (refinement
+// projections and the final labels follow that map), and ids beyond the
+// compressed graph count only in their cluster's size.
+// ---------------------------------------------------------------------------
+struct UnionFind {
+  std::vector<uint32_t> p;
+  explicit UnionFind(uint32_t n) : p(n) { std::iota(p.begin(), p.end(), 0u); }
+  uint32_t Find(uint32_t x) {
+    while (p[x] != x) {
+      p[x] = p[p[x]];
+      x = p[x];
+    }
+    return x;
+  }
+  void Unite(uint32_t a, uint32_t b) {
+    a = Find(a);
+    b = Find(b);
+    if (a == b) return;
+    if (a < b) std::swap(a, b);
+    p[a] = b;  // the larger root under the smaller
+  }
+};
+
+// |N(v) & N(u)| by a sorted-merge walk of the two rows (GBBS intersect),
+// over the sum of the two degrees, for every entry.
+std::vector<double> TriangleRatios(const Graph& g) {
+  std::vector<double> out(g.m, 0.0);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(NumThreads())
+  for (int64_t v = 0; v < int64_t(g.n); ++v) {
+    for (uint64_t j = g.off[v]; j < g.off[v + 1]; ++j) {
+      const uint32_t u = g.nbr[j];
+      uint64_t a = g.off[v], ae = g.off[v + 1], b = g.off[u], be = g.off[u + 1];
+      uint64_t common = 0;
+      while (a < ae && b < be) {
+        if (g.nbr[a] == g.nbr[b]) {
+          ++common;
+          ++a;
+          ++b;
+        } else if (g.nbr[a] < g.nbr[b]) {
+          ++a;
+        } else {
+          ++b;
+        }
+      }
+      out[j] = static_cast<double>(common) / static_cast<double>(g.degree(v) + g.degree(u));
+    }
+  }
+  return out;
+}
+
+// ComputeSubclusterConnectivitySlow (internal.cc:870-985) for one cluster:
+// local labels into lab[0..size), returns 1 + the largest label.
+uint32_t SlowSubclusters(const Graph& g, const std::vector<uint32_t>& members, const std::vector<uint32_t>& C,
+                         const Options& o, std::vector<uint8_t>& mark, std::vector<uint32_t>& lab) {
+  const size_t size = members.size();
+  const uint32_t c = C[members[0]];
+  std::vector<uint32_t> tmp(size);
+  std::iota(tmp.begin(), tmp.end(), 0u);
+  std::vector<char> single(size, 0);
+  auto outside = [&](uint32_t x) { return C[x] != c; };
+  for (size_t i = 0; i < size; ++i) {
+    if (single[i] != 0) continue;
+    const uint32_t cv = members[i];
+    int curr_num_edges = 0;
+    for (uint64_t j = g.off[cv]; j < g.off[cv + 1]; ++j)
+      if (outside(g.nbr[j])) curr_num_edges++;
+    if (static_cast<size_t>(curr_num_edges) < size - 1) continue;
+    // OutputIndicesById(tmp): groups of local indices by label.
+    std::vector<std::vector<uint32_t>> groups = GroupsById(tmp);
+    std::vector<char> invalid(groups.size(), 0);
+    int64_t num_valid = static_cast<int64_t>(groups.size());
+    for (size_t j = 0; j < groups.size(); ++j) {
+      const std::vector<uint32_t>& curr = groups[j];
+      if (curr.empty() || curr[0] == i) {
+        invalid[j] = 1;
+        num_valid--;
+        continue;
+      }
+      int num_edges = 0;
+      for (uint32_t x : curr) {
+        const uint32_t vx = members[x];
+        for (uint64_t e = g.off[vx]; e < g.off[vx + 1]; ++e)
+          if (outside(g.nbr[e])) num_edges++;
+      }
+      if (static_cast<size_t>(num_edges) < curr.size() * (size - curr.size())) {
+        invalid[j] = 1;
+        num_valid--;
+      }
+    }
+    if (num_valid == 0) continue;
+    double max_max = 0;
+    size_t idx_idx = 0;
+    for (size_t j = 0; j < groups.size(); ++j) {
+      if (invalid[j] != 0) continue;
+      const std::vector<uint32_t>& curr = groups[j];
+      for (uint32_t x : curr) mark[members[x]] = 2;
+      double weight = 0;
+      const double offset = o.offset * double(curr.size()) + o.res * double(curr.size());
+      for (uint64_t e = g.off[cv]; e < g.off[cv + 1]; ++e)
+        if (mark[g.nbr[e]] == 2) weight++;
+      for (uint32_t x : curr) mark[members[x]] = 0;
+      if (weight < offset) {
+        invalid[j] = 1;
+        num_valid--;
+      } else if (weight - offset >= max_max) {
+        max_max = weight - offset;
+        idx_idx = j;
+      }
+    }
+    if (num_valid == 0) continue;
+    const std::vector<uint32_t>& curr = groups[idx_idx];
+    tmp[i] = tmp[curr[0]];
+    single[i] = 1;
+    single[curr[0]] = 1;
+  }
+  uint32_t mx = 0;
+  for (size_t i = 0; i < size; ++i) {
+    lab[i] = tmp[i];
+    mx = std::max(mx, tmp[i]);
+  }
+  return mx + 1;
+}
+
+struct SubclusterMap {
+  std::vector<uint32_t> id;     // subcluster id of every vertex
+  std::vector<uint64_t> next;   // block start of every cluster (index order), then the total
+};
+
+SubclusterMap ComputeSubclusters(const Graph& g, const std::vector<uint32_t>& C, int method, const Options& o) {
+  const std::vector<std::vector<uint32_t>> groups = GroupsById(C);
+  const size_t G = groups.size();
+  SubclusterMap out;
+  out.id.assign(g.n, 0);
+  out.next.assign(G + 1, 0);
+  std::vector<uint32_t> local(g.n, 0);
+  for (const auto& mem : groups)
+    for (size_t x = 0; x < mem.size(); ++x) local[mem[x]] = static_cast<uint32_t>(x);
+  std::vector<double> tri;
+  if (method == PCC_TRIANGLE_SUBCLUSTERING) tri = TriangleRatios(g);
+  std::vector<std::vector<uint32_t>> labels(G);
+#pragma omp parallel num_threads(NumThreads())
+  {
+    std::vector<uint8_t> mark;
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t gi = 0; gi < int64_t(G); ++gi) {
+      const std::vector<uint32_t>& mem = groups[gi];
+      std::vector<uint32_t>& lab = labels[gi];
+      lab.assign(mem.size(), 0);
+      uint32_t block = 0;
+      if (method == PCC_SLOW_CONNECTIVITY_SUBCLUSTERING) {
+        if (mark.size() != g.n) mark.assign(g.n, 0);
+        block = SlowSubclusters(g, mem, C, o, mark, lab);
+      } else {
+        UnionFind uf(static_cast<uint32_t>(mem.size()));
+        const uint32_t c = C[mem[0]];
+        for (size_t x = 0; x < mem.size(); ++x) {
+          const uint32_t v = mem[x];
+          for (uint64_t j = g.off[v]; j < g.off[v + 1]; ++j) {
+            const uint32_t u = g.nbr[j];
+            if (C[u] != c) continue;
+            if (method == PCC_TRIANGLE_SUBCLUSTERING && !(tri[j] > 0.25)) continue;
+            uf.Unite(static_cast<uint32_t>(x), local[u]);
+          }
+        }
+        uint32_t mx = 0;
+        for (size_t x = 0; x < mem.size(); ++x) {
+          lab[x] = uf.Find(static_cast<uint32_t>(x));
+          mx = std::max(mx, lab[x]);
+        }
+        block = method == PCC_CONNECTIVITY_SUBCLUSTERING ? static_cast<uint32_t>(mem.size()) : mx + 1;
+      }
+      out.next[gi] = block;
+    }
+  }
+  uint64_t run = 0;
+  for (size_t gi = 0; gi < G; ++gi) {
+    const uint64_t b = out.next[gi];
+    out.next[gi] = run;
+    run += b;
+  }
+  out.next[G] = run;
+  for (size_t gi = 0; gi < G; ++gi)
+    for (size_t x = 0; x < groups[gi].size(); ++x)
+      out.id[groups[gi][x]] = static_cast<uint32_t>(out.next[gi] + labels[gi][x]);
+  return out;
+}
+
+// The next level's starting clustering after compression by subcluster id.
+void HelperFromSubclusters(Helper& h, uint32_t n2, std::vector<double> k2, const SubclusterMap& sm) {
+  h.n = n2;
+  h.k = std::move(k2);
+  h.C.assign(n2, 0);
+  h.s.assign(n2, 0);
+  h.K.assign(n2, 0.0);
+  const size_t G = sm.next.size() - 1;
+  for (size_t gi = 0; gi < G; ++gi) {
+    h.s[gi] = static_cast<uint32_t>(sm.next[gi + 1] - sm.next[gi]);
+    for (uint64_t j = sm.next[gi]; j < sm.next[gi + 1] && j < n2; ++j) {
+      h.C[j] = static_cast<uint32_t>(gi);
+      h.K[gi] += h.k[j];
+    }
+  }
+}
+
 struct ClusterResult {
   std::vector<uint32_t> labels;  // dense group index
   uint32_t num_clusters = 0;
@@ -855,7 +1094,15 @@ int RefineClustersSubroutine(const Graph& graph, const pcc_config& cfg,
   } else {
     return PCC_UNIMPLEMENTED;
   }
-  if (cfg.subclustering_method != PCC_NONE_SUBCLUSTERING) return PCC_UNIMPLEMENTED;
+  const int sub_method = cfg.subclustering_method;
+  if (sub_method != PCC_NONE_SUBCLUSTERING && sub_method != PCC_TRIANGLE_SUBCLUSTERING &&
+      sub_method != PCC_CONNECTIVITY_SUBCLUSTERING && sub_method != PCC_SLOW_CONNECTIVITY_SUBCLUSTERING)
+    return PCC_UNIMPLEMENTED;
+  // Subcluster moves inside the DEFAULT_CLUSTER_MOVES rounds are not
+  // restated (the library answers UNIMPLEMENTED for them too).
+  if (sub_method != PCC_NONE_SUBCLUSTERING && cfg.clustering_moves_method == PCC_DEFAULT_CLUSTER_MOVES)
+    return PCC_UNIMPLEMENTED;
+  const bool subclusters = sub_method != PCC_NONE_SUBCLUSTERING;
 
   Options o;
   o.res = cfg.resolution;
@@ -870,10 +1117,13 @@ int RefineClustersSubroutine(const Graph& graph, const pcc_config& cfg,
 
   std::vector<std::unique_ptr<Helper>> rec_helpers;
   std::vector<std::unique_ptr<Graph>> rec_graphs;
+  std::vector<std::vector<uint32_t>> rec_maps;  // subclustering: level-i vertex -> level-(i+1) vertex
   if (refine) {
     rec_helpers.resize(num_iterations);
     rec_graphs.resize(num_iterations);
+    rec_maps.resize(num_iterations);
   }
+  bool vertex_ids = false;  // no refine, subclustering: cluster_ids hold vertex ids of the current level
   auto helper = std::make_unique<Helper>();
   {
     std::vector<double> k = node_weights;
@@ -898,16 +1148,22 @@ int RefineClustersSubroutine(const Graph& graph, const pcc_config& cfg,
       break;
     }
     result->levels++;
+    const bool last = iter == num_iterations - 1;
+    SubclusterMap sm;
+    if (subclusters && !last) sm = ComputeSubclusters(cur, helper->C, sub_method, o);
     if (!refine) {
-      // FlattenClustering (parallel-graph-utils.cc:233-243).
-      for (uint32_t i = 0; i < n; ++i) cluster_ids[i] = helper->C[cluster_ids[i]];
-    } else if (iter == num_iterations - 1) {
+      // FlattenClustering (parallel-graph-utils.cc:233-243); with
+      // subclusters the map to the next level is the subcluster id.
+      const std::vector<uint32_t>& map = (subclusters && !last) ? sm.id : helper->C;
+      for (uint32_t i = 0; i < n; ++i) cluster_ids[i] = map[cluster_ids[i]];
+      vertex_ids = subclusters && !last;
+    } else if (last) {
       rec_helpers[iter] = std::move(helper);
       rec_graphs[iter] = (iter == 0) ? nullptr : std::move(compressed);
     }
-    if (iter == num_iterations - 1) break;
+    if (last) break;
 
-    auto next = std::make_unique<Graph>(CompressGraph(cur, helper->C, helper->k));
+    auto next = std::make_unique<Graph>(CompressGraph(cur, subclusters ? sm.id : helper->C, helper->k));
     std::vector<double> next_k = std::move(next->node_w);
     next->node_w.clear();
     std::unique_ptr<Graph> prev = std::move(compressed);
@@ -915,10 +1171,19 @@ int RefineClustersSubroutine(const Graph& graph, const pcc_config& cfg,
     if (refine) {
       rec_helpers[iter] = std::move(helper);
       rec_graphs[iter] = std::move(prev);  // graph of level `iter` (nullptr at 0)
+      if (subclusters) rec_maps[iter] = sm.id;
     }
     helper = std::make_unique<Helper>();
-    helper->InitSingletons(compressed->n, std::move(next_k));
+    if (subclusters) {
+      HelperFromSubclusters(*helper, compressed->n, std::move(next_k), sm);
+    } else {
+      helper->InitSingletons(compressed->n, std::move(next_k));
+    }
   }
+  // No refine, subclusters: the last level did not move; its starting
+  // clustering names the clusters of the vertices cluster_ids now hold.
+  if (vertex_ids)
+    for (uint32_t i = 0; i < n; ++i) cluster_ids[i] = helper->C[cluster_ids[i]];
 
   if (refine && iter > 0) {
     for (int64_t i = iter - 1; i >= 0; --i) {
@@ -926,7 +1191,8 @@ int RefineClustersSubroutine(const Graph& graph, const pcc_config& cfg,
       Helper& hi = *rec_helpers[i];
       const Helper& hup = *rec_helpers[i + 1];
       std::vector<uint32_t> flat(hi.n);
-      for (uint32_t j = 0; j < hi.n; ++j) flat[j] = hup.C[hi.C[j]];
+      const std::vector<uint32_t>& map = subclusters ? rec_maps[i] : hi.C;
+      for (uint32_t j = 0; j < hi.n; ++j) flat[j] = hup.C[map[j]];
       hi.SetGroups(GroupsById(flat));
       IterateBestMoves(cur, hi, num_inner, o, result->ctr);
       result->refine_passes++;
@@ -1283,6 +1549,22 @@ pcco_graph* pcco_compress(const pcco_graph* g, const uint32_t* C,
   auto* out = new pcco_graph;
   out->g = CompressGraph(g->g, c, kk);
   return out;
+}
+
+// Subcluster ids of a clustering C (one level of CompressSubclusters):
+// out_ids[n]; out_next[G + 1] block starts in cluster order, then the total
+// (G = number of clusters; the array must hold n + 1 entries).
+int pcco_subclusters(const pcco_graph* g, const uint32_t* C, int32_t method, double resolution,
+                     double edge_weight_offset, uint32_t* out_ids, uint64_t* out_next, uint32_t* num_clusters) {
+  std::vector<uint32_t> c(C, C + g->g.n);
+  Options o;
+  o.res = resolution;
+  o.offset = edge_weight_offset;
+  const SubclusterMap sm = ComputeSubclusters(g->g, c, method, o);
+  std::copy(sm.id.begin(), sm.id.end(), out_ids);
+  std::copy(sm.next.begin(), sm.next.end(), out_next);
+  *num_clusters = static_cast<uint32_t>(sm.next.size() - 1);
+  return PCC_OK;
 }
 
 pcco_graph* pcco_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,

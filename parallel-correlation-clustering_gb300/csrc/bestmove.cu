@@ -652,18 +652,21 @@ Status SetSmem(K kernel, size_t bytes, int threads, int* per_sm) {
 
 template <bool kInt, bool kAsync>
 Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint32_t* counts,
-                 const uint32_t* starts, const uint32_t* host_counts, uint32_t max_deg) {
+                 const uint32_t* starts, const uint32_t* host_counts, uint32_t max_deg, int families) {
   const unsigned sms = unsigned(ctx->num_sms);
   auto grid = [&](int bin, uint64_t per_block, unsigned cap) -> unsigned {
     if (!host_counts) return cap;
     return Blocks(host_counts[bin], unsigned(per_block), cap);
   };
-  auto want = [&](int bin) { return !host_counts || host_counts[bin] > 0; };
+  auto want = [&](int bin) {
+    const int fam = bin <= kBinG32 ? kLaunchGroups : kLaunchWarps;
+    return (families & fam) && (!host_counts || host_counts[bin] > 0);
+  };
   cudaStream_t st = ctx->stream;
   constexpr bool kCert = kInt && !kAsync;
   int ng = 0;
   for (int b = kBinG4; b <= kBinG32; ++b) ng += want(b) ? 1 : 0;
-  FamBegin(ctx, kFamGroup);
+  if (families & kLaunchGroups) FamBegin(ctx, kFamGroup);
   if constexpr (kCert) {
     // One wave of resident CTAs (grid-stride kernels).
     auto group_bin = [&](auto k, int bin, uint64_t per_block) -> Status {
@@ -679,19 +682,27 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
     PCC_RETURN_IF_ERROR(group_bin(CertGroupKernel<16>, kBinG16, 16));
     PCC_RETURN_IF_ERROR(group_bin(CertGroupKernel<32>, kBinG32, 8));
   } else {
-    if (want(kBinG4))
-      BestMoveGroupKernel<4, kInt, kAsync><<<grid(kBinG4, 64, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG4); PCC_COUNT(1);
-    if (want(kBinG8))
-      BestMoveGroupKernel<8, kInt, kAsync><<<grid(kBinG8, 32, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG8); PCC_COUNT(1);
-    if (want(kBinG16))
-      BestMoveGroupKernel<16, kInt, kAsync><<<grid(kBinG16, 16, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG16); PCC_COUNT(1);
-    if (want(kBinG32))
-      BestMoveGroupKernel<32, kInt, kAsync><<<grid(kBinG32, 8, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG32); PCC_COUNT(1);
+    if (want(kBinG4)) {
+      BestMoveGroupKernel<4, kInt, kAsync><<<grid(kBinG4, 64, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG4);
+      PCC_COUNT(1);
+    }
+    if (want(kBinG8)) {
+      BestMoveGroupKernel<8, kInt, kAsync><<<grid(kBinG8, 32, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG8);
+      PCC_COUNT(1);
+    }
+    if (want(kBinG16)) {
+      BestMoveGroupKernel<16, kInt, kAsync><<<grid(kBinG16, 16, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG16);
+      PCC_COUNT(1);
+    }
+    if (want(kBinG32)) {
+      BestMoveGroupKernel<32, kInt, kAsync><<<grid(kBinG32, 8, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG32);
+      PCC_COUNT(1);
+    }
   }
-  FamEnd(ctx, kFamGroup, ng);
+  if (families & kLaunchGroups) FamEnd(ctx, kFamGroup, ng);
   int nw = 0;
   for (int b = kBinW128; b <= kBinW1000; ++b) nw += want(b) ? 1 : 0;
-  FamBegin(ctx, kFamWarp);
+  if (families & kLaunchWarps) FamBegin(ctx, kFamWarp);
   // Grid-stride kernels: at most one wave of resident CTAs, so no partial
   // last wave.
   auto warp_bin = [&](auto k, size_t smem, int bin, unsigned cap) -> Status {
@@ -725,7 +736,7 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
     PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<1024, kInt, kAsync>, WarpKernelSmem<1024>(), kBinW512, sms * 4));
     PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<2048, kInt, kAsync>, WarpKernelSmem<2048>(), kBinW1000, sms * 2));
   }
-  FamEnd(ctx, kFamWarp, nw);
+  if (families & kLaunchWarps) FamEnd(ctx, kFamWarp, nw);
   return LaunchCheck();
 }
 
@@ -765,13 +776,13 @@ Status PrepareBestMoveKernels() {
 
 Status LaunchBestMoves(Context* ctx, const BMArgs& a, const uint32_t* list, const uint32_t* bin_counts,
                        const uint32_t* bin_starts, const uint32_t* host_counts, bool int_mode,
-                       uint32_t max_deg) {
+                       uint32_t max_deg, int families) {
   if (a.async) {
-    return int_mode ? LaunchAll<true, true>(ctx, a, list, bin_counts, bin_starts, host_counts, max_deg)
-                    : LaunchAll<false, true>(ctx, a, list, bin_counts, bin_starts, host_counts, max_deg);
+    return int_mode ? LaunchAll<true, true>(ctx, a, list, bin_counts, bin_starts, host_counts, max_deg, families)
+                    : LaunchAll<false, true>(ctx, a, list, bin_counts, bin_starts, host_counts, max_deg, families);
   }
-  return int_mode ? LaunchAll<true, false>(ctx, a, list, bin_counts, bin_starts, host_counts, max_deg)
-                  : LaunchAll<false, false>(ctx, a, list, bin_counts, bin_starts, host_counts, max_deg);
+  return int_mode ? LaunchAll<true, false>(ctx, a, list, bin_counts, bin_starts, host_counts, max_deg, families)
+                  : LaunchAll<false, false>(ctx, a, list, bin_counts, bin_starts, host_counts, max_deg, families);
 }
 
 }  // namespace pcc

@@ -107,8 +107,32 @@ struct Context {
   void PutEvent(cudaEvent_t e) {
     if (e) event_pool.push_back(e);
   }
+  // Side streams for the best-move kernel families of a synchronous round:
+  // the warp and hub launches run on streams forked from `stream` (an event
+  // recorded there) and joined back into it, so their kernels overlap the
+  // lane-group kernels and each other.  Under stream capture the fork and
+  // the join become parallel branches of the captured graph.
+  static constexpr int kSideStreams = 3;
+  cudaStream_t side[kSideStreams] = {nullptr, nullptr, nullptr};
+  cudaEvent_t fork_ev = nullptr;
+  cudaEvent_t join_ev[kSideStreams] = {nullptr, nullptr, nullptr};
+  bool overlap_families = true;  // off: every family on `stream` in turn
+  Status EnsureSideStreams() {
+    if (fork_ev) return Status::Ok();
+    for (int i = 0; i < kSideStreams; ++i) {
+      PCC_CUDA(cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking));
+      PCC_CUDA(cudaEventCreateWithFlags(&join_ev[i], cudaEventDisableTiming));
+    }
+    PCC_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+    return Status::Ok();
+  }
   ~Context() {
     for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
+    for (int i = 0; i < kSideStreams; ++i) {
+      if (side[i]) cudaStreamDestroy(side[i]);
+      if (join_ev[i]) cudaEventDestroy(join_ev[i]);
+    }
+    if (fork_ev) cudaEventDestroy(fork_ev);
   }
 
   Status Alloc(void** p, uint64_t bytes) {
@@ -205,6 +229,17 @@ struct DBuf {
     if (n) PCC_CUDA(cudaMemcpyAsync(h, p, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
     return Status::Ok();
   }
+};
+
+// Launches issued while this is alive go to side stream i of the context
+// (the launchers read ctx->stream).
+struct OnSideStream {
+  Context* ctx;
+  cudaStream_t saved;
+  OnSideStream(Context* c, int i) : ctx(c), saved(c->stream) { c->stream = c->side[i]; }
+  ~OnSideStream() { ctx->stream = saved; }
+  OnSideStream(const OnSideStream&) = delete;
+  OnSideStream& operator=(const OnSideStream&) = delete;
 };
 
 inline Status Sync(Context* c) {

@@ -240,6 +240,32 @@ struct BMArgs {
 __device__ __forceinline__ double ResOf(const BMArgs& a, uint32_t v) { return a.vres ? a.vres[v] : a.res; }
 __device__ __forceinline__ float Res32Of(const BMArgs& a, uint32_t v) { return a.vres32 ? a.vres32[v] : a.res32; }
 
+// Asynchronous whole-cluster moves (AsyncSetMoves, clustermoves.cu).
+struct SetMoveArgs {
+  const DevGraph* g;
+  uint32_t* C;          // live state
+  uint32_t* s;
+  const double* k;
+  double* K;
+  double res;
+  double offset;
+  bool exact_sums;      // integral entry values: run sums in any order
+  uint32_t waves;       // hashed waves of sets
+  uint32_t salt;
+  uint32_t* free_ids;   // empty ids offered to new clusters (as the vertex moves)
+  uint32_t* free_ctr;
+  uint32_t free_cap;
+  uint32_t* mod_stamp;  // moved-cluster flags (set at the members' vertex ids)
+  uint32_t stamp;
+  DevCounters* ctr;
+  // One-member sets go through the vertex AsyncMove: the caller's kernels
+  // evaluate the vertices with aux_front[v] == val (val = aux_base + wave)
+  // and leave aux_moved[v] == val for the ones that moved.
+  uint32_t* aux_front;
+  const uint32_t* aux_moved;
+  uint32_t aux_base;
+};
+
 // Configures (shared-memory limit, occupancy) every synchronous best-move
 // kernel once per process, so that launches captured into a graph make no
 // runtime configuration calls.
@@ -249,9 +275,12 @@ Status PrepareBestMoveKernels();
 // (counts read on the device); hubs go through LaunchHubBestMoves.
 // int_mode selects exact integer accumulation (all weights and the offset
 // integral and small) over FP64 accumulation in adjacency order.
+// families: kLaunchGroups (degree <= 32) and/or kLaunchWarps (33-1000).
+constexpr int kLaunchGroups = 1;
+constexpr int kLaunchWarps = 2;
 Status LaunchBestMoves(Context* ctx, const BMArgs& a, const uint32_t* list, const uint32_t* bin_counts,
                        const uint32_t* bin_starts, const uint32_t* host_counts, bool int_mode,
-                       uint32_t max_deg);
+                       uint32_t max_deg, int families = kLaunchGroups | kLaunchWarps);
 
 // The hub plan of a graph (built on first use).
 Status EnsureHubPlan(Context* ctx, const DevGraph* g);

@@ -4,6 +4,8 @@
 // (clustering/cluster-in-memory_main.cc:231-306): the CSR arrays are copied
 // once into HBM and stay there for every clustering call.
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 
 #include "graphops.cuh"
 #include "hubs.cuh"
@@ -355,6 +357,10 @@ pcc_status pcc_create(pcc_context** out, int device, uint64_t hbm_budget_bytes) 
   c.num_sms = prop.multiProcessorCount;
   c.smem_optin = prop.sharedMemPerBlockOptin;
   c.budget = hbm_budget_bytes;
+  // PCC_SERIAL_FAMILIES=1 runs the best-move kernel families one after the
+  // other on the context stream instead of as parallel branches (same
+  // results; for comparisons).
+  if (const char* e = std::getenv("PCC_SERIAL_FAMILIES")) c.overlap_families = std::strcmp(e, "1") != 0;
   if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
     return PCC_UNAVAILABLE;

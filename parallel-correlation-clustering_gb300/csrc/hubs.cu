@@ -903,9 +903,9 @@ int PrepareOnce(K kernel, int threads, size_t smem) {
 }
 
 template <bool kInt, bool kAsync, typename V>
-Status LaunchHubT(Context* ctx, const HubArgs& h, uint32_t num_small, uint32_t num_wide) {
+Status LaunchHubT(Context* ctx, const HubArgs& h, uint32_t num_small, uint32_t num_wide, int families) {
   const unsigned sms = unsigned(ctx->num_sms);
-  if (num_small) {
+  if (num_small && (families & kLaunchSmallHubs)) {
     // Hubs whose 2d + 2 slots exceed the narrow table (listed first) take
     // the wide one; the rest run with twice the CTAs per SM.
     const int nl = (num_wide > 0) + (num_small > num_wide);
@@ -935,7 +935,7 @@ Status LaunchHubT(Context* ctx, const HubArgs& h, uint32_t num_small, uint32_t n
     FamEnd(ctx, kFamHubSmall, nl);
   }
   const bool glob = !kAsync && h.num_glob;
-  if (h.num_items) {
+  if (h.num_items && (families & kLaunchBigHubs)) {
     FamBegin(ctx, kFamHubBig);
     if (glob) {
       HubGlobalAccumKernel<kInt, V><<<std::min<unsigned>(h.num_glob_items, sms * 8), kGlobThreads, 0,
@@ -1127,7 +1127,7 @@ Status PrepareHubKernels() {
 }
 
 Status LaunchHubBestMoves(Context* ctx, const BMArgs& a, const HubPlan& plan, HubState& st, bool int_mode,
-                          bool narrow) {
+                          bool narrow, int families) {
   if (plan.num_hubs == 0) return Status::Ok();
   HubArgs h;
   h.a = a;
@@ -1165,11 +1165,11 @@ Status LaunchHubBestMoves(Context* ctx, const BMArgs& a, const HubPlan& plan, Hu
   h.gpart_id = st.gpart_id.p;
   h.gdone = st.gdone.p;
   if (a.async) {
-    if (!int_mode) return LaunchHubT<false, true, double>(ctx, h, plan.num_small, plan.num_small_wide);
-    return narrow ? LaunchHubT<true, true, int>(ctx, h, plan.num_small, plan.num_small_wide) : LaunchHubT<true, true, long long>(ctx, h, plan.num_small, plan.num_small_wide);
+    if (!int_mode) return LaunchHubT<false, true, double>(ctx, h, plan.num_small, plan.num_small_wide, families);
+    return narrow ? LaunchHubT<true, true, int>(ctx, h, plan.num_small, plan.num_small_wide, families) : LaunchHubT<true, true, long long>(ctx, h, plan.num_small, plan.num_small_wide, families);
   }
-  if (!int_mode) return LaunchHubT<false, false, double>(ctx, h, plan.num_small, plan.num_small_wide);
-  return narrow ? LaunchHubT<true, false, int>(ctx, h, plan.num_small, plan.num_small_wide) : LaunchHubT<true, false, long long>(ctx, h, plan.num_small, plan.num_small_wide);
+  if (!int_mode) return LaunchHubT<false, false, double>(ctx, h, plan.num_small, plan.num_small_wide, families);
+  return narrow ? LaunchHubT<true, false, int>(ctx, h, plan.num_small, plan.num_small_wide, families) : LaunchHubT<true, false, long long>(ctx, h, plan.num_small, plan.num_small_wide, families);
 }
 
 }  // namespace pcc

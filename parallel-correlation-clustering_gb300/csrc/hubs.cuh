@@ -91,8 +91,12 @@ Status BuildHubPlan(Context* ctx, const DevGraph& g, const BinSet& bins, HubPlan
 Status PrepareHubKernels();
 Status AllocHubState(Context* ctx, const HubPlan& plan, HubState* st);
 // narrow: INT mode with every neighbour-cluster sum below 2^31 in
-// magnitude, so the tables hold 32-bit sums.
+// magnitude, so the tables hold 32-bit sums.  families: kLaunchSmallHubs
+// (degree <= 4096, one CTA per hub) and/or kLaunchBigHubs (the partitioned
+// and global paths).
+constexpr int kLaunchSmallHubs = 4;
+constexpr int kLaunchBigHubs = 8;
 Status LaunchHubBestMoves(Context* ctx, const BMArgs& a, const HubPlan& plan, HubState& st, bool int_mode,
-                          bool narrow);
+                          bool narrow, int families = kLaunchSmallHubs | kLaunchBigHubs);
 
 }  // namespace pcc

@@ -13,6 +13,7 @@
 // counters once per best-move round and once per level.
 #include <chrono>
 #include <cmath>
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -27,6 +28,10 @@ Status CompressGraph(Context* ctx, const DevGraph& g, const uint32_t* C, const d
 Status FindClusterMoves(Context* ctx, const DevGraph& g, const uint32_t* C, const double* k, const double* K,
                         double res, double offset, bool exact_sums, uint32_t* moves, uint32_t* movers,
                         DevCounters* ctr);
+Status AsyncSetMoves(Context* ctx, const SetMoveArgs& a, const std::function<Status(uint32_t)>& vertex_moves);
+Status ComputeSubclustersDevice(Context* ctx, const DevGraph& g, const uint32_t* C, int method, double res,
+                                double offset, DBuf<uint32_t>* sub, DBuf<uint64_t>* next, uint32_t* num_clusters,
+                                uint64_t* total);
 
 namespace {
 
@@ -109,6 +114,22 @@ bool IntegralWeights(const double* w, uint32_t n) {
 }
 
 // cluster_ids[i] = C[cluster_ids[i]] (FlattenClustering).
+// The starting cluster of every vertex of a level compressed by subcluster
+// id: the cluster whose block [next[i], next[i + 1]) holds the id.
+__global__ void BlockOfKernel(uint32_t n, const uint64_t* __restrict__ next, uint32_t G, uint32_t* __restrict__ out) {
+  for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += uint64_t(gridDim.x) * blockDim.x) {
+    uint32_t lo = 0, hi = G;
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (next[mid] <= j) lo = mid;
+      else hi = mid;
+    }
+    out[j] = lo;
+  }
+}
+
+__global__ void AddU32Kernel(uint32_t* p, uint32_t x) { *p += x; }
+
 __global__ void FlattenKernel(uint32_t n, uint32_t* ids, const uint32_t* __restrict__ C) {
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
     ids[i] = C[ids[i]];
@@ -557,6 +578,9 @@ struct Level {
   // its value is 0 and no vertex can join it.
   const BinSet* bins = nullptr;
   bool int_mode = false;
+  // Subclustering: the vertex of the next level every vertex became (its
+  // subcluster id); empty when the level was compressed by cluster id.
+  DBuf<uint32_t> sub;
   // Per-vertex resolution (unions of graphs with different resolutions).
   DBuf<double> vres;
   DBuf<float> vres32;
@@ -632,6 +656,13 @@ class Engine {
     if (cfg_.async) {
       PCC_RETURN_IF_ERROR(free_ids_.Alloc(ctx_, nn));
       PCC_RETURN_IF_ERROR(free_ctr_.Alloc(ctx_, 2));
+      if (cfg_.clustering_moves_method == PCC_DEFAULT_CLUSTER_MOVES) {
+        PCC_RETURN_IF_ERROR(sm_front_.Alloc(ctx_, nn));
+        PCC_RETURN_IF_ERROR(sm_moved_.Alloc(ctx_, nn));
+        PCC_RETURN_IF_ERROR(sm_dummy_.Alloc(ctx_, nn));
+        PCC_RETURN_IF_ERROR(sm_front_.Zero());
+        PCC_RETURN_IF_ERROR(sm_moved_.Zero());
+      }
     }
     PCC_RETURN_IF_ERROR(ctr_.Alloc(ctx_, 1));
     PCC_RETURN_IF_ERROR(ctr_.Zero());
@@ -765,11 +796,16 @@ class Engine {
     // the moves of the waves before it.
     a.waves = cfg_.async ? kAsyncWaves : 1;
     a.wave_salt = static_cast<uint32_t>(cfg_.random_seed * 0x9E3779B97F4A7C15ull >> 32) ^ (stamp_ * 0x85EBCA6Bu);
-    for (uint32_t w = 0; w < a.waves; ++w) {
-      a.wave = w;
-      PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx_, a, bins.list.p, bins.counts.p, bins.counts.p + kNumBins,
-                                          bins.host_counts, L->int_mode, g.max_deg));
-      PCC_RETURN_IF_ERROR(LaunchHubBestMoves(ctx_, a, *g.hub_plan, hub_state_, L->int_mode, a.narrow != 0));
+
+    if (!cfg_.async && !ctx_->detailed_timing && ctx_->overlap_families) {
+      PCC_RETURN_IF_ERROR(OverlappedBestMoves(L, a));
+    } else {
+      for (uint32_t w = 0; w < a.waves; ++w) {
+        a.wave = w;
+        PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx_, a, bins.list.p, bins.counts.p, bins.counts.p + kNumBins,
+                                            bins.host_counts, L->int_mode, g.max_deg));
+        PCC_RETURN_IF_ERROR(LaunchHubBestMoves(ctx_, a, *g.hub_plan, hub_state_, L->int_mode, a.narrow != 0));
+      }
     }
     timer_.End(kPhaseBestMoves);
 
@@ -798,6 +834,8 @@ class Engine {
       }
       PCC_RETURN_IF_ERROR(LaunchCheck());
       if (cfg_.clustering_moves_method == PCC_DEFAULT_CLUSTER_MOVES) PCC_RETURN_IF_ERROR(WholeClusterMoves(L));
+    } else if (cfg_.clustering_moves_method == PCC_DEFAULT_CLUSTER_MOVES) {
+      PCC_RETURN_IF_ERROR(AsyncWholeClusterMoves(L, a));
     }
     timer_.End(kPhaseApply);
     if (cfg_.move_method == PCC_ALL_MOVE) return Status::Ok();
@@ -844,6 +882,43 @@ class Engine {
     return Status::Ok();
   }
 
+  // The best-move families of one synchronous round as parallel branches:
+  // big hubs, warps and small hubs on side streams forked from the context
+  // stream, the lane groups on the context stream, then a join.  The
+  // families read the same round state and write disjoint per-vertex
+  // outputs (moves, moved stamps) plus atomic counters and the atomic
+  // movers list, so their order does not matter.  The join runs even when
+  // a launch failed, so a stream capture is never left with unjoined work.
+  Status OverlappedBestMoves(Level* L, const BMArgs& a) {
+    const DevGraph& g = *L->g;
+    const BinSet& bins = *L->bins;
+    PCC_RETURN_IF_ERROR(ctx_->EnsureSideStreams());
+    PCC_CUDA(cudaEventRecord(ctx_->fork_ev, ctx_->stream));
+    for (int i = 0; i < Context::kSideStreams; ++i) PCC_CUDA(cudaStreamWaitEvent(ctx_->side[i], ctx_->fork_ev, 0));
+    Status st;
+    {
+      OnSideStream on(ctx_, 0);
+      st = LaunchHubBestMoves(ctx_, a, *g.hub_plan, hub_state_, L->int_mode, a.narrow != 0, kLaunchBigHubs);
+    }
+    if (st.ok()) {
+      OnSideStream on(ctx_, 1);
+      st = LaunchBestMoves(ctx_, a, bins.list.p, bins.counts.p, bins.counts.p + kNumBins, bins.host_counts,
+                           L->int_mode, g.max_deg, kLaunchWarps);
+    }
+    if (st.ok()) {
+      OnSideStream on(ctx_, 2);
+      st = LaunchHubBestMoves(ctx_, a, *g.hub_plan, hub_state_, L->int_mode, a.narrow != 0, kLaunchSmallHubs);
+    }
+    if (st.ok())
+      st = LaunchBestMoves(ctx_, a, bins.list.p, bins.counts.p, bins.counts.p + kNumBins, bins.host_counts,
+                           L->int_mode, g.max_deg, kLaunchGroups);
+    for (int i = 0; i < Context::kSideStreams; ++i) {
+      PCC_CUDA(cudaEventRecord(ctx_->join_ev[i], ctx_->side[i]));
+      PCC_CUDA(cudaStreamWaitEvent(ctx_->stream, ctx_->join_ev[i], 0));
+    }
+    return st;
+  }
+
   // Whole-cluster moves after the round's vertex moves (DEFAULT_CLUSTER_MOVES,
   // parallel-correlation-clusterer.cc:167-297): the moving clusters'
   // members go through the same apply as vertex movers, and the clusters it
@@ -881,6 +956,54 @@ class Engine {
     RefreshKfKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, L->K.p, L->Kf.p, mod_stamp_.p, stamp_, nullptr);
     PCC_COUNT(1);
     return LaunchCheck();
+  }
+
+  // The async branch of the whole-cluster moves (parallel-correlation-
+  // clusterer.cc:255-268): every cluster's members, fixed after the round's
+  // vertex moves, move as a set (AsyncSetMoves); one-member sets take the
+  // vertex AsyncMove through the async best-move kernels, evaluated over the
+  // wave's marked vertices with their moved flags redirected.
+  Status AsyncWholeClusterMoves(Level* L, const BMArgs& round_args) {
+    const DevGraph& g = *L->g;
+    const BinSet& bins = *L->bins;
+    const bool exact = L->int_mode && static_cast<double>(g.m) * (g.max_abs_w + std::fabs(cfg_.edge_weight_offset)) <
+                                          9007199254740992.0;
+    SetMoveArgs sm{};
+    sm.g = &g;
+    sm.C = L->C.p;
+    sm.s = L->s.p;
+    sm.k = L->k.p;
+    sm.K = L->K.p;
+    sm.res = cfg_.resolution;
+    sm.offset = cfg_.edge_weight_offset;
+    sm.exact_sums = exact;
+    sm.waves = kAsyncWaves;
+    sm.salt = round_args.wave_salt ^ 0xA511E9B3u;
+    sm.free_ids = free_ids_.p;
+    sm.free_ctr = free_ctr_.p;
+    sm.free_cap = g.n;
+    sm.mod_stamp = mod_stamp_.p;
+    sm.stamp = stamp_;
+    sm.ctr = ctr_.p;
+    sm.aux_front = sm_front_.p;
+    sm.aux_moved = sm_moved_.p;
+    sm.aux_base = sm_val_ + 1;
+    sm_val_ += kAsyncWaves;
+    auto vertex_moves = [&](uint32_t val) -> Status {
+      BMArgs b = round_args;
+      b.waves = 1;
+      b.wave = 0;
+      b.rs = nullptr;
+      b.front_stamp = sm_front_.p;
+      b.front_val = val;
+      b.stamp = val;
+      b.moved_stamp = sm_moved_.p;
+      b.moved_cluster_stamp = sm_dummy_.p;
+      PCC_RETURN_IF_ERROR(LaunchBestMoves(ctx_, b, bins.list.p, bins.counts.p, bins.counts.p + kNumBins,
+                                          bins.host_counts, L->int_mode, g.max_deg));
+      return LaunchHubBestMoves(ctx_, b, *g.hub_plan, hub_state_, L->int_mode, b.narrow != 0);
+    };
+    return AsyncSetMoves(ctx_, sm, vertex_moves);
   }
 
   // One best-move round over `front` (host_counts known), driven from the
@@ -930,6 +1053,7 @@ class Engine {
     const DevGraph& g = *L->g;
     PCC_RETURN_IF_ERROR(PrepareBestMoveKernels());
     PCC_RETURN_IF_ERROR(PrepareHubKernels());
+    PCC_RETURN_IF_ERROR(ctx_->EnsureSideStreams());
     RoundState h{};
     h.stamp = stamp_;  // RoundBeginKernel increments it first
     h.front_all = 1;
@@ -1062,19 +1186,22 @@ class Engine {
     } else if (cfg_.clustering_moves_method == PCC_DEFAULT_CLUSTER_MOVES) {
       // One level of up to num_iterations rounds (:487-492), each with
       // whole-cluster moves after the vertex moves.
-      if (cfg_.async)
-        return MakeError(PCC_UNIMPLEMENTED, "DEFAULT_CLUSTER_MOVES with async moves is not available");
       num_iterations = 1;
       num_inner = cfg_.num_iterations > 0 ? cfg_.num_iterations : 20;
     } else {
       return MakeError(PCC_UNIMPLEMENTED,
                        "Correlation clustering moves must be DEFAULT_CLUSTER_MOVES or LOUVAIN.");
     }
-    if (cfg_.subclustering_method != PCC_NONE_SUBCLUSTERING)
-      return MakeError(PCC_UNIMPLEMENTED, "subclustering_method other than NONE_SUBCLUSTERING is not available");
+    const int sub_method = cfg_.subclustering_method;
+    if (sub_method < PCC_NONE_SUBCLUSTERING || sub_method > PCC_SLOW_CONNECTIVITY_SUBCLUSTERING)
+      return MakeError(PCC_UNIMPLEMENTED, "unknown subclustering_method");
+    if (sub_method != PCC_NONE_SUBCLUSTERING && cfg_.clustering_moves_method == PCC_DEFAULT_CLUSTER_MOVES)
+      return MakeError(PCC_UNIMPLEMENTED, "subcluster moves inside DEFAULT_CLUSTER_MOVES rounds are not available");
+    const bool subclusters = sub_method != PCC_NONE_SUBCLUSTERING;
     const bool refine = cfg_.refine != 0;
     const uint32_t n = g0.n;
     PCC_RETURN_IF_ERROR(Init(n, g0.max_deg));
+    bool vertex_ids = false;  // no refine, subclusters: cluster_ids hold vertex ids of the current level
 
     std::vector<std::unique_ptr<Level>> rec;
     if (refine) rec.resize(static_cast<size_t>(num_iterations));
@@ -1093,24 +1220,62 @@ class Engine {
         break;
       }
       res_.levels++;
+      const bool last = iter == num_iterations - 1;
+      // Subclustering before compression (CompressSubclusters,
+      // parallel-correlation-clusterer.cc:436-474).
+      DBuf<uint32_t> sub;
+      DBuf<uint64_t> blocks;
+      uint32_t nclust = 0;
+      uint64_t nsub = 0;
+      if (subclusters && !last)
+        PCC_RETURN_IF_ERROR(ComputeSubclustersDevice(ctx_, *helper->g, helper->C.p, sub_method, cfg_.resolution,
+                                                     cfg_.edge_weight_offset, &sub, &blocks, &nclust, &nsub));
+      const uint32_t* map = (subclusters && !last) ? sub.p : helper->C.p;
       if (!refine) {
-        if (n) FlattenKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, cluster_ids.p, helper->C.p); PCC_COUNT(1);
-      } else if (iter == num_iterations - 1) {
+        if (n) FlattenKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, cluster_ids.p, map); PCC_COUNT(1);
+        vertex_ids = subclusters && !last;
+      } else if (last) {
         rec[static_cast<size_t>(iter)] = std::move(helper);
       }
-      if (iter == num_iterations - 1) break;
+      if (last) break;
       std::unique_ptr<DevGraph> next;
       timer_.Begin(kPhaseCompress);
-      PCC_RETURN_IF_ERROR(CompressGraph(ctx_, *helper->g, helper->C.p, helper->k.p, &next));
+      PCC_RETURN_IF_ERROR(CompressGraph(ctx_, *helper->g, map, helper->k.p, &next));
       timer_.End(kPhaseCompress);
       res_.algo_bytes_compress += CompressBytes(*helper->g, *next);
       DevGraph* ng = next.get();
       std::unique_ptr<Level> nl;
-      PCC_RETURN_IF_ERROR(MakeLevel(ng, std::move(next), ng->node_w.p, false, nullptr, &nl));
+      if (subclusters) {
+        // The next level starts with the subclusters of one cluster together;
+        // a cluster's size is its block size, ids beyond the compressed graph
+        // (the last block's unused tail) included.
+        DBuf<uint32_t> start_labels;
+        const uint32_t n2 = ng->n;
+        PCC_RETURN_IF_ERROR(start_labels.Alloc(ctx_, std::max<uint64_t>(n2, 1)));
+        if (n2) {
+          BlockOfKernel<<<GridFor(ctx_, n2), kT, 0, ctx_->stream>>>(n2, blocks.p, nclust, start_labels.p);
+          PCC_COUNT(1);
+        }
+        PCC_RETURN_IF_ERROR(MakeLevel(ng, std::move(next), ng->node_w.p, false, start_labels.p, &nl));
+        if (nsub > n2 && nclust > 0) {
+          AddU32Kernel<<<1, 1, 0, ctx_->stream>>>(nl->s.p + (nclust - 1), static_cast<uint32_t>(nsub - n2));
+          PCC_COUNT(1);
+        }
+        PCC_RETURN_IF_ERROR(LaunchCheck());
+      } else {
+        PCC_RETURN_IF_ERROR(MakeLevel(ng, std::move(next), ng->node_w.p, false, nullptr, &nl));
+      }
       if (refine) {
+        if (subclusters) helper->sub = std::move(sub);
         rec[static_cast<size_t>(iter)] = std::move(helper);
       }
       helper = std::move(nl);
+    }
+    // No refine, subclusters, and the last level did not move: its starting
+    // clustering names the clusters of the vertices cluster_ids now hold.
+    if (vertex_ids && n) {
+      FlattenKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, cluster_ids.p, helper->C.p);
+      PCC_COUNT(1);
     }
 
     if (refine && iter > 0) {
@@ -1123,8 +1288,8 @@ class Engine {
         const uint32_t ni = Li->g->n, nu = Lu->g->n;
         stamp_++;
         if (ni) {
-          ProjectKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->C.p, Lu->C.p, flat.p, aux_stamp_.p,
-                                                                    stamp_); PCC_COUNT(1);
+          ProjectKernel<<<GridFor(ctx_, ni), kT, 0, ctx_->stream>>>(ni, Li->sub.p ? Li->sub.p : Li->C.p, Lu->C.p,
+                                                                    flat.p, aux_stamp_.p, stamp_); PCC_COUNT(1);
           PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, nu, StampInput{aux_stamp_.p, stamp_},
                                                   StorePrefix<uint32_t>{rank.p}, scan_tiles_,
                                                   static_cast<uint32_t*>(nullptr)));
@@ -1447,6 +1612,10 @@ class Engine {
   DBuf<uint32_t> moves_, movers_, moved_stamp_, mod_stamp_, next_stamp_, new_stamp_, aux_stamp_;
   DBuf<uint32_t> zero_ids_, new_list_;
   DBuf<uint32_t> free_ids_, free_ctr_;  // async: ids of clusters emptied during the level
+  // Async whole-cluster moves: the one-member sets' vertex frontier and moved
+  // flags (values sm_val_ + 1, + 2, ...), and a sink for their cluster flags.
+  DBuf<uint32_t> sm_front_, sm_moved_, sm_dummy_;
+  uint32_t sm_val_ = 0;
   DBuf<uint32_t> scan_tiles_;
   HubState hub_state_;
   DBuf<DevCounters> ctr_;

@@ -251,23 +251,23 @@ static __global__ void __launch_bounds__(kSortThreads) RadixScatterKernel(const 
   __syncwarp();
   const uint64_t tbase = uint64_t(blockIdx.x) * kSortTile;
   const uint64_t wbase = tbase + uint64_t(warp) * 32 * kSortItems;
-  uint64_t k[kSortItems];
-  uint32_t v[kSortItems];
-  uint32_t pos[kSortItems];
+  // Only the digit and the in-warp rank of each item stay in registers
+  // across the block-wide scan (16 bits each); the key and value are read
+  // again for the staging writes (the tile is still in L1/L2), which keeps
+  // the register count, and so the warps resident per SM, in check.
+  uint32_t dp[kSortItems];  // (digit << 16) | rank within the warp's digit run
 #pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
     const uint64_t i = wbase + uint64_t(r) * 32 + lane;
     const bool valid = i < n;
-    k[r] = valid ? keys_in[i] : 0;
-    v[r] = valid ? vals_in[i] : 0;
-    const uint32_t d = valid ? uint32_t((k[r] >> shift) & 255u) : 256u + lane;
+    const uint32_t d = valid ? uint32_t((keys_in[i] >> shift) & 255u) : 256u + lane;
     const unsigned peers = __match_any_sync(kFull, d);
     uint32_t base = 0;
     if (valid) base = wcount[warp][d];
     __syncwarp();
     if (valid && int(lane) == __ffs(peers) - 1) wcount[warp][d] = base + __popc(peers);
     __syncwarp();
-    pos[r] = base + __popc(peers & LaneMaskLt());
+    dp[r] = ((d & 255u) << 16) | (base + __popc(peers & LaneMaskLt()));
   }
   __syncthreads();
   // Thread d: exclusive scan across warps of digit d (in place), the
@@ -295,14 +295,14 @@ static __global__ void __launch_bounds__(kSortThreads) RadixScatterKernel(const 
   for (int w = 0; w < kSortWarps; ++w) wpre += unsigned(w) < warp ? wsum[w] : 0u;
   dstart[d] = wpre + incl - tot;
   __syncthreads();
-#pragma unroll
+#pragma unroll 4
   for (int r = 0; r < kSortItems; ++r) {
     const uint64_t i = wbase + uint64_t(r) * 32 + lane;
     if (i < n) {
-      const uint32_t dg = uint32_t((k[r] >> shift) & 255u);
-      const uint32_t li = dstart[dg] + wcount[warp][dg] + pos[r];
-      sk[li] = k[r];
-      sv[li] = v[r];
+      const uint32_t dg = dp[r] >> 16;
+      const uint32_t li = dstart[dg] + wcount[warp][dg] + (dp[r] & 0xFFFFu);
+      sk[li] = keys_in[i];
+      sv[li] = vals_in[i];
     }
   }
   __syncthreads();

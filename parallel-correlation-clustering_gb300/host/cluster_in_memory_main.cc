@@ -11,7 +11,9 @@
 //   --is_symmetric_graph  accepted for compatibility (the adjacency input is
 //                         symmetric already)
 //   --input_communities   ground-truth communities: prints precision / recall
-// GPU options (no reference counterpart): --device, --hbm_budget_gb.
+// GPU options (no reference counterpart): --device, --hbm_budget_gb,
+// --device_io (default true: the graph file is parsed and the clustering
+// file formatted on the GPU; --nodevice_io uses the host reader and writer).
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -40,10 +42,10 @@ struct Flags {
   }
 };
 
-const char* const kBoolFlags[] = {"float_weighted", "is_symmetric_graph"};
+const char* const kBoolFlags[] = {"float_weighted", "is_symmetric_graph", "device_io"};
 const char* const kKnownFlags[] = {"clusterer_name", "clusterer_config", "input_graph", "output_clustering",
                                    "float_weighted", "is_symmetric_graph", "input_communities", "device",
-                                   "hbm_budget_gb"};
+                                   "hbm_budget_gb", "device_io"};
 
 bool IsBool(const std::string& k) {
   for (const char* b : kBoolFlags)
@@ -113,9 +115,15 @@ Status Main(int argc, char** argv) {
   if (!made.ok()) return made.status();
   std::unique_ptr<pcc_gb300::InMemoryClusterer> clusterer = std::move(made.value());
 
+  const bool device_io = flags.Bool("device_io", true);
   const auto begin_read = std::chrono::steady_clock::now();
-  auto* graph = static_cast<pcc_gb300::CsrGraph*>(clusterer->MutableGraph());
-  s = pcc_gb300::ReadGbbsAdjacencyGraph(flags.Str("input_graph"), flags.Bool("float_weighted", false), graph);
+  if (device_io) {
+    auto* gpu = static_cast<pcc_gb300::ParallelCorrelationClustererGB300*>(clusterer.get());
+    s = gpu->ReadGraphOnDevice(flags.Str("input_graph"), flags.Bool("float_weighted", false));
+  } else {
+    auto* graph = static_cast<pcc_gb300::CsrGraph*>(clusterer->MutableGraph());
+    s = pcc_gb300::ReadGbbsAdjacencyGraph(flags.Str("input_graph"), flags.Bool("float_weighted", false), graph);
+  }
   if (!s.ok()) return s;
   PrintTime(begin_read, std::chrono::steady_clock::now(), "Read graph");
 
@@ -142,7 +150,8 @@ Status Main(int argc, char** argv) {
 
   const std::string out = flags.Str("output_clustering");
   if (!out.empty()) {
-    s = pcc_gb300::WriteClustering(out, *clustering);
+    s = device_io ? pcc_gb300::WriteClusteringOnDevice(out, *clustering, opt.device)
+                  : pcc_gb300::WriteClustering(out, *clustering);
     if (!s.ok()) return s;
   }
   return Status::Ok();

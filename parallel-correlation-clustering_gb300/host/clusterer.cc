@@ -549,8 +549,7 @@ ParallelCorrelationClustererGB300::~ParallelCorrelationClustererGB300() {
   }
 }
 
-Status ParallelCorrelationClustererGB300::EnsureDevice() const {
-  if (!graph_.finished()) return Status(PCC_FAILED_PRECONDITION, "FinishImport has not been called");
+Status ParallelCorrelationClustererGB300::EnsureContext() const {
   if (!ctx_) {
     const pcc_status s = pcc_create(&ctx_, options_.device, options_.hbm_budget_bytes);
     if (s != PCC_OK) {
@@ -558,6 +557,27 @@ Status ParallelCorrelationClustererGB300::EnsureDevice() const {
       return Status(s, "pcc_create failed (no usable GPU)");
     }
   }
+  return Status::Ok();
+}
+
+Status ParallelCorrelationClustererGB300::ReadGraphOnDevice(const std::string& path, bool float_weighted) {
+  PCC_TRY(EnsureContext());
+  pcc_graph* g = nullptr;
+  const pcc_status s = pcc_graph_read_gbbs(ctx_, path.c_str(), float_weighted ? 1 : 0, &g);
+  if (s != PCC_OK) return Status(s, pcc_last_error(ctx_));
+  uint64_t m = 0;
+  int32_t hw = 0;
+  pcc_graph_info(g, &device_nodes_, &m, &hw);
+  if (dgraph_) pcc_graph_free(ctx_, dgraph_);
+  dgraph_ = g;
+  device_graph_only_ = true;
+  return Status::Ok();
+}
+
+Status ParallelCorrelationClustererGB300::EnsureDevice() const {
+  if (device_graph_only_) return Status::Ok();
+  if (!graph_.finished()) return Status(PCC_FAILED_PRECONDITION, "FinishImport has not been called");
+  PCC_TRY(EnsureContext());
   // Re-upload when the graph changed since the last upload.
   if (dgraph_ && (uploaded_nodes_ != graph_.num_nodes() || uploaded_entries_ != graph_.num_entries())) {
     pcc_graph_free(ctx_, dgraph_);
@@ -583,7 +603,7 @@ Status ParallelCorrelationClustererGB300::Run(const ClustererConfig& config,
                                              Clustering* out) const {
   PCC_TRY(EnsureDevice());
   const pcc_config p = ToPccConfig(config);
-  const uint32_t n = graph_.num_nodes();
+  const uint32_t n = num_nodes();
   std::vector<uint32_t> labels(n);
   stats_ = pcc_stats{};
   const uint32_t* init = initial ? initial->data() : nullptr;
@@ -609,8 +629,9 @@ StatusOr<InMemoryClusterer::Clustering> ParallelCorrelationClustererGB300::Clust
 Status ParallelCorrelationClustererGB300::RefineClusters(const ClustererConfig& config,
                                                         Clustering* clustering) const {
   if (!clustering) return Invalid("null clustering");
-  if (!graph_.finished()) return Status(PCC_FAILED_PRECONDITION, "FinishImport has not been called");
-  const uint32_t n = graph_.num_nodes();
+  if (!device_graph_only_ && !graph_.finished())
+    return Status(PCC_FAILED_PRECONDITION, "FinishImport has not been called");
+  const uint32_t n = num_nodes();
   std::vector<uint32_t> init(n, 0xFFFFFFFFu);
   for (size_t c = 0; c < clustering->size(); ++c) {
     for (NodeId v : (*clustering)[c]) {
@@ -757,6 +778,26 @@ Status WriteClustering(const std::string& path, const InMemoryClusterer::Cluster
     f << "\n";
   }
   return Status::Ok();
+}
+
+Status WriteClusteringOnDevice(const std::string& path, const InMemoryClusterer::Clustering& clustering,
+                               int device) {
+  size_t n = 0;
+  for (const auto& c : clustering) n += c.size();
+  std::vector<uint32_t> labels(n, 0xFFFFFFFFu);
+  for (size_t c = 0; c < clustering.size(); ++c)
+    for (auto v : clustering[c]) {
+      if (v >= n || labels[v] != 0xFFFFFFFFu) return Invalid("the clustering must cover nodes 0..n-1 once each");
+      labels[v] = static_cast<uint32_t>(c);
+    }
+  if (n > 0xFFFFFFFFull) return Status(PCC_OUT_OF_RANGE, "more than 2^32 - 1 nodes");
+  pcc_context* ctx = nullptr;
+  pcc_status s = pcc_create(&ctx, device, 0);
+  if (s != PCC_OK) return Status(s, "pcc_create failed (no usable GPU)");
+  s = pcc_write_clustering(ctx, path.c_str(), static_cast<uint32_t>(n), labels.data());
+  const std::string msg = s == PCC_OK ? "" : pcc_last_error(ctx);
+  pcc_destroy(ctx);
+  return Status(s, msg);
 }
 
 Status ReadCommunities(const std::string& path, std::vector<std::vector<uint32_t>>* communities) {

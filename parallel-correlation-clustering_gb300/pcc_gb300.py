@@ -292,6 +292,15 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.pcc_best_moves.restype = ctypes.c_int
     lib.pcc_compress.argtypes = [vp, vp, P(ctypes.c_uint32), P(ctypes.c_double), P(vp)]
     lib.pcc_compress.restype = ctypes.c_int
+    lib.pcc_graph_parse_gbbs.argtypes = [vp, ctypes.c_char_p, ctypes.c_uint64, ctypes.c_int32, P(vp)]
+    lib.pcc_graph_parse_gbbs.restype = ctypes.c_int
+    lib.pcc_graph_read_gbbs.argtypes = [vp, ctypes.c_char_p, ctypes.c_int32, P(vp)]
+    lib.pcc_graph_read_gbbs.restype = ctypes.c_int
+    lib.pcc_format_clustering.argtypes = [vp, ctypes.c_uint32, P(ctypes.c_uint32), ctypes.c_char_p,
+                                          ctypes.c_uint64, P(ctypes.c_uint64)]
+    lib.pcc_format_clustering.restype = ctypes.c_int
+    lib.pcc_write_clustering.argtypes = [vp, ctypes.c_char_p, ctypes.c_uint32, P(ctypes.c_uint32)]
+    lib.pcc_write_clustering.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -352,6 +361,39 @@ class Context:
             self._h, g.n, g.m, _ptr(off, ctypes.c_uint64), _ptr(nbr, ctypes.c_uint32),
             _ptr(w, ctypes.c_float), ctypes.byref(h)))
         return DeviceGraph(self, h)
+
+
+    def parse_gbbs(self, text: bytes, float_weighted: bool) -> "DeviceGraph":
+        """pcc_graph_parse_gbbs: GBBS adjacency text (bytes) parsed on the
+        device into a resident graph."""
+        h = ctypes.c_void_p()
+        self.check(self.lib.pcc_graph_parse_gbbs(self._h, text, len(text), 1 if float_weighted else 0,
+                                                 ctypes.byref(h)))
+        return DeviceGraph(self, h)
+
+    def read_gbbs(self, path: str, float_weighted: bool) -> "DeviceGraph":
+        """pcc_graph_read_gbbs: a GBBS adjacency file parsed on the device."""
+        h = ctypes.c_void_p()
+        self.check(self.lib.pcc_graph_read_gbbs(self._h, os.fsencode(path), 1 if float_weighted else 0,
+                                                ctypes.byref(h)))
+        return DeviceGraph(self, h)
+
+    def format_clustering(self, labels) -> bytes:
+        """pcc_format_clustering: the clustering file's text (WriteClustering
+        format) for labels (cluster index per node)."""
+        lab = np.ascontiguousarray(labels, dtype=np.uint32)
+        length = ctypes.c_uint64()
+        self.check(self.lib.pcc_format_clustering(self._h, lab.size, _ptr(lab, ctypes.c_uint32), None, 0,
+                                                  ctypes.byref(length)))
+        buf = ctypes.create_string_buffer(max(int(length.value), 1))
+        self.check(self.lib.pcc_format_clustering(self._h, lab.size, _ptr(lab, ctypes.c_uint32), buf,
+                                                  length.value, ctypes.byref(length)))
+        return buf.raw[:int(length.value)]
+
+    def write_clustering(self, path: str, labels) -> None:
+        """pcc_write_clustering: WriteClustering formatted on the device."""
+        lab = np.ascontiguousarray(labels, dtype=np.uint32)
+        self.check(self.lib.pcc_write_clustering(self._h, os.fsencode(path), lab.size, _ptr(lab, ctypes.c_uint32)))
 
 
 class DeviceGraph:

@@ -26,8 +26,11 @@ def _read_clustering(path):
     return out
 
 
+@pytest.mark.parametrize("device_io", [True, False])
 @pytest.mark.parametrize("case", ["sbm_corr", "sbm_mod", "lfr_weighted"])
-def test_cli_matches_c_abi(ctx, tmp_path, case):
+def test_cli_matches_c_abi(ctx, tmp_path, case, device_io):
+    """--device_io (the default) parses the graph and formats the clustering
+    on the GPU; --nodevice_io uses the host reader and writer."""
     if case == "lfr_weighted":
         g, truth = G.lfr(5000, mean_degree=15, dmax=300, seed=3)
         name, objective = "ParallelCorrelationClusterer", 0
@@ -55,10 +58,15 @@ def test_cli_matches_c_abi(ctx, tmp_path, case):
             f"--output_clustering={out}", f"--input_communities={cpath}"]
     if g.weights is not None:
         args.append("--float_weighted")
+    if not device_io:
+        args.append("--nodevice_io")
     r = subprocess.run(args, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert "Avg precision:" in r.stdout and "Avg recall:" in r.stdout
     got = _read_clustering(out)
+    with open(out) as f:
+        text_out = f.read()
+    assert text_out == "".join("".join(f"{v}\t" for v in c) + "\n" for c in got)
 
     cfg = P.make_config(**kw)
     dg = ctx.upload(g)

@@ -319,11 +319,12 @@ def test_errors_are_status_codes(ctx, graphs):
     with pytest.raises(P.PccError) as e:
         P.correlation_cluster(dg, P.make_config(clustering_moves_method=7))
     assert e.value.code == 12  # UNIMPLEMENTED, as the reference
-    with pytest.raises(P.PccError) as e:
-        P.correlation_cluster(dg, P.make_config(subclustering_method=1))
+    with pytest.raises(P.PccError) as e:  # subcluster moves inside cluster-move rounds are not built
+        P.correlation_cluster(dg, P.make_config(subclustering_method=1,
+                                                clustering_moves_method=P.DEFAULT_CLUSTER_MOVES))
     assert e.value.code == 12
-    with pytest.raises(P.PccError) as e:  # async whole-cluster moves are not built
-        P.correlation_cluster(dg, P.make_config(clustering_moves_method=P.DEFAULT_CLUSTER_MOVES, async_=True))
+    with pytest.raises(P.PccError) as e:
+        P.correlation_cluster(dg, P.make_config(subclustering_method=9))
     assert e.value.code == 12
     bad = np.full(g.n, g.n + 5, np.uint32)
     with pytest.raises(P.PccError) as e:
@@ -397,24 +398,32 @@ def test_best_moves_certified_paths(ctx, graphs, name, weights):
             np.testing.assert_array_equal(m_g, m_o)
 
 
-@pytest.mark.parametrize("name,kind,res,move", [
-    ("sbm2k", "corr", 0.01, P.NBHR_CLUSTER_MOVE),
-    ("rmat16", "mod", 1.0, P.NBHR_MOVE),
-    ("lfr20k_real", "corr", 0.1, P.NBHR_CLUSTER_MOVE),
+@pytest.mark.parametrize("name,kind,res,move,permute", [
+    ("sbm2k", "corr", 0.01, P.NBHR_CLUSTER_MOVE, True),
+    ("rmat16", "mod", 1.0, P.NBHR_MOVE, True),
+    ("lfr20k_real", "corr", 0.1, P.NBHR_CLUSTER_MOVE, True),
+    ("sbm2k", "corr", 0.01, P.NBHR_CLUSTER_MOVE, False),
+    ("rmat16", "mod", 1.0, P.NBHR_MOVE, False),
 ])
-def test_async_mean_objective_matches_oracle(ctx, graphs, name, kind, res, move):
+def test_async_mean_objective_matches_oracle(ctx, graphs, name, kind, res, move, permute):
     """Async mode is nondeterministic in the reference too (AsyncMove,
     parallel-correlation-clusterer-internal.cc:371-403), so quality is
-    compared as a mean over seeds: the GPU's mean objective must lie within
-    0.5% of the oracle's async mean, either way.  Twenty seeds keep the
-    standard error of each mean near 0.1-0.15%, well inside the window.
+    compared as a mean over seeds.  The reference's async quality also moves
+    with its worker count (the oracle's RMAT-16 mean: 0.09806 on one worker,
+    0.0975-0.0978 on 8-16), so the oracle runs on one worker: the reference's
+    algorithm without scheduler noise, deterministic per seed.  Permuted
+    rounds (vertexMapPermute, parallel-correlation-clusterer.cc:69-109): the
+    GPU's mean objective over 20 seeds must lie within 0.5% of the oracle's,
+    either way.  Unpermuted rounds: the GPU's hashed waves are not the
+    reference's id order, so the GPU mean must not be more than 0.5% worse.
     Every GPU objective is first recomputed by the oracle from the GPU's
     labels."""
     g = graphs[name]
     dg, og = _both(ctx, g)
     gpu, cpu = [], []
+    O.set_threads(1)
     for seed in range(ASYNC_SEEDS):
-        cfg = P.make_config(resolution=res, refine=True, async_=True, move_method=move, permute=True,
+        cfg = P.make_config(resolution=res, refine=True, async_=True, move_method=move, permute=permute,
                             random_seed=seed + 1)
         if kind == "mod":
             lab, sg = P.modularity_cluster(dg, cfg)
@@ -430,8 +439,13 @@ def test_async_mean_objective_matches_oracle(ctx, graphs, name, kind, res, move)
             assert q == pytest.approx(sg["objective"], rel=1e-9, abs=1e-9)
             gpu.append(q)
             cpu.append(so["objective"])
+    O.set_threads(0)
     mg, mc = float(np.mean(gpu)), float(np.mean(cpu))
-    assert abs(mg - mc) <= ASYNC_WINDOW * abs(mc), (name, mg, mc, (mg - mc) / abs(mc), gpu, cpu)
+    info = (name, permute, mg, mc, (mg - mc) / abs(mc), gpu, cpu)
+    if permute:
+        assert abs(mg - mc) <= ASYNC_WINDOW * abs(mc), info
+    else:
+        assert mg >= mc - ASYNC_WINDOW * abs(mc), info
 
 
 @pytest.mark.parametrize("move", [P.NBHR_CLUSTER_MOVE, P.NBHR_MOVE, P.ALL_MOVE])
@@ -464,3 +478,87 @@ def test_device_round_loop_matches_host_loop(graphs, move, refine):
             dg.free()
     finally:
         c.close()
+
+
+def test_overlapped_families_match_serial(graphs, monkeypatch):
+    """Synchronous rounds launch the best-move families (lane groups, warps,
+    small hubs, big hubs) as parallel stream branches; with
+    PCC_SERIAL_FAMILIES=1 they run one after another.  Labels and every
+    counter must be identical, in the device-side loop and host-driven."""
+    c_par = P.Context(0)
+    monkeypatch.setenv("PCC_SERIAL_FAMILIES", "1")
+    c_ser = P.Context(0)
+    monkeypatch.delenv("PCC_SERIAL_FAMILIES")
+    try:
+        for name, kind, res, move in [("rmat16", "mod", 1.0, P.NBHR_MOVE), ("hubs100k", "corr", 0.05, P.ALL_MOVE),
+                                      ("sbm3k_int", "corr", 0.05, P.NBHR_CLUSTER_MOVE),
+                                      ("lfr20k_real", "corr", 0.1, P.NBHR_CLUSTER_MOVE)]:
+            cfg = P.make_config(resolution=res, refine=True, move_method=move)
+            out = []
+            for c in (c_par, c_ser):
+                dg = c.upload(graphs[name])
+                run = P.modularity_cluster if kind == "mod" else P.correlation_cluster
+                out.append(run(dg, cfg))
+                dg.free()
+            (l0, s0), (l1, s1) = out
+            np.testing.assert_array_equal(l0, l1, err_msg=name)
+            for key in ("objective", "modularity", "num_clusters", "levels", "rounds", "edge_visits", "moves"):
+                assert s0[key] == s1[key], (name, key, s0[key], s1[key])
+    finally:
+        c_par.close()
+        c_ser.close()
+
+
+@pytest.mark.parametrize("name,res,move", [
+    ("sbm2k", 0.01, P.NBHR_CLUSTER_MOVE),
+    ("lfr20k_real", 0.1, P.NBHR_CLUSTER_MOVE),
+])
+def test_async_cluster_moves_mean_objective(ctx, graphs, name, res, move):
+    """Async whole-cluster moves (DEFAULT_CLUSTER_MOVES with async:
+    parallel-correlation-clusterer.cc:255-268, AsyncMove(moving_nodes) at
+    parallel-correlation-clusterer-internal.cc:405-446) are nondeterministic
+    in the reference; the oracle restates them as every cluster moving in
+    turn on live state, with the vertex moves on one worker.  The GPU's mean
+    objective over seeds (recomputed by the oracle from the GPU's labels)
+    must lie within 0.5% of the oracle's mean, either way."""
+    g = graphs[name]
+    dg, og = _both(ctx, g)
+    gpu, cpu = [], []
+    O.set_threads(1)
+    for seed in range(ASYNC_SEEDS):
+        cfg = P.make_config(resolution=res, async_=True, move_method=move, permute=True, random_seed=seed + 1,
+                            clustering_moves_method=P.DEFAULT_CLUSTER_MOVES)
+        lab, sg = P.correlation_cluster(dg, cfg)
+        q = O.objective(og, cfg, lab)
+        assert q == pytest.approx(sg["objective"], rel=1e-9, abs=1e-9)
+        _, so = O.correlation_cluster(og, cfg)
+        gpu.append(q)
+        cpu.append(so["objective"])
+    O.set_threads(0)
+    mg, mc = float(np.mean(gpu)), float(np.mean(cpu))
+    assert abs(mg - mc) <= ASYNC_WINDOW * abs(mc), (name, mg, mc, (mg - mc) / abs(mc), gpu, cpu)
+
+
+@pytest.mark.parametrize("method", [1, 2, 3])  # TRIANGLE, CONNECTIVITY, SLOW_CONNECTIVITY
+@pytest.mark.parametrize("name,kind,res", [("sbm2k", "corr", 0.05), ("rmat14", "mod", 1.0), ("sbm3k_int", "corr", 0.1),
+                                           ("lfr20k_real", "corr", 0.1)])
+@pytest.mark.parametrize("refine", [True, False])
+def test_subclustering_matches_oracle(ctx, graphs, method, name, kind, res, refine):
+    """Subclustering before compression (CompressSubclusters,
+    parallel-correlation-clusterer.cc:436-474; ComputeSubcluster and its
+    methods, parallel-correlation-clusterer-internal.cc:784-1120): labels,
+    levels, rounds and edge visits bit-exact against the oracle on integer
+    weights; the objective within 1e-9 on real weights (FP64 mode)."""
+    g = graphs[name]
+    dg, og = _both(ctx, g)
+    cfg = P.make_config(resolution=res, refine=refine, subclustering_method=method, move_method=P.NBHR_MOVE,
+                        louvain_num_iterations=4)
+    run_g = P.modularity_cluster if kind == "mod" else P.correlation_cluster
+    run_o = O.modularity_cluster if kind == "mod" else O.correlation_cluster
+    lab_g, st_g = run_g(dg, cfg)
+    lab_o, st_o = run_o(og, cfg)
+    if g.weights is None or name == "sbm3k_int":
+        np.testing.assert_array_equal(lab_g, lab_o)
+        for key in ("levels", "rounds", "refine_passes", "edge_visits", "num_clusters"):
+            assert st_g[key] == st_o[key], (key, st_g[key], st_o[key])
+    assert st_g["objective"] == pytest.approx(st_o["objective"], rel=REL_TOL, abs=1e-9)

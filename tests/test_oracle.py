@@ -20,6 +20,7 @@ import pytest
 
 import oracle as O
 import pcc_gb300 as P
+import pcc_graphs as G
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
@@ -284,3 +285,134 @@ def test_oracle_compare_communities_brute_force(ci):
     assert gp.tolist() == wp and gr.tolist() == wr
     for key, val in want.items():
         assert got[key] == val, key
+
+
+def _py_subclusters(g, C, method, res, offset):
+    """Independent restatement of ComputeSubcluster over every cluster
+    (parallel-correlation-clusterer-internal.cc:784-1120, with components
+    labelled by their smallest member's local index): (ids, block starts)."""
+    off = g.offsets.astype(np.int64)
+    nbr = g.neighbors.astype(np.int64)
+    rows = [set(nbr[off[v]:off[v + 1]].tolist()) for v in range(g.n)]
+    clusters = sorted(set(int(c) for c in C))
+    members = {c: [v for v in range(g.n) if C[v] == c] for c in clusters}
+    blocks, labels = [], {}
+    for c in clusters:
+        mem = members[c]
+        local = {v: x for x, v in enumerate(mem)}
+        if method in (1, 2):
+            parent = list(range(len(mem)))
+
+            def find(x):
+                while parent[x] != x:
+                    x = parent[x]
+                return x
+            for x, v in enumerate(mem):
+                for j in range(off[v], off[v + 1]):
+                    u = int(nbr[j])
+                    if C[u] != c:
+                        continue
+                    if method == 1:
+                        ratio = len(rows[v] & rows[u]) / float(len(rows[v]) + len(rows[u]))
+                        if not ratio > 0.25:
+                            continue
+                    a, b = find(x), find(local[u])
+                    if a != b:
+                        parent[max(a, b)] = min(a, b)
+            lab = [find(x) for x in range(len(mem))]
+            block = len(mem) if method == 2 else max(lab) + 1
+        else:
+            size = len(mem)
+            tmp = list(range(size))
+            single = [0] * size
+            outside = lambda u: C[u] != c  # noqa: E731
+            for i in range(size):
+                if single[i]:
+                    continue
+                cv = mem[i]
+                if sum(1 for u in nbr[off[cv]:off[cv + 1]] if outside(int(u))) < size - 1:
+                    continue
+                groups = {}
+                for x, t in enumerate(tmp):
+                    groups.setdefault(t, []).append(x)
+                glist = [groups[t] for t in sorted(groups)]
+                valid = []
+                for curr in glist:
+                    if curr[0] == i:
+                        valid.append(False)
+                        continue
+                    ne = sum(1 for x in curr for u in nbr[off[mem[x]]:off[mem[x] + 1]] if outside(int(u)))
+                    valid.append(ne >= len(curr) * (size - len(curr)))
+                if not any(valid):
+                    continue
+                best, idx, any_left = 0.0, 0, False
+                for j, curr in enumerate(glist):
+                    if not valid[j]:
+                        continue
+                    cs = set(mem[x] for x in curr)
+                    weight = float(sum(1 for u in nbr[off[cv]:off[cv + 1]] if int(u) in cs))
+                    o = offset * len(curr) + res * len(curr)
+                    if weight < o:
+                        continue
+                    any_left = True
+                    if weight - o >= best:
+                        best, idx = weight - o, j
+                if not any_left:
+                    continue
+                tmp[i] = tmp[glist[idx][0]]
+                single[i] = 1
+                single[glist[idx][0]] = 1
+            lab = tmp
+            block = max(lab) + 1
+        blocks.append(block)
+        labels[c] = lab
+    nxt = np.zeros(len(clusters) + 1, np.uint64)
+    nxt[1:] = np.cumsum(blocks)
+    ids = np.zeros(g.n, np.uint32)
+    for gi, c in enumerate(clusters):
+        for x, v in enumerate(members[c]):
+            ids[v] = nxt[gi] + labels[c][x]
+    return ids, nxt
+
+
+@pytest.mark.parametrize("method", [1, 2, 3])
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_subclusters_match_pure_python(method, seed):
+    """Subcluster ids (triangle, connectivity, slow connectivity) of the
+    oracle against an independent Python restatement, on SBM graphs with
+    random coarse clusterings (so clusters hold several components)."""
+    rng = np.random.default_rng(seed)
+    g, blocks = G.sbm(120, 6, 0.25, 0.02, seed)
+    C = np.where(rng.random(g.n) < 0.8, blocks, rng.integers(0, 6, g.n)).astype(np.uint32) * 3
+    og = O.OracleGraph(g)
+    res = [0.0, 0.5, 2.0][seed - 1]
+    ids, nxt = O.subclusters(og, C, method, res, 0.0)
+    want_ids, want_next = _py_subclusters(g, C, method, res, 0.0)
+    np.testing.assert_array_equal(nxt, want_next)
+    np.testing.assert_array_equal(ids, want_ids)
+
+
+def test_subclusters_known_answers():
+    """Two 4-cliques joined by one edge, all in one cluster: connectivity
+    keeps one component (block of 8); the triangle filter keeps the clique
+    edges (ratio 2/6 or 2/7 > 0.25) and cuts the bridge (0/8), giving the two
+    cliques labelled 0 and 4 (block 5).  Two triangles joined by an edge
+    have clique-edge ratios of exactly 1/4, which does not pass."""
+    k4 = [(a, b) for a in range(4) for b in range(a + 1, 4)]
+    g = _csr(8, k4 + [(a + 4, b + 4) for a, b in k4] + [(3, 4)])
+    og = O.OracleGraph(g)
+    C = np.zeros(8, np.uint32)
+    ids, nxt = O.subclusters(og, C, 2)
+    assert ids.tolist() == [0] * 8 and nxt.tolist() == [0, 8]
+    ids, nxt = O.subclusters(og, C, 1)
+    assert ids.tolist() == [0, 0, 0, 0, 4, 4, 4, 4] and nxt.tolist() == [0, 5]
+    t = _csr(6, [(0, 1), (1, 2), (0, 2), (3, 4), (4, 5), (3, 5), (2, 3)])
+    ids, nxt = O.subclusters(O.OracleGraph(t), np.zeros(6, np.uint32), 1)
+    assert ids.tolist() == [0, 1, 2, 3, 4, 5] and nxt.tolist() == [0, 6]
+    # Two clusters, one of them disconnected: components inside each cluster
+    # (cluster 5 = {0, 1, 5}: {0, 1} and {5}; cluster 9 = {2, 3, 4} joined
+    # through 2-3 and 3-4).
+    C2 = np.array([5, 5, 9, 9, 9, 5], np.uint32)
+    ids, nxt = O.subclusters(O.OracleGraph(t), C2, 2)
+    assert nxt.tolist() == [0, 3, 6]
+    assert ids.tolist() == [0, 0, 3, 3, 3, 2]
