@@ -153,6 +153,19 @@ uint64_t pcc_device_peak_bytes(pcc_context* ctx, int32_t reset);
 void pcc_set_detailed_timing(pcc_context* ctx, int32_t on);
 
 /*
+ * Best-move launch shape (no reference counterpart).  Lane-group bins (degree
+ * <= 4, 8, 16, 32) above group_max_degree (4, 8, 16 or 32) run on the warp
+ * kernel; certified (INT-mode, synchronous) warp bins (degree <= 128, 256,
+ * 512, 1000) above cta_min_degree (64, 128, 256, 512, or 1000 for none) run
+ * one CTA per vertex; the grid-stride best-move kernels launch grid_waves
+ * (0.125-16) times one wave of resident CTAs.  (0, 0, 0) returns to the
+ * compiled-in table, chosen per level-graph size class by tune_launch.py.
+ * Results are identical under every setting; only the time changes.
+ */
+pcc_status pcc_set_launch_tuning(pcc_context* ctx, uint32_t group_max_degree, uint32_t cta_min_degree,
+                                 float grid_waves);
+
+/*
  * Graph upload.  Copies a host CSR graph into HBM.  Replaces
  * GbbsGraph::Import/FinishImport (clustering/gbbs-graph.cc:32-76) and the
  * CLI's CopyGraph injection (clustering/cluster-in-memory_main.cc:231-306).
@@ -367,8 +380,10 @@ typedef struct pcc_batch_graph {
  * When the configs differ in resolution only (num_configs == 1 included), are
  * LOUVAIN, synchronous and without subclustering, and the offset is 0 or every
  * objective is correlation, the batch runs as disjoint unions
- * (pcc_cluster_union on one context; stats as documented there).  Otherwise
- * each graph runs on the worker pool and its stats equal a standalone call's.
+ * (pcc_cluster_union on one context; stats as documented there), with the
+ * graphs packed in ascending order of entry count (stable; results and stats
+ * are returned in the caller's order).  Otherwise each graph runs on the
+ * worker pool and its stats equal a standalone call's.
  */
 pcc_status pcc_cluster_batch(int device, uint32_t num_graphs, const pcc_batch_graph* graphs,
                              const pcc_config* configs, uint32_t num_configs,

@@ -628,6 +628,226 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
   FlushFamily(a, kFamWarp, fam_e, fam_v);
 }
 
+// ---------------------------------------------------------------------------
+// One CTA of kCtaWarps warps per vertex (degree 129-1000, INT mode, sync):
+// the same certified decision as CertWarpKernel, with the row and the
+// epilogue split over the CTA's warps.  One table of HC slots per CTA
+// instead of one per warp, so several times more vertices are in flight per
+// SM for the same shared memory, and each vertex's chain of dependent loads
+// and candidate loops is kCtaWarps times shorter.  Inserts claim slots with
+// atomicCAS and add with shared-memory atomics (any order: INT-mode sums
+// are exact); the warp maxima and lexicographic leaders are combined through
+// shared memory.  An uncertain (or replayed) vertex takes WarpExact on warp 0
+// over the whole table, exactly as in the warp kernel.
+// ---------------------------------------------------------------------------
+constexpr int kCtaWarps = 4;
+
+template <int HC, typename V>
+constexpr size_t CertCtaSmem() {
+  return size_t(HC) * (sizeof(V) + 4 + 2);  // vals, keys, used
+}
+
+template <typename V>
+__device__ __forceinline__ V WarpMaxV(V x) {
+  if constexpr (sizeof(V) == 4) {
+    return __reduce_max_sync(kFull, x);
+  } else {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) x = max(x, __shfl_xor_sync(kFull, x, o));
+    return x;
+  }
+}
+
+template <int HC, typename V>
+__global__ void __launch_bounds__(kCtaWarps * 32) CertCtaKernel(BMArgs a, const uint32_t* __restrict__ list,
+                                                               const uint32_t* __restrict__ bin_counts,
+                                                               const uint32_t* __restrict__ bin_starts, int bin) {
+  constexpr int BT = kCtaWarps * 32;
+  extern __shared__ __align__(16) unsigned char smem[];
+  V* vals = reinterpret_cast<V*>(smem);
+  uint32_t* keys = reinterpret_cast<uint32_t*>(smem + size_t(HC) * sizeof(V));
+  uint16_t* used = reinterpret_cast<uint16_t*>(smem + size_t(HC) * (sizeof(V) + 4));
+  __shared__ int stage[kCtaWarps][32];
+  __shared__ uint32_t s_nused;
+  __shared__ V s_max[kCtaWarps];
+  __shared__ float s_u[kCtaWarps];
+  __shared__ V s_ls[kCtaWarps], s_ts[kCtaWarps];
+  __shared__ unsigned long long s_lk[kCtaWarps], s_tk[kCtaWarps];
+  __shared__ uint32_t s_li[kCtaWarps], s_ti[kCtaWarps];
+  const uint32_t count = bin_counts[bin];
+  const uint32_t start = bin_starts[bin];
+  const unsigned tid = threadIdx.x, lane = LaneId(), warp = tid >> 5;
+  unsigned long long fam_e = 0, fam_v = 0;
+  const bool replay = a.out_target != nullptr;
+  const bool unit = a.w == nullptr;
+  for (int i = tid; i < HC; i += BT) {
+    keys[i] = kNone;
+    vals[i] = 0;
+  }
+  if (tid == 0) s_nused = 0;
+  __syncthreads();
+  uint32_t vid = blockIdx.x < count ? list[start + blockIdx.x] : 0u;
+  for (uint64_t idx = blockIdx.x; idx < count; idx += gridDim.x) {
+    const uint64_t nidx = idx + gridDim.x;
+    const uint32_t nvid = nidx < count ? list[start + nidx] : 0u;
+    if (!InFront(a, vid)) {  // uniform over the CTA
+      vid = nvid;
+      continue;
+    }
+    const VertexCtx x = LoadVertex<false>(a, vid);
+    vid = nvid;
+    if (tid == 0) {
+      fam_e += x.d;
+      fam_v += 1;
+    }
+    for (uint32_t e0 = 0; e0 < x.d; e0 += BT * kCertUnroll) {
+      uint32_t uu[kCertUnroll], cc[kCertUnroll];
+      float ww[kCertUnroll];
+#pragma unroll
+      for (int k = 0; k < kCertUnroll; ++k) {
+        const uint32_t e = e0 + BT * k + tid;
+        uu[k] = x.v;
+        ww[k] = 0.f;
+        if (e < x.d) {
+          uu[k] = a.nbr[x.b + e];
+          ww[k] = a.w ? a.w[x.b + e] : 1.0f;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kCertUnroll; ++k) cc[k] = uu[k] != x.v ? __ldg(a.C + uu[k]) : kNone;
+#pragma unroll
+      for (int k = 0; k < kCertUnroll; ++k) {
+        if (e0 + BT * k + 32 * warp >= x.d) break;  // uniform over the warp
+        const bool cand = uu[k] != x.v;
+        const uint32_t cu = cc[k];
+        const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane));
+        const bool leader = cand && int(lane) == __ffs(peers) - 1;
+        uint32_t slot = kNone;
+        bool ins = false;
+        if (leader) {
+          slot = FindOrInsertT<false>(keys, HC, cu, &ins);
+          if (slot == kNone) atomicExch(&a.ctr->error, kErrHashFull);
+        }
+        const unsigned im = __ballot_sync(kFull, ins);
+        if (im) {
+          const int first = __ffs(im) - 1;
+          uint32_t base = 0;
+          if (int(lane) == first) base = atomicAdd(&s_nused, uint32_t(__popc(im)));
+          base = __shfl_sync(kFull, base, first);
+          if (ins) used[base + __popc(im & LaneMaskLt())] = static_cast<uint16_t>(slot);
+        }
+        const int xi = cand ? (WeightToInt(ww[k]) - a.ioffset) : 0;
+        const int Sg = GroupSumInt(peers, xi, unit, leader, stage[warp]);
+        if (slot != kNone) {
+          if constexpr (sizeof(V) == 4)
+            atomicAdd(reinterpret_cast<int*>(&vals[slot]), Sg);
+          else
+            atomicAdd(reinterpret_cast<unsigned long long*>(&vals[slot]),
+                      static_cast<unsigned long long>(static_cast<long long>(Sg)));
+        }
+      }
+    }
+    __syncthreads();  // table complete
+    const uint32_t nused = s_nused;
+    V T = 0;
+    {
+      const uint32_t slot = FindT<false>(keys, HC, x.c);
+      if (slot != kNone) T = vals[slot];
+    }
+    const float k32 = a.kf[x.v];
+    const ChangeApproxT<V> ca = ApproxChange<V>(Res32Of(a, x.v), a.int_nw != 0, k32, a.Kf[x.c], T);
+    const float cabs = ChangeAbsBound(ca);
+    V vmax = sizeof(V) == 4 ? V(INT_MIN) : V(LLONG_MIN);
+    for (uint32_t i = tid; i < nused; i += BT) vmax = max(vmax, vals[used[i]]);
+    vmax = WarpMaxV<V>(vmax);
+    if (lane == 0) s_max[warp] = vmax;
+    __syncthreads();
+    V smax = s_max[0];
+#pragma unroll
+    for (int w = 1; w < kCtaWarps; ++w) smax = max(smax, s_max[w]);
+    float U = -CUDART_INF_F;
+    for (uint32_t i = tid; i < nused; i += BT) {
+      const uint32_t slot = used[i];
+      const FilterVal f = FilterOf<V>(Res32Of(a, x.v), k32, a.Kf[keys[slot]], vals[slot], smax, cabs);
+      if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
+    }
+    U = WarpMaxFinite(U);
+    if (lane == 0) s_u[warp] = U;
+    __syncthreads();
+    U = s_u[0];
+#pragma unroll
+    for (int w = 1; w < kCtaWarps; ++w) U = fmaxf(U, s_u[w]);
+    LexKeyT<V> lead, tail;
+    for (uint32_t i = tid; i < nused; i += BT) {
+      const uint32_t slot = used[i];
+      const uint32_t key = keys[slot];
+      const FilterVal f = FilterOf<V>(Res32Of(a, x.v), k32, a.Kf[key], vals[slot], smax, cabs);
+      if (f.sane && __fadd_rn(f.Y, f.e) < U) {
+        keys[slot] = kNone;  // not a contender: cleared now, skipped later
+        vals[slot] = 0;
+        used[i] = 0xFFFFu;
+        continue;
+      }
+      const unsigned long long ko = KOrder(a.K[key]);
+      const V S = vals[slot];
+      lead.Keep(S, ko, key);
+      tail.Keep(-S, ~ko, key);
+    }
+    if constexpr (sizeof(V) == 4) {
+      LexWarpLeaderInt(lead);
+      LexWarpLeaderInt(tail);
+    } else {
+      LexGroupReduce<32>(lead);
+      LexGroupReduce<32>(tail);
+    }
+    if (lane == 0) {
+      s_ls[warp] = lead.S;
+      s_lk[warp] = lead.K;
+      s_li[warp] = lead.id;
+      s_ts[warp] = tail.S;
+      s_tk[warp] = tail.K;
+      s_ti[warp] = tail.id;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      LexKeyT<V> L, Tl;
+#pragma unroll
+      for (int w = 0; w < kCtaWarps; ++w) {
+        L.Keep(s_ls[w], s_lk[w], s_li[w]);
+        Tl.Keep(s_ts[w], s_tk[w], s_ti[w]);
+      }
+      // One (S, K) class among the contenders iff the lowest-ranked one
+      // (Tl: smallest S, then largest K) is in the leader's class.
+      const bool single = L.id == kNone || (-Tl.S == L.S && ~Tl.K == L.K);
+      int cres = kUncertain;
+      uint32_t ctarget = kNone;
+      if (single) {
+        const float KfA = L.id != kNone ? a.Kf[L.id] : 0.f;
+        cres = CertifyDecision<V>(ca, Res32Of(a, x.v), k32, L.id != kNone, L.S, KfA, L.id, a.n, &ctarget);
+      }
+      const uint32_t cmove = cres == kUncertain ? kNone : CertifiedMove(a, x, ctarget, cres == kCertMove);
+      bool append = false;
+      if (replay || cres == kUncertain) {
+        append = WarpExact<HC, V>(a, x, T, keys, vals, used, nused, replay, cres, cmove);
+      } else if (lane == 0) {
+        append = ApplyCertified(a, x, cmove);
+      }
+      if (lane == 0 && append) a.movers[atomicAdd(&a.ctr->movers, 1u)] = x.v;
+    }
+    __syncthreads();  // the table is read by WarpExact up to here
+    for (uint32_t i = tid; i < nused; i += BT) {
+      const uint32_t slot = used[i];
+      if (slot != 0xFFFFu) {
+        keys[slot] = kNone;
+        vals[slot] = 0;
+      }
+    }
+    if (tid == 0) s_nused = 0;
+    __syncthreads();
+  }
+  if (warp == 0) FlushFamily(a, kFamWarp, fam_e, fam_v);
+}
+
 // Sets the kernel's dynamic shared-memory limit and queries its resident
 // CTAs per SM once per process (the runtime calls take a lock that
 // serialises concurrent contexts).  Each kernel is launched with one fixed
@@ -654,26 +874,70 @@ template <bool kInt, bool kAsync>
 Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint32_t* counts,
                  const uint32_t* starts, const uint32_t* host_counts, uint32_t max_deg, int families) {
   const unsigned sms = unsigned(ctx->num_sms);
+  const LaunchTuning tune = TuningFor(ctx, a.n);
+  // Resident CTAs of one wave scaled by the tuned wave count.
+  auto waves = [&](unsigned one_wave) -> unsigned {
+    return std::max(1u, unsigned(double(one_wave) * double(tune.grid_waves) + 0.5));
+  };
   auto grid = [&](int bin, uint64_t per_block, unsigned cap) -> unsigned {
     if (!host_counts) return cap;
     return Blocks(host_counts[bin], unsigned(per_block), cap);
   };
+  // Warp bins above the tuned degree run one CTA per vertex (INT mode).
+  auto on_cta = [&](int bin) {
+    return bin >= kBinW128 && bin <= kBinW1000 && kBinMaxDeg[bin] > tune.cta_min_degree;
+  };
+  // Lane-group bins above the tuned degree run on the 256-slot warp kernel,
+  // as part of the warp family (launched, timed and counted with it).
+  auto routed = [&](int bin) { return bin <= kBinG32 && kBinMaxDeg[bin] > tune.group_max_degree; };
   auto want = [&](int bin) {
-    const int fam = bin <= kBinG32 ? kLaunchGroups : kLaunchWarps;
+    const int fam = bin <= kBinG32 && !routed(bin) ? kLaunchGroups : kLaunchWarps;
     return (families & fam) && (!host_counts || host_counts[bin] > 0);
   };
   cudaStream_t st = ctx->stream;
   constexpr bool kCert = kInt && !kAsync;
+  // Grid-stride kernels: at most one wave of resident CTAs, so no partial
+  // last wave.
+  auto warp_bin = [&](auto k, size_t smem, int bin, unsigned cap) -> Status {
+    if (!want(bin)) return Status::Ok();
+    int per_sm = 0;
+    PCC_RETURN_IF_ERROR(SetSmem(k, smem, kWarpKernelWarps * 32, &per_sm));
+    if (per_sm > 0) cap = sms * unsigned(per_sm);
+    k<<<grid(bin, kWarpKernelWarps, waves(cap)), kWarpKernelWarps * 32, smem, st>>>(a, list, counts, starts, bin);
+    PCC_COUNT(1);
+    return Status::Ok();
+  };
+  auto cta_bin = [&](auto k, size_t smem, int bin) -> Status {
+    if (!want(bin)) return Status::Ok();
+    int per_sm = 0;
+    PCC_RETURN_IF_ERROR(SetSmem(k, smem, kCtaWarps * 32, &per_sm));
+    const unsigned cap = sms * unsigned(per_sm > 0 ? per_sm : 4);
+    k<<<grid(bin, 1, waves(cap)), kCtaWarps * 32, smem, st>>>(a, list, counts, starts, bin);
+    PCC_COUNT(1);
+    return Status::Ok();
+  };
+  // A certified warp bin on the warp kernel or, above the tuned degree, the
+  // CTA kernel of the same table size.
+  auto cert_bin = [&](auto kw, size_t smem_w, auto kc, size_t smem_c, int bin, unsigned cap) -> Status {
+    return on_cta(bin) ? cta_bin(kc, smem_c, bin) : warp_bin(kw, smem_w, bin, cap);
+  };
+  // The routed lane-group bins, on the warp kernel of the smallest table.
+  auto routed_bins = [&](auto k, size_t smem, unsigned cap) -> Status {
+    for (int b = kBinG4; b <= kBinG32; ++b)
+      if (routed(b)) PCC_RETURN_IF_ERROR(warp_bin(k, smem, b, cap));
+    return Status::Ok();
+  };
   int ng = 0;
-  for (int b = kBinG4; b <= kBinG32; ++b) ng += want(b) ? 1 : 0;
+  for (int b = kBinG4; b <= kBinG32; ++b) ng += want(b) && !routed(b) ? 1 : 0;
   if (families & kLaunchGroups) FamBegin(ctx, kFamGroup);
   if constexpr (kCert) {
     // One wave of resident CTAs (grid-stride kernels).
     auto group_bin = [&](auto k, int bin, uint64_t per_block) -> Status {
-      if (!want(bin)) return Status::Ok();
+      if (!want(bin) || routed(bin)) return Status::Ok();
       int per_sm = 0;
       PCC_RETURN_IF_ERROR(SetSmem(k, 0, 256, &per_sm));
-      k<<<grid(bin, per_block, sms * unsigned(per_sm > 0 ? per_sm : 8)), 256, 0, st>>>(a, list, counts, starts, bin);
+      k<<<grid(bin, per_block, waves(sms * unsigned(per_sm > 0 ? per_sm : 8))), 256, 0, st>>>(a, list, counts, starts,
+                                                                                          bin);
       PCC_COUNT(1);
       return Status::Ok();
     };
@@ -682,55 +946,59 @@ Status LaunchAll(Context* ctx, const BMArgs& a, const uint32_t* list, const uint
     PCC_RETURN_IF_ERROR(group_bin(CertGroupKernel<16>, kBinG16, 16));
     PCC_RETURN_IF_ERROR(group_bin(CertGroupKernel<32>, kBinG32, 8));
   } else {
-    if (want(kBinG4)) {
-      BestMoveGroupKernel<4, kInt, kAsync><<<grid(kBinG4, 64, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG4);
+    if (want(kBinG4) && !routed(kBinG4)) {
+      BestMoveGroupKernel<4, kInt, kAsync><<<grid(kBinG4, 64, waves(sms * 8)), 256, 0, st>>>(a, list, counts, starts,
+                                                                                            kBinG4);
       PCC_COUNT(1);
     }
-    if (want(kBinG8)) {
-      BestMoveGroupKernel<8, kInt, kAsync><<<grid(kBinG8, 32, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG8);
+    if (want(kBinG8) && !routed(kBinG8)) {
+      BestMoveGroupKernel<8, kInt, kAsync><<<grid(kBinG8, 32, waves(sms * 8)), 256, 0, st>>>(a, list, counts, starts,
+                                                                                            kBinG8);
       PCC_COUNT(1);
     }
-    if (want(kBinG16)) {
-      BestMoveGroupKernel<16, kInt, kAsync><<<grid(kBinG16, 16, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG16);
+    if (want(kBinG16) && !routed(kBinG16)) {
+      BestMoveGroupKernel<16, kInt, kAsync><<<grid(kBinG16, 16, waves(sms * 8)), 256, 0, st>>>(a, list, counts, starts,
+                                                                                            kBinG16);
       PCC_COUNT(1);
     }
-    if (want(kBinG32)) {
-      BestMoveGroupKernel<32, kInt, kAsync><<<grid(kBinG32, 8, sms * 8), 256, 0, st>>>(a, list, counts, starts, kBinG32);
+    if (want(kBinG32) && !routed(kBinG32)) {
+      BestMoveGroupKernel<32, kInt, kAsync><<<grid(kBinG32, 8, waves(sms * 8)), 256, 0, st>>>(a, list, counts, starts,
+                                                                                            kBinG32);
       PCC_COUNT(1);
     }
   }
   if (families & kLaunchGroups) FamEnd(ctx, kFamGroup, ng);
   int nw = 0;
-  for (int b = kBinW128; b <= kBinW1000; ++b) nw += want(b) ? 1 : 0;
+  for (int b = kBinG4; b <= kBinW1000; ++b) nw += want(b) && (b > kBinG32 || routed(b)) ? 1 : 0;
   if (families & kLaunchWarps) FamBegin(ctx, kFamWarp);
-  // Grid-stride kernels: at most one wave of resident CTAs, so no partial
-  // last wave.
-  auto warp_bin = [&](auto k, size_t smem, int bin, unsigned cap) -> Status {
-    if (!want(bin)) return Status::Ok();
-    int per_sm = 0;
-    PCC_RETURN_IF_ERROR(SetSmem(k, smem, kWarpKernelWarps * 32, &per_sm));
-    if (per_sm > 0) cap = sms * unsigned(per_sm);
-    k<<<grid(bin, kWarpKernelWarps, cap), kWarpKernelWarps * 32, smem, st>>>(a, list, counts, starts, bin);
-    PCC_COUNT(1);
-    return Status::Ok();
-  };
   if constexpr (kCert) {
     if (a.narrow) {
-      PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<256, int>, CertWarpSmem<256, int>(), kBinW128, sms * 16));
-      PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<512, int>, CertWarpSmem<512, int>(), kBinW256, sms * 8));
-      PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<1024, int>, CertWarpSmem<1024, int>(), kBinW512, sms * 6));
-      PCC_RETURN_IF_ERROR(warp_bin(CertWarpKernel<2048, int>, CertWarpSmem<2048, int>(), kBinW1000, sms * 3));
+      PCC_RETURN_IF_ERROR(routed_bins(CertWarpKernel<256, int>, CertWarpSmem<256, int>(), sms * 16));
+      PCC_RETURN_IF_ERROR(cert_bin(CertWarpKernel<256, int>, CertWarpSmem<256, int>(), CertCtaKernel<256, int>,
+                   CertCtaSmem<256, int>(), kBinW128, sms * 16));
+      PCC_RETURN_IF_ERROR(cert_bin(CertWarpKernel<512, int>, CertWarpSmem<512, int>(), CertCtaKernel<512, int>,
+                   CertCtaSmem<512, int>(), kBinW256, sms * 8));
+      PCC_RETURN_IF_ERROR(cert_bin(CertWarpKernel<1024, int>, CertWarpSmem<1024, int>(), CertCtaKernel<1024, int>,
+                   CertCtaSmem<1024, int>(), kBinW512, sms * 6));
+      PCC_RETURN_IF_ERROR(cert_bin(CertWarpKernel<2048, int>, CertWarpSmem<2048, int>(), CertCtaKernel<2048, int>,
+                   CertCtaSmem<2048, int>(), kBinW1000, sms * 3));
     } else {
+      PCC_RETURN_IF_ERROR(routed_bins(CertWarpKernel<256, long long>, CertWarpSmem<256, long long>(), sms * 16));
       PCC_RETURN_IF_ERROR(
-          warp_bin(CertWarpKernel<256, long long>, CertWarpSmem<256, long long>(), kBinW128, sms * 16));
+          cert_bin(CertWarpKernel<256, long long>, CertWarpSmem<256, long long>(), CertCtaKernel<256, long long>,
+                   CertCtaSmem<256, long long>(), kBinW128, sms * 16));
       PCC_RETURN_IF_ERROR(
-          warp_bin(CertWarpKernel<512, long long>, CertWarpSmem<512, long long>(), kBinW256, sms * 8));
+          cert_bin(CertWarpKernel<512, long long>, CertWarpSmem<512, long long>(), CertCtaKernel<512, long long>,
+                   CertCtaSmem<512, long long>(), kBinW256, sms * 8));
       PCC_RETURN_IF_ERROR(
-          warp_bin(CertWarpKernel<1024, long long>, CertWarpSmem<1024, long long>(), kBinW512, sms * 4));
+          cert_bin(CertWarpKernel<1024, long long>, CertWarpSmem<1024, long long>(), CertCtaKernel<1024, long long>,
+                   CertCtaSmem<1024, long long>(), kBinW512, sms * 4));
       PCC_RETURN_IF_ERROR(
-          warp_bin(CertWarpKernel<2048, long long>, CertWarpSmem<2048, long long>(), kBinW1000, sms * 2));
+          cert_bin(CertWarpKernel<2048, long long>, CertWarpSmem<2048, long long>(), CertCtaKernel<2048, long long>,
+                   CertCtaSmem<2048, long long>(), kBinW1000, sms * 2));
     }
   } else {
+    PCC_RETURN_IF_ERROR(routed_bins(BestMoveWarpKernel<256, kInt, kAsync>, WarpKernelSmem<256>(), sms * 16));
     PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<256, kInt, kAsync>, WarpKernelSmem<256>(), kBinW128, sms * 16));
     PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<512, kInt, kAsync>, WarpKernelSmem<512>(), kBinW256, sms * 8));
     PCC_RETURN_IF_ERROR(warp_bin(BestMoveWarpKernel<1024, kInt, kAsync>, WarpKernelSmem<1024>(), kBinW512, sms * 4));
@@ -766,6 +1034,15 @@ Status PrepareBestMoveKernels() {
   PCC_RETURN_IF_ERROR(Prep(CertWarpKernel<512, long long>, CertWarpSmem<512, long long>(), kW));
   PCC_RETURN_IF_ERROR(Prep(CertWarpKernel<1024, long long>, CertWarpSmem<1024, long long>(), kW));
   PCC_RETURN_IF_ERROR(Prep(CertWarpKernel<2048, long long>, CertWarpSmem<2048, long long>(), kW));
+  constexpr int kC = kCtaWarps * 32;
+  PCC_RETURN_IF_ERROR(Prep(CertCtaKernel<256, int>, CertCtaSmem<256, int>(), kC));
+  PCC_RETURN_IF_ERROR(Prep(CertCtaKernel<512, int>, CertCtaSmem<512, int>(), kC));
+  PCC_RETURN_IF_ERROR(Prep(CertCtaKernel<1024, int>, CertCtaSmem<1024, int>(), kC));
+  PCC_RETURN_IF_ERROR(Prep(CertCtaKernel<2048, int>, CertCtaSmem<2048, int>(), kC));
+  PCC_RETURN_IF_ERROR(Prep(CertCtaKernel<256, long long>, CertCtaSmem<256, long long>(), kC));
+  PCC_RETURN_IF_ERROR(Prep(CertCtaKernel<512, long long>, CertCtaSmem<512, long long>(), kC));
+  PCC_RETURN_IF_ERROR(Prep(CertCtaKernel<1024, long long>, CertCtaSmem<1024, long long>(), kC));
+  PCC_RETURN_IF_ERROR(Prep(CertCtaKernel<2048, long long>, CertCtaSmem<2048, long long>(), kC));
   PCC_RETURN_IF_ERROR(Prep(BestMoveWarpKernel<256, false, false>, WarpKernelSmem<256>(), kW));
   PCC_RETURN_IF_ERROR(Prep(BestMoveWarpKernel<512, false, false>, WarpKernelSmem<512>(), kW));
   PCC_RETURN_IF_ERROR(Prep(BestMoveWarpKernel<1024, false, false>, WarpKernelSmem<1024>(), kW));

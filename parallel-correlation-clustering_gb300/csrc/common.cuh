@@ -117,6 +117,12 @@ struct Context {
   cudaEvent_t fork_ev = nullptr;
   cudaEvent_t join_ev[kSideStreams] = {nullptr, nullptr, nullptr};
   bool overlap_families = true;  // off: every family on `stream` in turn
+  // Best-move launch shape set by pcc_set_launch_tuning (tuned false: the
+  // compiled-in table by graph size).
+  bool tuned = false;
+  uint32_t group_max_degree = 32;
+  uint32_t cta_min_degree = 1000;
+  float grid_waves = 1.0f;
   Status EnsureSideStreams() {
     if (fork_ev) return Status::Ok();
     for (int i = 0; i < kSideStreams; ++i) {

@@ -278,6 +278,34 @@ Status PrepareBestMoveKernels();
 // families: kLaunchGroups (degree <= 32) and/or kLaunchWarps (33-1000).
 constexpr int kLaunchGroups = 1;
 constexpr int kLaunchWarps = 2;
+
+// Launch shape of the best-move bins: lane-group bins whose degree cap is
+// above group_max_degree run on the warp kernel instead (4, 8, 16 or 32);
+// certified warp bins whose degree cap is above cta_min_degree run one CTA
+// per vertex (64, 128, 256, 512, or 1000 for none); the grid-stride kernels
+// get grid_waves times one wave of resident CTAs.  Every choice changes the
+// schedule only: each vertex's decision is the same, so the labels are too.
+struct LaunchTuning {
+  uint32_t group_max_degree;
+  uint32_t cta_min_degree;
+  float grid_waves;
+};
+struct TuningRow {
+  uint32_t max_vertices;  // the row applies to level graphs with n <= this
+  uint32_t group_max_degree;
+  uint32_t cta_min_degree;
+  float grid_waves;
+};
+}  // namespace pcc
+#include "tuning_table.cuh"
+namespace pcc {
+inline LaunchTuning TuningFor(const Context* ctx, uint32_t n) {
+  if (ctx->tuned) return LaunchTuning{ctx->group_max_degree, ctx->cta_min_degree, ctx->grid_waves};
+  for (const TuningRow& r : kTuningTable)
+    if (n <= r.max_vertices) return LaunchTuning{r.group_max_degree, r.cta_min_degree, r.grid_waves};
+  return LaunchTuning{32, 1000, 1.0f};
+}
+
 Status LaunchBestMoves(Context* ctx, const BMArgs& a, const uint32_t* list, const uint32_t* bin_counts,
                        const uint32_t* bin_starts, const uint32_t* host_counts, bool int_mode,
                        uint32_t max_deg, int families = kLaunchGroups | kLaunchWarps);

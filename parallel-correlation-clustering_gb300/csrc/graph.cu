@@ -391,6 +391,25 @@ void pcc_set_detailed_timing(pcc_context* ctx, int32_t on) {
   if (ctx) ctx->c.detailed_timing = on != 0;
 }
 
+pcc_status pcc_set_launch_tuning(pcc_context* ctx, uint32_t group_max_degree, uint32_t cta_min_degree,
+                                 float grid_waves) {
+  if (!ctx) return PCC_INVALID_ARGUMENT;
+  if (group_max_degree == 0 && cta_min_degree == 0 && grid_waves == 0.0f) {
+    ctx->c.tuned = false;
+    return PCC_OK;
+  }
+  const bool g_ok = group_max_degree == 4 || group_max_degree == 8 || group_max_degree == 16 ||
+                    group_max_degree == 32;
+  const bool c_ok = cta_min_degree == 64 || cta_min_degree == 128 || cta_min_degree == 256 ||
+                    cta_min_degree == 512 || cta_min_degree == 1000;
+  if (!g_ok || !c_ok || !(grid_waves >= 0.125f && grid_waves <= 16.0f)) return PCC_INVALID_ARGUMENT;
+  ctx->c.tuned = true;
+  ctx->c.group_max_degree = group_max_degree;
+  ctx->c.cta_min_degree = cta_min_degree;
+  ctx->c.grid_waves = grid_waves;
+  return PCC_OK;
+}
+
 uint64_t pcc_device_peak_bytes(pcc_context* ctx, int32_t reset) {
   if (!ctx) return 0;
   const uint64_t p = ctx->c.peak.load();

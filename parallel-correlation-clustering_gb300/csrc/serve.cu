@@ -317,7 +317,30 @@ pcc_status pcc_cluster_batch(int device, uint32_t num_graphs, const pcc_batch_gr
     // per entry counted) fit next to the fixed 64 MB.
     const uint64_t fixed = 64ull << 20;
     const uint64_t cap = hbm_budget == 0 ? 0 : std::max<uint64_t>(1, (hbm_budget > fixed ? hbm_budget - fixed : 0) / 252);
-    s = pcc_cluster_union(c, num_graphs, graphs, configs, num_configs, objectives, cap, out_labels, stats, nullptr);
+    // Graphs packed in ascending entry count (stable): unions of similar
+    // graphs end their levels and rounds closer together, so fewer launches
+    // run for a few stragglers.  Every graph's result is independent of its
+    // union, so the order changes no label.
+    std::vector<uint32_t> order(num_graphs);
+    for (uint32_t i = 0; i < num_graphs; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t a, uint32_t b) { return graphs[a].m < graphs[b].m; });
+    std::vector<pcc_batch_graph> sg(num_graphs);
+    std::vector<pcc_config> sc(num_configs);
+    std::vector<int32_t> so(objectives ? num_graphs : 0);
+    std::vector<uint32_t*> sl(num_graphs);
+    std::vector<pcc_stats> ss(stats ? num_graphs : 0);
+    for (uint32_t i = 0; i < num_graphs; ++i) {
+      sg[i] = graphs[order[i]];
+      sl[i] = out_labels[order[i]];
+      if (objectives) so[i] = objectives[order[i]];
+      if (num_configs != 1) sc[i] = configs[order[i]];
+    }
+    if (num_configs == 1) sc[0] = configs[0];
+    s = pcc_cluster_union(c, num_graphs, sg.data(), sc.data(), num_configs, objectives ? so.data() : nullptr, cap,
+                          sl.data(), stats ? ss.data() : nullptr, nullptr);
+    if (stats)
+      for (uint32_t i = 0; i < num_graphs; ++i) stats[order[i]] = ss[i];
     pcc_destroy(c);
     if (wall_ms) *wall_ms = pcc::MsBetween(t0, Clock::now());
     return s;

@@ -216,8 +216,12 @@ __global__ void ScSlowKernel(SlowArgs a) {
         for (uint32_t x = 0; x < size; ++x)
           if (tmp[x] == t) a.mark[mem[x]] = 2;
         double weight = 0;
-        for (uint64_t j = a.off[cv]; j < a.off[cv + 1]; ++j)
-          if (a.mark[a.nbr[j]] == 2) weight += 1.0;
+        // Marks are shared by all clusters' threads: a neighbour counts only
+        // if it is in this cluster, whose marks this thread alone writes.
+        for (uint64_t j = a.off[cv]; j < a.off[cv + 1]; ++j) {
+          const uint32_t u = a.nbr[j];
+          if (a.C[u] == c && a.mark[u] == 2) weight += 1.0;
+        }
         for (uint32_t x = 0; x < size; ++x)
           if (tmp[x] == t) a.mark[mem[x]] = 0;
         const double offset = a.offset * double(gsize) + a.res * double(gsize);

@@ -227,6 +227,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.pcc_cluster_batch.restype = ctypes.c_int
     lib.pcc_set_detailed_timing.argtypes = [vp, ctypes.c_int32]
     lib.pcc_set_detailed_timing.restype = None
+    lib.pcc_set_launch_tuning.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float]
+    lib.pcc_set_launch_tuning.restype = ctypes.c_int32
     lib.pcc_cluster_union.argtypes = [vp, ctypes.c_uint32, vp, vp, ctypes.c_uint32, vp, ctypes.c_uint64, vp, vp,
                                       vp]
     lib.pcc_cluster_union.restype = ctypes.c_int
@@ -348,6 +350,14 @@ class Context:
         (off, the default)."""
         self.lib.pcc_set_detailed_timing(self._h, 1 if on else 0)
         self.detailed_timing = bool(on)
+
+    def set_launch_tuning(self, group_max_degree: int = 0, cta_min_degree: int = 0, grid_waves: float = 0.0):
+        """pcc_set_launch_tuning: lane-group bins above group_max_degree on
+        the warp kernel, certified warp bins above cta_min_degree on one CTA
+        per vertex, grid_waves waves of resident CTAs per best-move launch;
+        (0, 0, 0) returns to the compiled-in table."""
+        self.check(self.lib.pcc_set_launch_tuning(self._h, int(group_max_degree), int(cta_min_degree),
+                                                  float(grid_waves)))
 
     def bytes_in_use(self) -> int:
         return int(self.lib.pcc_device_bytes_in_use(self._h))

@@ -509,6 +509,68 @@ def test_overlapped_families_match_serial(graphs, monkeypatch):
         c_ser.close()
 
 
+def test_launch_tuning_keeps_results(ctx, graphs):
+    """Every launch shape pcc_set_launch_tuning accepts (lane-group bins
+    routed to the warp kernel, certified warp bins on one CTA per vertex,
+    0.125-4 waves of CTAs) gives the labels and counters of the compiled-in
+    table: INT (certified) and FP64 kernels, synchronous rounds in the device
+    loop and host-driven.  Shapes outside the documented range are
+    INVALID_ARGUMENT."""
+    cases = [("rmat16", "mod", 1.0, P.NBHR_MOVE), ("sbm3k_int", "corr", 0.05, P.NBHR_CLUSTER_MOVE),
+             ("lfr20k_real", "corr", 0.1, P.NBHR_CLUSTER_MOVE), ("sbm2k", "corr", 0.05, P.ALL_MOVE),
+             ("hubs100k", "corr", 0.05, P.NBHR_MOVE)]
+    shapes = [(4, 1000, 1.0), (8, 512, 0.5), (16, 256, 2.0), (32, 128, 0.125), (32, 64, 4.0)]
+    keys = ("objective", "modularity", "num_clusters", "levels", "rounds", "edge_visits", "moves")
+    try:
+        for name, kind, res, move in cases:
+            cfg = P.make_config(resolution=res, refine=True, move_method=move, random_seed=3)
+            run = P.modularity_cluster if kind == "mod" else P.correlation_cluster
+            dg = ctx.upload(graphs[name])
+            ctx.set_launch_tuning(0, 0, 0.0)
+            l0, s0 = run(dg, cfg)
+            for gmax, cta, waves in shapes:
+                for detailed in (False, True):
+                    ctx.set_launch_tuning(gmax, cta, waves)
+                    ctx.set_detailed_timing(detailed)
+                    l1, s1 = run(dg, cfg)
+                    np.testing.assert_array_equal(l0, l1, err_msg=f"{name} {gmax}/{cta}/{waves}")
+                    for key in keys:
+                        assert s0[key] == s1[key], (name, gmax, cta, waves, key, s0[key], s1[key])
+            dg.free()
+        for bad in [(3, 1000, 1.0), (64, 1000, 1.0), (32, 1000, 0.0), (32, 1000, 100.0), (0, 1000, 1.0),
+                    (32, 100, 1.0), (32, 0, 1.0)]:
+            with pytest.raises(P.PccError) as e:
+                ctx.set_launch_tuning(*bad)
+            assert e.value.code == 3
+    finally:
+        ctx.set_launch_tuning(0, 0, 0.0)
+        ctx.set_detailed_timing(False)
+
+
+@pytest.mark.parametrize("name", ["sbm2k", "rmat14", "rmat16", "sbm3k_int", "hubs100k"])
+@pytest.mark.parametrize("nclusters_div", [1, 7, 300])
+def test_best_moves_replay_cta_kernels(ctx, graphs, name, nclusters_div):
+    """The one-CTA-per-vertex certified kernels (every warp bin routed to
+    them) against the oracle on one sync pass from a random state: targets,
+    values and moves bit-exact.  The replay path also checks each certified
+    decision against the exact FP64 one on the device (a mismatch is an
+    INTERNAL error)."""
+    g = graphs[name]
+    dg, og = _both(ctx, g)
+    C, s, k, K = rand_state(g.n, g.n // nclusters_div, seed=nclusters_div)
+    try:
+        ctx.set_launch_tuning(32, 64, 1.0)
+        for res, off in ((0.01, 0.0), (0.3, 0.0), (0.05, 1.0)):
+            cfg = P.make_config(resolution=res, edge_weight_offset=off)
+            t_g, v_g, m_g = P.best_moves(dg, cfg, C, s, k, K)
+            t_o, v_o, m_o = O.best_moves(og, cfg, C, s, k, K)
+            np.testing.assert_array_equal(t_g, t_o)
+            np.testing.assert_array_equal(v_g.view(np.uint64), v_o.view(np.uint64))
+            np.testing.assert_array_equal(m_g, m_o)
+    finally:
+        ctx.set_launch_tuning(0, 0, 0.0)
+
+
 @pytest.mark.parametrize("name,res,move", [
     ("sbm2k", 0.01, P.NBHR_CLUSTER_MOVE),
     ("lfr20k_real", 0.1, P.NBHR_CLUSTER_MOVE),
