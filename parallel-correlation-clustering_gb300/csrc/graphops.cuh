@@ -153,6 +153,123 @@ inline void LaunchEdgeIter(Context* ctx, const uint32_t* list, const uint32_t* c
 }
 
 // ---------------------------------------------------------------------------
+// Frontier push (gbbs edgeMap with an always-true update): stamp[u] = value
+// for every neighbour u of a row passing `row`.  The mid and big shapes load
+// kPushBatch neighbour ids per thread before storing any stamp: through the
+// generic functor the compiler must assume a store may alias the next id and
+// keeps one load in flight.  Small rows use EdgeIterSmallKernel.  A stamp
+// already equal to the value is not stored again: hub vertices are
+// neighbours of a large share of all rows, and same-address stores
+// serialise at their L2 slice while the loads are served by L1.
+// ---------------------------------------------------------------------------
+constexpr int kPushBatch = 8;
+
+struct StampValue {
+  uint32_t stamp;
+  const RoundState* rs;  // non-null: the value comes from here
+};
+
+template <class R>
+__global__ void __launch_bounds__(kIterThreads) PushMidKernel(const uint32_t* __restrict__ list,
+                                                             const uint32_t* __restrict__ starts,
+                                                             const uint64_t* __restrict__ off,
+                                                             const uint32_t* __restrict__ nbr,
+                                                             uint32_t* __restrict__ stamp, StampValue sv, R row) {
+  const uint32_t s0 = starts[kBinW128];
+  const uint32_t count = starts[kBinCta] - s0;  // bins W128..W1000
+  const unsigned lane = LaneId(), warp = threadIdx.x >> 5;
+  const uint32_t value = StampIn(sv.rs, sv.stamp);
+  for (uint64_t i = uint64_t(blockIdx.x) * (kIterThreads / 32) + warp; i < count;
+       i += uint64_t(gridDim.x) * (kIterThreads / 32)) {
+    const uint32_t v = list[s0 + i];
+    if (!row(v)) continue;
+    const uint64_t b = off[v], e = off[v + 1];
+    for (uint64_t j0 = b; j0 < e; j0 += 32 * kPushBatch) {
+      uint32_t u[kPushBatch];
+#pragma unroll
+      for (int k = 0; k < kPushBatch; ++k) {
+        const uint64_t j = j0 + 32 * k + lane;
+        u[k] = j < e ? nbr[j] : kNone;
+      }
+      uint32_t cur[kPushBatch];
+#pragma unroll
+      for (int k = 0; k < kPushBatch; ++k) cur[k] = u[k] != kNone ? stamp[u[k]] : value;
+#pragma unroll
+      for (int k = 0; k < kPushBatch; ++k)
+        if (cur[k] != value) stamp[u[k]] = value;
+    }
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(kIterBigThreads) PushBigKernel(const uint32_t* __restrict__ list,
+                                                                const uint32_t* __restrict__ starts,
+                                                                const uint64_t* __restrict__ off,
+                                                                const uint32_t* __restrict__ nbr,
+                                                                uint32_t* __restrict__ stamp, StampValue sv, R row) {
+  const uint32_t s0 = starts[kBinCta];
+  const uint32_t count = starts[kNumBins] - s0;  // bins Cta, Global
+  const uint32_t value = StampIn(sv.rs, sv.stamp);
+  for (uint64_t i = blockIdx.x; i < count; i += gridDim.x) {
+    const uint32_t v = list[s0 + i];
+    if (!row(v)) continue;
+    const uint64_t b = off[v], e = off[v + 1];
+    for (uint64_t j0 = b; j0 < e; j0 += uint64_t(kIterBigThreads) * kPushBatch) {
+      uint32_t u[kPushBatch];
+#pragma unroll
+      for (int k = 0; k < kPushBatch; ++k) {
+        const uint64_t j = j0 + uint64_t(kIterBigThreads) * k + threadIdx.x;
+        u[k] = j < e ? nbr[j] : kNone;
+      }
+      uint32_t cur[kPushBatch];
+#pragma unroll
+      for (int k = 0; k < kPushBatch; ++k) cur[k] = u[k] != kNone ? stamp[u[k]] : value;
+#pragma unroll
+      for (int k = 0; k < kPushBatch; ++k)
+        if (cur[k] != value) stamp[u[k]] = value;
+    }
+  }
+}
+
+struct PushStampFn {
+  const uint32_t* nbr;
+  uint32_t* stamp;
+  StampValue sv;
+  __device__ void operator()(uint32_t, uint64_t j, uint64_t) const {
+    const uint32_t u = nbr[j], value = StampIn(sv.rs, sv.stamp);
+    if (stamp[u] != value) stamp[u] = value;
+  }
+};
+
+// The push over a BinSet-layout list (starts on device; host_counts may be
+// null: every shape launched).
+template <class R>
+inline void LaunchPush(Context* ctx, const uint32_t* list, const uint32_t* counts, const uint32_t* starts,
+                       const uint32_t* host_counts, const uint64_t* off, const uint32_t* nbr, uint32_t* stamp,
+                       StampValue sv, R row) {
+  auto any = [&](int b0, int b1) {
+    if (!host_counts) return true;
+    for (int b = b0; b < b1; ++b)
+      if (host_counts[b]) return true;
+    return false;
+  };
+  cudaStream_t st = ctx->stream;
+  if (any(kBinG4, kBinW128)) {
+    EdgeIterSmallKernel<PushStampFn, R><<<IterSmallGrid(ctx), kIterThreads, 0, st>>>(
+        list, counts, starts, off, PushStampFn{nbr, stamp, sv}, row);
+    PCC_COUNT(1);
+  }
+  if (any(kBinW128, kBinCta)) {
+    PushMidKernel<R><<<IterMidGrid(ctx), kIterThreads, 0, st>>>(list, starts, off, nbr, stamp, sv, row);
+    PCC_COUNT(1);
+  }
+  if (any(kBinCta, kNumBins)) {
+    PushBigKernel<R><<<IterBigGrid(ctx), kIterBigThreads, 0, st>>>(list, starts, off, nbr, stamp, sv, row);
+    PCC_COUNT(1);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Degree binning of a vertex predicate over [0, n): count, starts, scatter.
 // The order inside a bin is not specified (warp-aggregated atomics).
 // ---------------------------------------------------------------------------

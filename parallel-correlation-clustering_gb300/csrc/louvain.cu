@@ -423,14 +423,6 @@ __global__ void __launch_bounds__(kT) ObjectiveUnionKernel(uint32_t n, const uin
 
 // Marked vertices for the next frontier.
 
-struct PushNeighbors {  // gbbs::edgeMap with an always-true functor
-  const uint32_t* nbr;
-  uint32_t* next_stamp;
-  uint32_t stamp;
-  const RoundState* rs = nullptr;
-  __device__ void operator()(uint32_t, uint64_t j, uint64_t) const { next_stamp[nbr[j]] = StampIn(rs, stamp); }
-};
-
 // Marked vertices of the next frontier.
 struct PredModifiedCluster {  // NBHR_CLUSTER_MOVE: vertices of modified clusters
   const uint32_t* C;
@@ -843,13 +835,13 @@ class Engine {
     // Neighbourhood of the marked set (edgeMap), rows taken from the static
     // degree bins with a marked-row predicate, then the next frontier's size.
     timer_.Begin(kPhaseFrontier);
-    const PushNeighbors push{g.nbr.p, next_stamp_.p, stamp_, rs};
+    const StampValue sv{stamp_, rs};
     if (cfg_.move_method == PCC_NBHR_CLUSTER_MOVE) {
-      LaunchEdgeIter(ctx_, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins, g.bins.host_counts,
-                     g.off.p, push, PredModifiedCluster{L->C.p, mod_stamp_.p, stamp_, rs});  // rows with d > 0
+      LaunchPush(ctx_, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins, g.bins.host_counts, g.off.p,
+                 g.nbr.p, next_stamp_.p, sv, PredModifiedCluster{L->C.p, mod_stamp_.p, stamp_, rs});  // rows with d > 0
     } else {
-      LaunchEdgeIter(ctx_, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins, g.bins.host_counts,
-                     g.off.p, push, PredStamp{moved_stamp_.p, stamp_, rs});
+      LaunchPush(ctx_, g.bins.list.p, g.bins.counts.p, g.bins.counts.p + kNumBins, g.bins.host_counts, g.off.p,
+                 g.nbr.p, next_stamp_.p, sv, PredStamp{moved_stamp_.p, stamp_, rs});
     }
     if (n) {
       CountDegreesKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g.off.p, PredStamp{next_stamp_.p, stamp_, rs},
