@@ -39,6 +39,8 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
                                                           const uint32_t* __restrict__ bin_counts,
                                                           const uint32_t* __restrict__ bin_starts, int bin) {
   __shared__ double stage[8][32];
+  __shared__ uint32_t mover_buf[8][64];
+  WarpMoverBuffer mb{mover_buf[threadIdx.x >> 5]};
   const uint32_t count = bin_counts[bin];
   const uint32_t start = bin_starts[bin];
   const unsigned lane = LaneId(), warp = threadIdx.x >> 5;
@@ -111,11 +113,9 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
     }
     bool append = false;
     if (vvalid && gl == 0) append = Decide<kAsync>(a, x, val, id, change);
-    if (!kAsync) {
-      const uint32_t slot = WarpAppendFull(&a.ctr->movers, append);
-      if (append) a.movers[slot] = x.v;
-    }
+    if (!kAsync) mb.Add(&a.ctr->movers, a.movers, append, x.v);
   }
+  if (!kAsync) mb.Flush(&a.ctr->movers, a.movers);
   FlushFamily(a, kFamGroup, fam_e, fam_v);
 }
 
@@ -140,6 +140,8 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
                                                                            const uint32_t* __restrict__ bin_counts,
                                                                            const uint32_t* __restrict__ bin_starts,
                                                                            int bin) {
+  __shared__ uint32_t mover_buf[kWarpKernelWarps][64];
+  WarpMoverBuffer mb{mover_buf[threadIdx.x >> 5]};
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t count = bin_counts[bin];
   const uint32_t start = bin_starts[bin];
@@ -250,14 +252,12 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
     }
     bool append = false;
     if (lane == 0) append = Decide<kAsync>(a, x, best, bid, change);
-    if (!kAsync) {
-      const uint32_t pos = WarpAppendFull(&a.ctr->movers, append);
-      if (append) a.movers[pos] = x.v;
-    }
+    if (!kAsync) mb.Add(&a.ctr->movers, a.movers, append, x.v);
     __syncwarp();
     if (lane == 0) *used_count = 0;
     __syncwarp();
   }
+  if (!kAsync) mb.Flush(&a.ctr->movers, a.movers);
   FlushFamily(a, kFamWarp, fam_e, fam_v);
 }
 
@@ -346,6 +346,8 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
                                                       const uint32_t* __restrict__ bin_counts,
                                                       const uint32_t* __restrict__ bin_starts, int bin) {
   __shared__ int stage[8][32];
+  __shared__ uint32_t mover_buf[8][64];
+  WarpMoverBuffer mb{mover_buf[threadIdx.x >> 5]};
   const uint32_t count = bin_counts[bin];
   const uint32_t start = bin_starts[bin];
   const unsigned lane = LaneId(), warp = threadIdx.x >> 5;
@@ -449,9 +451,9 @@ __global__ void __launch_bounds__(256) CertGroupKernel(BMArgs a, const uint32_t*
       const bool app = GroupExact<G>(a, x, fp64, contender, gl, T, S, KD, cu, replay, cres, cmove);
       append = append || app;
     }
-    const uint32_t slot = WarpAppendFull(&a.ctr->movers, append);
-    if (append) a.movers[slot] = x.v;
+    mb.Add(&a.ctr->movers, a.movers, append, x.v);
   }
+  mb.Flush(&a.ctr->movers, a.movers);
   FlushFamily(a, kFamGroup, fam_e, fam_v);
 }
 
@@ -467,23 +469,27 @@ constexpr size_t CertWarpSmem() {
 }
 
 // V: int when every cluster sum fits in 32 bits (narrow), else long long.
+// Every entry inserts its cluster itself (atomicCAS claims a slot) and adds
+// its integer weight with a shared-memory atomic: INT-mode sums are exact in
+// any order, and grouping equal clusters first with match.any cost more than
+// the atomics it saves.
 template <int HC, typename V>
 __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a, const uint32_t* __restrict__ list,
                                                                        const uint32_t* __restrict__ bin_counts,
                                                                        const uint32_t* __restrict__ bin_starts,
                                                                        int bin) {
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t mover_buf[kWarpKernelWarps][64];
+  WarpMoverBuffer mb{mover_buf[threadIdx.x >> 5]};
   const uint32_t count = bin_counts[bin];
   const uint32_t start = bin_starts[bin];
   const unsigned lane = LaneId(), warp = threadIdx.x >> 5;
   unsigned char* base = smem + size_t(warp) * CertWarpStride<HC, V>();
   V* vals = reinterpret_cast<V*>(base);
   uint32_t* keys = reinterpret_cast<uint32_t*>(base + size_t(HC) * sizeof(V));
-  int* stage = reinterpret_cast<int*>(base + size_t(HC) * (sizeof(V) + 4));
   uint16_t* used = reinterpret_cast<uint16_t*>(base + size_t(HC) * (sizeof(V) + 4) + 32 * 4);
   unsigned long long fam_e = 0, fam_v = 0;
   const bool replay = a.out_target != nullptr;
-  const bool unit = a.w == nullptr;
   for (int i = lane; i < HC; i += 32) {
     keys[i] = kNone;
     vals[i] = 0;
@@ -531,11 +537,9 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
       const float wt = ww[k];
       const bool cand = uu[k] != x.v;
       const uint32_t cu = cc[k];
-      const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane));
-      const bool leader = cand && int(lane) == __ffs(peers) - 1;
       uint32_t slot = kNone;
       bool ins = false;
-      if (leader) {
+      if (cand) {
         slot = FindOrInsertT<false>(keys, HC, cu, &ins);
         if (slot == kNone) atomicExch(&a.ctr->error, kErrHashFull);
       }
@@ -545,8 +549,10 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
         nused += __popc(im);
       }
       const int xi = cand ? (WeightToInt(wt) - a.ioffset) : 0;
-      const int Sg = GroupSumInt(peers, xi, unit, leader, stage);
-      if (slot != kNone) vals[slot] += static_cast<V>(Sg);
+      if (slot != kNone) {
+        if constexpr (sizeof(V) == 4) atomicAdd(reinterpret_cast<int*>(&vals[slot]), xi);
+        else atomicAdd(reinterpret_cast<unsigned long long*>(&vals[slot]), static_cast<unsigned long long>(static_cast<long long>(xi)));
+      }
       __syncwarp();
       }
     }
@@ -621,10 +627,10 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
         vals[slot] = 0;
       }
     }
-    const uint32_t pos = WarpAppendFull(&a.ctr->movers, append);
-    if (append) a.movers[pos] = x.v;
+    mb.Add(&a.ctr->movers, a.movers, append, x.v);
     __syncwarp();
   }
+  mb.Flush(&a.ctr->movers, a.movers);
   FlushFamily(a, kFamWarp, fam_e, fam_v);
 }
 
@@ -667,19 +673,19 @@ __global__ void __launch_bounds__(kCtaWarps * 32) CertCtaKernel(BMArgs a, const 
   V* vals = reinterpret_cast<V*>(smem);
   uint32_t* keys = reinterpret_cast<uint32_t*>(smem + size_t(HC) * sizeof(V));
   uint16_t* used = reinterpret_cast<uint16_t*>(smem + size_t(HC) * (sizeof(V) + 4));
-  __shared__ int stage[kCtaWarps][32];
   __shared__ uint32_t s_nused;
   __shared__ V s_max[kCtaWarps];
   __shared__ float s_u[kCtaWarps];
   __shared__ V s_ls[kCtaWarps], s_ts[kCtaWarps];
   __shared__ unsigned long long s_lk[kCtaWarps], s_tk[kCtaWarps];
   __shared__ uint32_t s_li[kCtaWarps], s_ti[kCtaWarps];
+  __shared__ uint32_t mover_buf[64];  // warp 0's
+  WarpMoverBuffer mb{mover_buf};
   const uint32_t count = bin_counts[bin];
   const uint32_t start = bin_starts[bin];
   const unsigned tid = threadIdx.x, lane = LaneId(), warp = tid >> 5;
   unsigned long long fam_e = 0, fam_v = 0;
   const bool replay = a.out_target != nullptr;
-  const bool unit = a.w == nullptr;
   for (int i = tid; i < HC; i += BT) {
     keys[i] = kNone;
     vals[i] = 0;
@@ -720,11 +726,9 @@ __global__ void __launch_bounds__(kCtaWarps * 32) CertCtaKernel(BMArgs a, const 
         if (e0 + BT * k + 32 * warp >= x.d) break;  // uniform over the warp
         const bool cand = uu[k] != x.v;
         const uint32_t cu = cc[k];
-        const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane));
-        const bool leader = cand && int(lane) == __ffs(peers) - 1;
         uint32_t slot = kNone;
         bool ins = false;
-        if (leader) {
+        if (cand) {
           slot = FindOrInsertT<false>(keys, HC, cu, &ins);
           if (slot == kNone) atomicExch(&a.ctr->error, kErrHashFull);
         }
@@ -737,13 +741,12 @@ __global__ void __launch_bounds__(kCtaWarps * 32) CertCtaKernel(BMArgs a, const 
           if (ins) used[base + __popc(im & LaneMaskLt())] = static_cast<uint16_t>(slot);
         }
         const int xi = cand ? (WeightToInt(ww[k]) - a.ioffset) : 0;
-        const int Sg = GroupSumInt(peers, xi, unit, leader, stage[warp]);
         if (slot != kNone) {
           if constexpr (sizeof(V) == 4)
-            atomicAdd(reinterpret_cast<int*>(&vals[slot]), Sg);
+            atomicAdd(reinterpret_cast<int*>(&vals[slot]), xi);
           else
             atomicAdd(reinterpret_cast<unsigned long long*>(&vals[slot]),
-                      static_cast<unsigned long long>(static_cast<long long>(Sg)));
+                      static_cast<unsigned long long>(static_cast<long long>(xi)));
         }
       }
     }
@@ -832,7 +835,7 @@ __global__ void __launch_bounds__(kCtaWarps * 32) CertCtaKernel(BMArgs a, const 
       } else if (lane == 0) {
         append = ApplyCertified(a, x, cmove);
       }
-      if (lane == 0 && append) a.movers[atomicAdd(&a.ctr->movers, 1u)] = x.v;
+      mb.Add(&a.ctr->movers, a.movers, append, x.v);
     }
     __syncthreads();  // the table is read by WarpExact up to here
     for (uint32_t i = tid; i < nused; i += BT) {
@@ -845,7 +848,10 @@ __global__ void __launch_bounds__(kCtaWarps * 32) CertCtaKernel(BMArgs a, const 
     if (tid == 0) s_nused = 0;
     __syncthreads();
   }
-  if (warp == 0) FlushFamily(a, kFamWarp, fam_e, fam_v);
+  if (warp == 0) {
+    mb.Flush(&a.ctr->movers, a.movers);
+    FlushFamily(a, kFamWarp, fam_e, fam_v);
+  }
 }
 
 // Sets the kernel's dynamic shared-memory limit and queries its resident

@@ -512,11 +512,18 @@ __device__ __forceinline__ void ScanRow(const BMArgs& a, const VertexCtx& x, uin
         const uint32_t hp = Mix32(cu);
         mine = mine && __umulhi(hp, P) == p && ((hp >> 8) & (Q - 1)) == q;
       }
-      const unsigned peers = __match_any_sync(kFull, mine ? cu : LaneSentinel(lane));
-      const bool leader = mine && int(lane) == __ffs(peers) - 1;
-      int Si = 0;
+      // INT mode: every entry adds its own integer weight (exact in any
+      // order); FP64 mode: equal clusters of the warp are summed in lane
+      // order first, one atomic per cluster.
+      unsigned peers = 0;
+      bool leader = mine;
+      int Si = xi;
       double Sd = 0.0;
-      GroupWeights<BT, kInt>(a, peers, leader, xi, xd, sh, &Si, &Sd);
+      if (!kInt) {
+        peers = __match_any_sync(kFull, mine ? cu : LaneSentinel(lane));
+        leader = mine && int(lane) == __ffs(peers) - 1;
+        GroupWeights<BT, kInt>(a, peers, leader, xi, xd, sh, &Si, &Sd);
+      }
       if (leader && *reinterpret_cast<volatile uint32_t*>(&sh.overflow) == 0) {
         bool ins;
         const uint32_t slot = HubInsert(skeys, cap, SlotHash(cu), cu, &ins);
@@ -767,11 +774,15 @@ __global__ void __launch_bounds__(kGlobThreads) HubGlobalAccumKernel(HubArgs h) 
           else
             t_dbl = Dadd(t_dbl, xd);
         }
-        const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane));
-        const bool leader = cand && int(lane) == __ffs(peers) - 1;
-        int Si = 0;
+        unsigned peers = 0;
+        bool leader = cand;
+        int Si = xi;
         double Sd = 0.0;
-        GroupWeights<BT, kInt>(a, peers, leader, xi, xd, sh, &Si, &Sd);
+        if (!kInt) {
+          peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane));
+          leader = cand && int(lane) == __ffs(peers) - 1;
+          GroupWeights<BT, kInt>(a, peers, leader, xi, xd, sh, &Si, &Sd);
+        }
         if (leader) {
           bool ins;
           const uint32_t slot = HubInsert(keys, cap, SlotHash(cu), cu, &ins);

@@ -27,6 +27,44 @@ __device__ __forceinline__ uint32_t WarpAppendFull(uint32_t* counter, bool pred)
   return base + __popc(mask & LaneMaskLt());
 }
 
+// Movers appended through a per-warp buffer of 64 ids in shared memory: one
+// atomic per 32 movers instead of one per evaluation step.  The movers
+// counter is shared by every CTA of a round, and an atomic whose result is
+// needed is a round trip the warp waits for.  Every lane calls Add and
+// Flush; the order of the movers list carries no meaning.
+struct WarpMoverBuffer {
+  uint32_t* buf;       // 64 entries, owned by the calling warp
+  uint32_t count = 0;  // warp-uniform
+  __device__ void Add(uint32_t* counter, uint32_t* movers, bool pred, uint32_t v) {
+    const unsigned m = __ballot_sync(kFull, pred);
+    if (!m) return;
+    const unsigned lane = LaneId();
+    if (pred) buf[count + __popc(m & LaneMaskLt())] = v;
+    count += __popc(m);
+    if (count < 32) return;
+    __syncwarp();
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(counter, 32u);
+    base = __shfl_sync(kFull, base, 0);
+    movers[base + lane] = buf[lane];
+    __syncwarp();
+    if (lane < count - 32) buf[lane] = buf[32 + lane];
+    count -= 32;
+    __syncwarp();
+  }
+  __device__ void Flush(uint32_t* counter, uint32_t* movers) {
+    __syncwarp();
+    if (count == 0) return;
+    const unsigned lane = LaneId();
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(counter, count);
+    base = __shfl_sync(kFull, base, 0);
+    if (lane < count) movers[base + lane] = buf[lane];
+    count = 0;
+    __syncwarp();
+  }
+};
+
 template <bool kAsync>
 __device__ __forceinline__ uint32_t LdC(const uint32_t* p) {
   return kAsync ? __ldcg(p) : __ldg(p);
