@@ -127,6 +127,7 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
 // ---------------------------------------------------------------------------
 constexpr int kWarpKernelWarps = 4;
 constexpr int kCertUnroll = 4;  // chunks of 32 entries loaded together
+constexpr int kCertRegRounds = 1;  // candidates per lane held in registers
 
 template <int HC>
 constexpr size_t WarpKernelSmem() {
@@ -516,6 +517,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
       fam_v += 1;
     }
     uint32_t nused = 0;  // used[] entries (warp-uniform)
+    int tpart = 0;       // this lane's part of T (entries in the vertex's own cluster)
     for (uint32_t e0 = 0; e0 < x.d; e0 += 32 * kCertUnroll) {
       uint32_t uu[kCertUnroll], cc[kCertUnroll];
       float ww[kCertUnroll];
@@ -549,6 +551,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
         nused += __popc(im);
       }
       const int xi = cand ? (WeightToInt(wt) - a.ioffset) : 0;
+      if (cand && cu == x.c) tpart += xi;
       if (slot != kNone) {
         if constexpr (sizeof(V) == 4) atomicAdd(reinterpret_cast<int*>(&vals[slot]), xi);
         else atomicAdd(reinterpret_cast<unsigned long long*>(&vals[slot]), static_cast<unsigned long long>(static_cast<long long>(xi)));
@@ -556,17 +559,41 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
       __syncwarp();
       }
     }
-    V T = 0;
-    if (lane == 0) {
-      const uint32_t slot = FindT<false>(keys, HC, x.c);
-      if (slot != kNone) T = vals[slot];
+    // T: the lanes' own-cluster parts (a lane's part is at most
+    // ceil(1000 / 32) weights of |w - offset| <= 2^22, so it fits an int).
+    V T;
+    if constexpr (sizeof(V) == 4) {
+      T = __reduce_add_sync(kFull, tpart);
+    } else {
+      T = tpart;
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) T += __shfl_xor_sync(kFull, T, o);
     }
-    T = __shfl_sync(kFull, T, 0);
+    const float r32 = Res32Of(a, x.v);
     const float k32 = a.kf[x.v];
-    const ChangeApproxT<V> ca = ApproxChange<V>(Res32Of(a, x.v), a.int_nw != 0, k32, a.Kf[x.c], T);
+    const ChangeApproxT<V> ca = ApproxChange<V>(r32, a.int_nw != 0, k32, a.Kf[x.c], T);
     const float cabs = ChangeAbsBound(ca);
+    // The first kCertRegRounds candidates of each lane (i = lane + 32 r) keep
+    // their slot, sum, Kf and filter value in registers across the passes;
+    // any further ones are read again.
+    uint32_t rslot[kCertRegRounds];
+    V rS[kCertRegRounds];
+    float rKf[kCertRegRounds];
     V vmax = sizeof(V) == 4 ? V(INT_MIN) : V(LLONG_MIN);
-    for (uint32_t i = lane; i < nused; i += 32) vmax = max(vmax, vals[used[i]]);
+#pragma unroll
+    for (int r = 0; r < kCertRegRounds; ++r) {
+      const uint32_t i = lane + 32 * r;
+      rslot[r] = 0xFFFFu;
+      rS[r] = 0;
+      rKf[r] = 0.f;
+      if (i < nused) {
+        rslot[r] = used[i];
+        rS[r] = vals[rslot[r]];
+        rKf[r] = a.Kf[keys[rslot[r]]];
+        vmax = max(vmax, rS[r]);
+      }
+    }
+    for (uint32_t i = lane + 32 * kCertRegRounds; i < nused; i += 32) vmax = max(vmax, vals[used[i]]);
     if constexpr (sizeof(V) == 4) {
       vmax = __reduce_max_sync(kFull, vmax);
     } else {
@@ -575,17 +602,42 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     }
     const V smax = vmax;
     float U = -CUDART_INF_F;
-    for (uint32_t i = lane; i < nused; i += 32) {
+    FilterVal rf[kCertRegRounds];
+#pragma unroll
+    for (int r = 0; r < kCertRegRounds; ++r) {
+      rf[r].sane = false;
+      if (lane + 32 * r < nused) {
+        rf[r] = FilterOf<V>(r32, k32, rKf[r], rS[r], smax, cabs);
+        if (rf[r].sane) U = fmaxf(U, __fsub_rn(rf[r].Y, rf[r].e));
+      }
+    }
+    for (uint32_t i = lane + 32 * kCertRegRounds; i < nused; i += 32) {
       const uint32_t slot = used[i];
-      const FilterVal f = FilterOf<V>(Res32Of(a, x.v), k32, a.Kf[keys[slot]], vals[slot], smax, cabs);
+      const FilterVal f = FilterOf<V>(r32, k32, a.Kf[keys[slot]], vals[slot], smax, cabs);
       if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
     }
     U = WarpMaxFinite(U);
     LexKeyT<V> lead, tail;
-    for (uint32_t i = lane; i < nused; i += 32) {
+#pragma unroll
+    for (int r = 0; r < kCertRegRounds; ++r) {
+      const uint32_t i = lane + 32 * r;
+      if (i >= nused) continue;
+      const uint32_t slot = rslot[r];
+      if (rf[r].sane && __fadd_rn(rf[r].Y, rf[r].e) < U) {
+        keys[slot] = kNone;  // not a contender: cleared now, skipped later
+        vals[slot] = 0;
+        used[i] = 0xFFFFu;
+        continue;
+      }
+      const uint32_t key = keys[slot];
+      const unsigned long long ko = KOrder(a.K[key]);
+      lead.Keep(rS[r], ko, key);
+      tail.Keep(-rS[r], ~ko, key);
+    }
+    for (uint32_t i = lane + 32 * kCertRegRounds; i < nused; i += 32) {
       const uint32_t slot = used[i];
       const uint32_t key = keys[slot];
-      const FilterVal f = FilterOf<V>(Res32Of(a, x.v), k32, a.Kf[key], vals[slot], smax, cabs);
+      const FilterVal f = FilterOf<V>(r32, k32, a.Kf[key], vals[slot], smax, cabs);
       if (f.sane && __fadd_rn(f.Y, f.e) < U) {
         keys[slot] = kNone;  // not a contender: cleared now, skipped later
         vals[slot] = 0;
@@ -609,7 +661,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     uint32_t ctarget = kNone;
     if (single) {
       const float KfA = lead.id != kNone ? a.Kf[lead.id] : 0.f;
-      cres = CertifyDecision<V>(ca, Res32Of(a, x.v), k32, lead.id != kNone, lead.S, KfA, lead.id, a.n, &ctarget);
+      cres = CertifyDecision<V>(ca, r32, k32, lead.id != kNone, lead.S, KfA, lead.id, a.n, &ctarget);
     }
     const uint32_t cmove = cres == kUncertain ? kNone : CertifiedMove(a, x, ctarget, cres == kCertMove);
     bool append = false;
