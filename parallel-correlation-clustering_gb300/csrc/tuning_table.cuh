@@ -6,10 +6,10 @@
 namespace pcc {
 
 constexpr TuningRow kTuningTable[] = {
-    {65536u, 32u, 1000u, 1.0f},
-    {1048576u, 32u, 1000u, 1.0f},
-    {16777216u, 32u, 1000u, 1.0f},
-    {0xFFFFFFFFu, 32u, 1000u, 1.0f},
+    {65536u, 32u, 256u, 1.0f},
+    {1048576u, 32u, 512u, 2.0f},
+    {16777216u, 32u, 512u, 2.0f},
+    {4294967295u, 32u, 512u, 2.0f},
 };
 
 }  // namespace pcc
