@@ -25,6 +25,7 @@ constexpr int kEvalBatch = 4;              // table slots per thread in flight (
 
 constexpr int kSmallThreads = 256;         // small hubs: CTA size, table slots
 constexpr uint32_t kSmallSlots = 2 * kHubSmallMax;
+constexpr uint32_t kSmallMidSlots = 3 * kHubSmallMax / 2;  // hubs with 2d + 2 <= kSmallMidSlots
 constexpr uint32_t kSmallNarrowSlots = kHubSmallMax;  // hubs with 2d + 2 <= kSmallNarrowSlots
 constexpr int kBigThreads = 1024;          // big hubs
 // Big-hub table: ~192 KB of (key, sum) slots.
@@ -913,36 +914,36 @@ int PrepareOnce(K kernel, int threads, size_t smem) {
   return per_sm;
 }
 
+// One small-hub table class over small_v[lo, hi).
+template <bool kInt, bool kAsync, typename V, uint32_t kSlots>
+Status LaunchSmallClass(Context* ctx, const HubArgs& h, uint32_t lo, uint32_t hi) {
+  if (hi <= lo) return Status::Ok();
+  constexpr size_t smem = size_t(kSlots) * (sizeof(V) + sizeof(uint32_t));
+  auto k = HubSmallKernel<kInt, kAsync, V, kSlots>;
+  const int per_sm = PrepareOnce(k, kSmallThreads, smem);
+  if (per_sm <= 0) return MakeError(PCC_INTERNAL, "small-hub kernel cannot be configured");
+  HubArgs hc = h;
+  hc.small_lo = lo;
+  hc.small_hi = hi;
+  k<<<Blocks(hi - lo, 1, unsigned(ctx->num_sms) * unsigned(per_sm)), kSmallThreads, smem, ctx->stream>>>(hc);
+  PCC_COUNT(1);
+  return Status::Ok();
+}
+
 template <bool kInt, bool kAsync, typename V>
-Status LaunchHubT(Context* ctx, const HubArgs& h, uint32_t num_small, uint32_t num_wide, int families) {
+Status LaunchHubT(Context* ctx, const HubArgs& h, uint32_t num_small, uint32_t num_wide, uint32_t num_mid,
+                  int families) {
   const unsigned sms = unsigned(ctx->num_sms);
   if (num_small && (families & kLaunchSmallHubs)) {
-    // Hubs whose 2d + 2 slots exceed the narrow table (listed first) take
-    // the wide one; the rest run with twice the CTAs per SM.
-    const int nl = (num_wide > 0) + (num_small > num_wide);
+    // Three table sizes, each hub in the smallest that holds its 2d + 2
+    // slots (the classes are consecutive in small_v, widest first): smaller
+    // tables fit more CTAs per SM.
+    const uint32_t end_mid = num_wide + num_mid;
+    const int nl = (num_wide > 0) + (num_mid > 0) + (num_small > end_mid);
     FamBegin(ctx, kFamHubSmall);
-    if (num_wide) {
-      constexpr size_t smem = size_t(kSmallSlots) * (sizeof(V) + sizeof(uint32_t));
-      auto k = HubSmallKernel<kInt, kAsync, V, kSmallSlots>;
-      const int per_sm = PrepareOnce(k, kSmallThreads, smem);
-      if (per_sm <= 0) return MakeError(PCC_INTERNAL, "small-hub kernel cannot be configured");
-      HubArgs hw = h;
-      hw.small_lo = 0;
-      hw.small_hi = num_wide;
-      k<<<Blocks(num_wide, 1, sms * unsigned(per_sm)), kSmallThreads, smem, ctx->stream>>>(hw);
-      PCC_COUNT(1);
-    }
-    if (num_small > num_wide) {
-      constexpr size_t smem = size_t(kSmallNarrowSlots) * (sizeof(V) + sizeof(uint32_t));
-      auto k = HubSmallKernel<kInt, kAsync, V, kSmallNarrowSlots>;
-      const int per_sm = PrepareOnce(k, kSmallThreads, smem);
-      if (per_sm <= 0) return MakeError(PCC_INTERNAL, "small-hub kernel cannot be configured");
-      HubArgs hn = h;
-      hn.small_lo = num_wide;
-      hn.small_hi = num_small;
-      k<<<Blocks(num_small - num_wide, 1, sms * unsigned(per_sm)), kSmallThreads, smem, ctx->stream>>>(hn);
-      PCC_COUNT(1);
-    }
+    PCC_RETURN_IF_ERROR((LaunchSmallClass<kInt, kAsync, V, kSmallSlots>(ctx, h, 0, num_wide)));
+    PCC_RETURN_IF_ERROR((LaunchSmallClass<kInt, kAsync, V, kSmallMidSlots>(ctx, h, num_wide, end_mid)));
+    PCC_RETURN_IF_ERROR((LaunchSmallClass<kInt, kAsync, V, kSmallNarrowSlots>(ctx, h, end_mid, num_small)));
     FamEnd(ctx, kFamHubSmall, nl);
   }
   const bool glob = !kAsync && h.num_glob;
@@ -1007,7 +1008,8 @@ Status BuildHubPlan(Context* ctx, const DevGraph& g, const BinSet& bins, HubPlan
     const uint32_t i = order[r];
     if (hd[i] <= kHubSmallMax) {
       small_v.push_back(hv[i]);
-      if (2 * hd[i] + 2 > kSmallNarrowSlots) plan->num_small_wide++;
+      if (2 * hd[i] + 2 > kSmallMidSlots) plan->num_small_wide++;
+      else if (2 * hd[i] + 2 > kSmallNarrowSlots) plan->num_small_mid++;
       continue;
     }
     const uint32_t P = std::max<uint32_t>(1, (hd[i] + kHubBigKeys - 1) / kHubBigKeys);
@@ -1125,6 +1127,9 @@ Status PrepareHubKernels() {
   };
   small(HubSmallKernel<true, false, int, kSmallSlots>, kSmallSlots, sizeof(int));
   small(HubSmallKernel<true, false, int, kSmallNarrowSlots>, kSmallNarrowSlots, sizeof(int));
+  small(HubSmallKernel<true, false, int, kSmallMidSlots>, kSmallMidSlots, sizeof(int));
+  small(HubSmallKernel<true, false, long long, kSmallMidSlots>, kSmallMidSlots, sizeof(long long));
+  small(HubSmallKernel<false, false, double, kSmallMidSlots>, kSmallMidSlots, sizeof(double));
   small(HubSmallKernel<true, false, long long, kSmallSlots>, kSmallSlots, sizeof(long long));
   small(HubSmallKernel<true, false, long long, kSmallNarrowSlots>, kSmallNarrowSlots, sizeof(long long));
   small(HubSmallKernel<false, false, double, kSmallSlots>, kSmallSlots, sizeof(double));
@@ -1176,11 +1181,17 @@ Status LaunchHubBestMoves(Context* ctx, const BMArgs& a, const HubPlan& plan, Hu
   h.gpart_id = st.gpart_id.p;
   h.gdone = st.gdone.p;
   if (a.async) {
-    if (!int_mode) return LaunchHubT<false, true, double>(ctx, h, plan.num_small, plan.num_small_wide, families);
-    return narrow ? LaunchHubT<true, true, int>(ctx, h, plan.num_small, plan.num_small_wide, families) : LaunchHubT<true, true, long long>(ctx, h, plan.num_small, plan.num_small_wide, families);
+    if (!int_mode)
+      return LaunchHubT<false, true, double>(ctx, h, plan.num_small, plan.num_small_wide, plan.num_small_mid, families);
+    return narrow ? LaunchHubT<true, true, int>(ctx, h, plan.num_small, plan.num_small_wide, plan.num_small_mid, families)
+                  : LaunchHubT<true, true, long long>(ctx, h, plan.num_small, plan.num_small_wide, plan.num_small_mid,
+                                                      families);
   }
-  if (!int_mode) return LaunchHubT<false, false, double>(ctx, h, plan.num_small, plan.num_small_wide, families);
-  return narrow ? LaunchHubT<true, false, int>(ctx, h, plan.num_small, plan.num_small_wide, families) : LaunchHubT<true, false, long long>(ctx, h, plan.num_small, plan.num_small_wide, families);
+  if (!int_mode)
+    return LaunchHubT<false, false, double>(ctx, h, plan.num_small, plan.num_small_wide, plan.num_small_mid, families);
+  return narrow ? LaunchHubT<true, false, int>(ctx, h, plan.num_small, plan.num_small_wide, plan.num_small_mid, families)
+                : LaunchHubT<true, false, long long>(ctx, h, plan.num_small, plan.num_small_wide, plan.num_small_mid,
+                                                     families);
 }
 
 }  // namespace pcc

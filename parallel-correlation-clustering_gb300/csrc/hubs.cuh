@@ -36,7 +36,8 @@ constexpr uint32_t kHubGlobalSlice = 1024;   // table slots evaluated by one CTA
 struct HubPlan {
   uint32_t num_hubs = 0;
   uint32_t num_small = 0;      // hubs with degree <= kHubSmallMax
-  uint32_t num_small_wide = 0; // of those, the first ones, with degree > kHubSmallMax / 2 - 1
+  uint32_t num_small_wide = 0; // of those, the first ones, with 2 * degree + 2 > 6144 slots
+  uint32_t num_small_mid = 0;  // then those with 4096 < 2 * degree + 2 <= 6144
   uint32_t num_big = 0;
   uint32_t num_items = 0;      // big-hub work items (hub, partition)
   uint64_t num_partials = 0;   // one per big-hub item
