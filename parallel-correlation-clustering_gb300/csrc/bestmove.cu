@@ -49,15 +49,19 @@ __global__ void __launch_bounds__(256) BestMoveGroupKernel(BMArgs a, const uint3
   const unsigned gmask = G == 32 ? kFull : (((1u << G) - 1u) << (g * G));
   unsigned long long fam_e = 0, fam_v = 0;
   const uint64_t stride = uint64_t(gridDim.x) * 8 * kVpw;
-  for (uint64_t base = (uint64_t(blockIdx.x) * 8 + warp) * kVpw; base < count; base += stride) {
+  // Vertex ids are loaded one iteration ahead (latency-bound kernel).
+  uint64_t base = (uint64_t(blockIdx.x) * 8 + warp) * kVpw;
+  uint32_t vid = base + g < count ? list[start + base + g] : 0u;
+  for (; base < count; base += stride) {
     const uint64_t idx = base + g;
+    const uint32_t nvid = base + stride + g < count ? list[start + base + stride + g] : 0u;
     bool vvalid = idx < count;
     VertexCtx x{};
     if (vvalid) {
-      const uint32_t v = list[start + idx];
-      vvalid = InFront(a, v);
-      if (vvalid) x = LoadVertex<kAsync>(a, v);
+      vvalid = InFront(a, vid);
+      if (vvalid) x = LoadVertex<kAsync>(a, vid);
     }
+    vid = nvid;
     if (__ballot_sync(kFull, vvalid) == 0) continue;
     if (vvalid && gl == 0) {
       fam_e += x.d;
@@ -160,26 +164,47 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
   }
   if (lane == 0) *used_count = 0;
   __syncwarp();
-  for (uint64_t idx = uint64_t(blockIdx.x) * kWarpKernelWarps + warp; idx < count;
-       idx += uint64_t(gridDim.x) * kWarpKernelWarps) {
-    const uint32_t vid = list[start + idx];
-    if (!InFront(a, vid)) continue;
+  // The next vertex id is loaded one iteration ahead and each vertex's
+  // entries kCertUnroll chunks at a time (the loads of the chunks are in
+  // flight together; the sums still run chunk by chunk, in adjacency order).
+  const uint64_t wstride = uint64_t(gridDim.x) * kWarpKernelWarps;
+  uint64_t idx = uint64_t(blockIdx.x) * kWarpKernelWarps + warp;
+  uint32_t vid = idx < count ? list[start + idx] : 0u;
+  for (; idx < count; idx += wstride) {
+    const uint64_t nidx = idx + wstride;
+    const uint32_t nvid = nidx < count ? list[start + nidx] : 0u;
+    if (!InFront(a, vid)) {
+      vid = nvid;
+      continue;
+    }
     const VertexCtx x = LoadVertex<kAsync>(a, vid);
+    vid = nvid;
     if (lane == 0) {
       fam_e += x.d;
       fam_v += 1;
     }
-    for (uint32_t e0 = 0; e0 < x.d; e0 += 32) {
-      const uint32_t e = e0 + lane;
-      const bool has = e < x.d;
-      uint32_t u = x.v;
-      float wt = 0.f;
-      if (has) {
-        u = a.nbr[x.b + e];
-        wt = a.w ? a.w[x.b + e] : 1.0f;
+    for (uint32_t e00 = 0; e00 < x.d; e00 += 32 * kCertUnroll) {
+      uint32_t uu[kCertUnroll], cc[kCertUnroll];
+      float ww[kCertUnroll];
+#pragma unroll
+      for (int k = 0; k < kCertUnroll; ++k) {
+        const uint32_t e = e00 + 32 * k + lane;
+        uu[k] = x.v;
+        ww[k] = 0.f;
+        if (e < x.d) {
+          uu[k] = a.nbr[x.b + e];
+          ww[k] = a.w ? a.w[x.b + e] : 1.0f;
+        }
       }
-      const bool cand = has && u != x.v;
-      const uint32_t cu = cand ? LdC<kAsync>(a.C + u) : kNone;
+#pragma unroll
+      for (int k = 0; k < kCertUnroll; ++k) cc[k] = uu[k] != x.v ? LdC<kAsync>(a.C + uu[k]) : kNone;
+#pragma unroll
+      for (int k = 0; k < kCertUnroll; ++k) {
+      if (e00 + 32 * k >= x.d) break;  // warp-uniform
+      const uint32_t u = uu[k];
+      const float wt = ww[k];
+      const bool cand = u != x.v;
+      const uint32_t cu = cc[k];
       const unsigned peers = __match_any_sync(kFull, cand ? cu : LaneSentinel(lane));
       const bool leader = cand && int(lane) == __ffs(peers) - 1;
       uint32_t slot = kNone;
@@ -215,6 +240,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) BestMoveWarpKernel(BMAr
         }
       }
       __syncwarp();
+      }
     }
     double T = 0.0;
     if (lane == 0) {
