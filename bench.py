@@ -59,7 +59,7 @@ UNIT = "edge-visits/s"
 # frontier; cold L2); the summary and command are in profiles/.  Traffic
 # scales with the entries evaluated, so the per-launch figure at the bench's
 # size is this times the entries of a launch.
-TRAFFIC_BYTES_PER_ENTRY = {"groups": 52.0, "warps": 8.84, "small_hubs": 6.22, "big_hubs": 9.92}
+TRAFFIC_BYTES_PER_ENTRY = {"groups": 51.9, "warps": 8.82, "small_hubs": 6.22, "big_hubs": 9.92}
 
 
 def parse_args():
