@@ -546,9 +546,48 @@ __global__ void BigRunKernel(uint32_t S, uint64_t E, const uint32_t* __restrict_
   }
 }
 
-// One CTA per run longer than 1024: the pbbs blocked fold, level by level,
-// with partials in global scratch (two regions of ceil(len/1024) floats per
-// run at the run's scratch offset).
+// First level of the pbbs blocked fold of every run longer than 1024, over
+// the whole grid: one thread per 1024-item block (bbase: exclusive prefix of
+// the runs' block counts), written to the run's scratch slots.
+struct LongBlocksInput {
+  const uint32_t* long_run;
+  const uint32_t* seg_start;
+  uint32_t S;
+  uint64_t E;
+  __device__ uint64_t operator()(uint64_t li) const {
+    const uint32_t s = long_run[li];
+    const uint64_t len = (s + 1 < S ? seg_start[s + 1] : E) - seg_start[s];
+    return (len + 1023) / 1024;
+  }
+};
+
+__global__ void LongBlocksKernel(uint32_t cnt, uint64_t NB, const uint64_t* __restrict__ bbase,
+                                 const uint32_t* __restrict__ long_run, const uint32_t* __restrict__ seg_start,
+                                 uint32_t S, uint64_t E, const uint32_t* __restrict__ vals,
+                                 float* __restrict__ scratch) {
+  for (uint64_t b = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; b < NB; b += uint64_t(gridDim.x) * blockDim.x) {
+    uint32_t lo = 0, hi = cnt;  // the last run with bbase <= b
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (bbase[mid] <= b) lo = mid;
+      else hi = mid;
+    }
+    const uint32_t s = long_run[lo];
+    const uint64_t a = seg_start[s];
+    const uint64_t len = (s + 1 < S ? seg_start[s + 1] : E) - a;
+    const uint64_t blk = b - bbase[lo];
+    const uint64_t s0 = blk * 1024;
+    const uint64_t l = min(uint64_t(1024), len - s0);
+    float r = __uint_as_float(vals[a + s0]);
+    for (uint64_t j = 1; j < l; ++j) r = __fadd_rn(r, __uint_as_float(vals[a + s0 + j]));
+    scratch[a / 256 + blk] = r;
+  }
+}
+
+// One CTA per run longer than 1024: the pbbs blocked fold from the first
+// level's partials (LongBlocksKernel) on, level by level, with partials in
+// global scratch (two regions of ceil(len/1024) floats per run at the run's
+// scratch offset).
 constexpr int kLongThreads = 1024;
 __global__ void __launch_bounds__(kLongThreads) BigLongKernel(const uint32_t* __restrict__ long_run,
                                                              const uint32_t* __restrict__ long_count,
@@ -566,14 +605,6 @@ __global__ void __launch_bounds__(kLongThreads) BigLongKernel(const uint32_t* __
     float* p0 = scratch + (a / 256);
     uint64_t nb = (len + 1023) / 1024;
     float* p1 = p0 + nb;
-    for (uint64_t blk = threadIdx.x; blk < nb; blk += kLongThreads) {
-      const uint64_t s0 = blk * 1024;
-      const uint64_t l = min(uint64_t(1024), len - s0);
-      float r = __uint_as_float(vals[a + s0]);
-      for (uint64_t j = 1; j < l; ++j) r = __fadd_rn(r, __uint_as_float(vals[a + s0 + j]));
-      p0[blk] = r;
-    }
-    __syncthreads();
     float* cur = p0;
     float* nxt = p1;
     while (nb > 1024) {
@@ -827,11 +858,27 @@ Status CompressGraph(Context* ctx, const DevGraph& g, const uint32_t* C, const d
           S, E, seg_start.p, bkeys.p, bvals.p, kbits, drop, grun.p, blist, ids.p, bkey.p, bval.p, ucount.p,
           long_run.p, long_count.p);
       PCC_COUNT(1);
-      DBuf<float> scratch;
-      PCC_RETURN_IF_ERROR(scratch.Alloc(ctx, E / 256 + 64));
-      BigLongKernel<<<unsigned(ctx->num_sms) * 2, kLongThreads, 0, st>>>(long_run.p, long_count.p, seg_start.p, S,
-                                                                         E, bvals.p, scratch.p, bval.p);
-      PCC_COUNT(1);
+      uint32_t nlong = 0;
+      PCC_RETURN_IF_ERROR(long_count.ToHost(&nlong, 1));
+      PCC_RETURN_IF_ERROR(Sync(ctx));
+      if (nlong) {
+        DBuf<float> scratch;
+        PCC_RETURN_IF_ERROR(scratch.Alloc(ctx, E / 256 + 64));
+        DBuf<uint64_t> bbase, nbtot;
+        PCC_RETURN_IF_ERROR(bbase.Alloc(ctx, nlong));
+        PCC_RETURN_IF_ERROR(nbtot.Alloc(ctx, 1));
+        PCC_RETURN_IF_ERROR(ScanApply<uint64_t>(ctx, nlong, LongBlocksInput{long_run.p, seg_start.p, S, E},
+                                                StorePrefix<uint64_t>{bbase.p}, scan64, nbtot.p));
+        uint64_t NB = 0;
+        PCC_RETURN_IF_ERROR(nbtot.ToHost(&NB, 1));
+        PCC_RETURN_IF_ERROR(Sync(ctx));
+        LongBlocksKernel<<<Blocks(NB, 256, unsigned(ctx->num_sms) * 16), 256, 0, st>>>(
+            nlong, NB, bbase.p, long_run.p, seg_start.p, S, E, bvals.p, scratch.p);
+        PCC_COUNT(1);
+        BigLongKernel<<<unsigned(ctx->num_sms) * 2, kLongThreads, 0, st>>>(long_run.p, long_count.p, seg_start.p,
+                                                                           S, E, bvals.p, scratch.p, bval.p);
+        PCC_COUNT(1);
+      }
     }
     PCC_RETURN_IF_ERROR(LaunchCheck());
     RowCountKernel<<<Blocks(R, 256, ctx->num_sms * 8), 256, 0, st>>>(R, ids.p, ucount.p, row_count.p);
