@@ -219,6 +219,48 @@ __global__ void __launch_bounds__(kT) ApplyLeaveKernel(ApplyArgs a) {
   }
 }
 
+// Leave and join in one pass over the movers: every size and weight update
+// is an atomic add, and the adds commute (the FP64 weight sums are exact for
+// integral node weights), so each mover can leave its cluster and enter its
+// target at once.  Equal clusters inside a warp are combined first, for the
+// leave and for the join.
+__global__ void __launch_bounds__(kT) ApplyMoveKernel(ApplyArgs a) {
+  const uint32_t count = a.ctr->movers;
+  const uint64_t limit = (uint64_t(count) + 31) & ~uint64_t(31);
+  for (uint64_t i = uint64_t(blockIdx.x) * kT + threadIdx.x; i < limit; i += uint64_t(gridDim.x) * kT) {
+    const bool in = i < count;
+    const uint32_t v = in ? a.movers[i] : 0u;
+    const uint32_t c = in ? a.C[v] : kNone;
+    const uint32_t t = in ? a.moves[v] : a.n;
+    const double kv = in ? a.k[v] : 0.0;
+    {
+      const unsigned peers = __match_any_sync(kFull, c);
+      const double tot = GroupSum(peers, kv);
+      if (in && int(LaneId()) == __ffs(peers) - 1) {
+        atomicSub(&a.s[c], uint32_t(__popc(peers)));
+        atomicAdd(&a.K[c], -tot);
+        a.mod_stamp[c] = StampIn(a.rs, a.stamp);
+      }
+    }
+    const bool isnew = in && t == a.n;
+    if (isnew) a.new_stamp[v] = StampIn(a.rs, a.stamp);
+    const unsigned nb = __ballot_sync(kFull, isnew);
+    if (nb && LaneId() == 0) atomicAdd(&a.ctr->new_movers, uint32_t(__popc(nb)));
+    const bool join = in && t != a.n;
+    {
+      const uint32_t key = join ? t : kNone;
+      const unsigned peers = __match_any_sync(kFull, key);
+      const double tot = GroupSum(peers, join ? kv : 0.0);
+      if (join && int(LaneId()) == __ffs(peers) - 1) {
+        atomicAdd(&a.s[t], uint32_t(__popc(peers)));
+        atomicAdd(&a.K[t], tot);
+        a.mod_stamp[t] = StampIn(a.rs, a.stamp);
+      }
+    }
+    if (join) a.C[v] = t;
+  }
+}
+
 // Join: movers to existing clusters enter them.
 __global__ void __launch_bounds__(kT) ApplyJoinKernel(ApplyArgs a) {
   const uint32_t count = a.ctr->movers;
@@ -806,8 +848,7 @@ class Engine {
       ApplyArgs ap{n, L->C.p, L->s.p, L->k.p, L->K.p, moves_.p, movers_.p, mod_stamp_.p, new_stamp_.p, stamp_,
                    ctr_.p, rs};
       const unsigned grid = GridFor(ctx_, rs ? uint64_t(n) : front_size);
-      ApplyLeaveKernel<<<grid, kT, 0, ctx_->stream>>>(ap); PCC_COUNT(1);
-      ApplyJoinKernel<<<grid, kT, 0, ctx_->stream>>>(ap); PCC_COUNT(1);
+      ApplyMoveKernel<<<grid, kT, 0, ctx_->stream>>>(ap); PCC_COUNT(1);
       PCC_RETURN_IF_ERROR(ScanApply<uint32_t>(ctx_, n, ZeroSizeInput{L->s.p, ctr_.p},
                                               StoreIndexIfSet{zero_ids_.p}, scan_tiles_,
                                               un_ ? zcount_.p : static_cast<uint32_t*>(nullptr)));
