@@ -363,9 +363,10 @@ __global__ void __launch_bounds__(kT) AssignNewUnionKernel(ApplyArgs a, const ui
 // Per graph: flags[j] = stamp when the frontier (st == stamp) holds a vertex
 // of graph j, and edges[j] += the degrees of those vertices.
 __global__ void __launch_bounds__(kT) GraphFrontierKernel(uint32_t n, const uint64_t* __restrict__ off,
-                                                          const uint32_t* __restrict__ st, uint32_t stamp,
-                                                          const uint32_t* __restrict__ vbase, uint32_t B,
-                                                          uint32_t* flags, unsigned long long* edges) {
+                                                          const uint32_t* __restrict__ st, uint32_t stamp_arg,
+                                                          const RoundState* rs, const uint32_t* __restrict__ vbase,
+                                                          uint32_t B, uint32_t* flags, unsigned long long* edges) {
+  const uint32_t stamp = StampIn(rs, stamp_arg);
   const uint64_t limit = (uint64_t(n) + 31) & ~uint64_t(31);
   for (uint64_t v = uint64_t(blockIdx.x) * kT + threadIdx.x; v < limit; v += uint64_t(gridDim.x) * kT) {
     const bool in = v < n && st[v] == stamp;
@@ -594,6 +595,36 @@ __global__ void RoundEndKernel(RoundState* rs, DevCounters* ctr, cudaGraphCondit
   if (next) ctr->level_moved = 1;
   rs->iter += 1;
   cudaGraphSetConditional(loop, (next && rs->iter < num_inner) ? 1u : 0u);
+}
+
+// Per-graph bookkeeping of a union round in the device-side loop (after the
+// round's per-graph frontier flags): every graph still in the loop counts
+// the round and its frontier's entries; a graph whose next frontier is empty
+// leaves the loop, as it would alone.  ub: in_loop[B] (bytes) | moved[B]
+// (bytes); pend/ev: per-graph frontier entries and edge visits; rounds.
+struct UnionBook {
+  uint8_t* in_loop;
+  uint8_t* moved;
+  unsigned long long* pend;
+  unsigned long long* ev;
+  uint32_t* rounds;
+};
+
+__global__ void UnionRoundEndKernel(uint32_t B, const RoundState* rs, int all_move, UnionBook ub,
+                                    const uint32_t* __restrict__ gflags, const unsigned long long* __restrict__ gedges) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < B; j += gridDim.x * blockDim.x) {
+    if (!ub.in_loop[j]) continue;
+    ub.rounds[j] += 1;
+    ub.ev[j] += ub.pend[j];
+    if (all_move) {
+      ub.moved[j] = 1;
+    } else if (gflags[j] == rs->stamp) {
+      ub.moved[j] = 1;
+      ub.pend[j] = gedges[j];
+    } else {
+      ub.in_loop[j] = 0;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -890,7 +921,7 @@ class Engine {
       PCC_COUNT(1);
       if (un_) {
         PCC_RETURN_IF_ERROR(gedges_.Zero());
-        GraphFrontierKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g.off.p, next_stamp_.p, stamp_,
+        GraphFrontierKernel<<<GridFor(ctx_, n), kT, 0, ctx_->stream>>>(n, g.off.p, next_stamp_.p, stamp_, rs,
                                                                        un_->d_vbase.p, un_->B, gflags_.p,
                                                                        gedges_.p); PCC_COUNT(1);
       }
@@ -1082,17 +1113,26 @@ class Engine {
   // whether it runs again, and the host reads the counters once the loop is
   // over.  Same kernels and arguments as the host-driven loop, with the stamp
   // and the frontier taken from rs_.
-  Status IterateDevice(Level* L, int64_t num_inner, bool* moved_out) {
+  // init: the round-0 frontier (null: every vertex); book: the union's
+  // per-graph bookkeeping (null: one graph).  *fell_back (when given) is set
+  // instead of running the host-driven loop if CUDA graphs are unavailable.
+  Status IterateDevice(Level* L, int64_t num_inner, bool* moved_out, const RoundState* init = nullptr,
+                       const UnionBook* book = nullptr, bool* fell_back = nullptr) {
     const DevGraph& g = *L->g;
     PCC_RETURN_IF_ERROR(PrepareBestMoveKernels());
     PCC_RETURN_IF_ERROR(PrepareHubKernels());
     PCC_RETURN_IF_ERROR(ctx_->EnsureSideStreams());
     RoundState h{};
+    if (init) {
+      h = *init;
+    } else {
+      h.front_all = 1;
+      h.front_edges = g.m;
+      h.front_size = g.n;
+      h.visited = L->bins->size;
+    }
     h.stamp = stamp_;  // RoundBeginKernel increments it first
-    h.front_all = 1;
-    h.front_edges = g.m;
-    h.front_size = g.n;
-    h.visited = L->bins->size;
+    h.iter = 0;
     PCC_RETURN_IF_ERROR(rs_.FromHost(&h, 1));
     PCC_CUDA(cudaMemsetAsync(&ctr_.p->level_moved, 0, sizeof(uint32_t) * 2, ctx_->stream));  // level_moved, rounds
     PCC_CUDA(cudaMemsetAsync(&ctr_.p->edge_visits, 0, sizeof(unsigned long long) * 2, ctx_->stream));
@@ -1119,6 +1159,10 @@ class Engine {
       cleanup();
       cudaGetLastError();
       ctx_->graphs_failed = true;
+      if (fell_back) {
+        *fell_back = true;
+        return Status::Ok();
+      }
       return IterateBestMoves(L, num_inner, moved_out);
     }
     cudaGraph_t body = cp.conditional.phGraph_out[0];
@@ -1135,10 +1179,19 @@ class Engine {
       cleanup();
       cudaGetLastError();
       ctx_->graphs_failed = true;
+      if (fell_back) {
+        *fell_back = true;
+        return Status::Ok();
+      }
       return IterateBestMoves(L, num_inner, moved_out);
     }
     RoundBeginKernel<<<1, 1, 0, ctx_->stream>>>(rs_.p); PCC_COUNT(1);
     Status st = EnqueueRound(L, 0, g.n, rs_.p);
+    if (book && st.ok()) {
+      UnionRoundEndKernel<<<Blocks(un_->B, 256, 1024), 256, 0, ctx_->stream>>>(
+          un_->B, rs_.p, cfg_.move_method == PCC_ALL_MOVE ? 1 : 0, *book, gflags_.p, gedges_.p);
+      PCC_COUNT(1);
+    }
     RoundEndKernel<<<1, 1, 0, ctx_->stream>>>(rs_.p, ctr_.p, loop, static_cast<uint32_t>(num_inner),
                                               cfg_.move_method == PCC_ALL_MOVE ? 1 : 0, g.n, g.m, L->bins->size);
     PCC_COUNT(1);
@@ -1403,6 +1456,16 @@ class Engine {
       return MakeError(PCC_INTERNAL, "ALL_MOVE union rounds must include every graph");
     GraphEntriesKernel<<<Blocks(B, kT, 1024), kT, 0, ctx_->stream>>>(B, g.n, un_->d_vbase.p, g.off.p, gedges_.p);
     PCC_COUNT(1);
+    const bool device_loop = !ctx_->detailed_timing && !ctx_->graphs_failed && g.m >= ctx_->device_loop_min_entries;
+    if (device_loop) {
+      // Round-0 per-graph frontier entries, flags and counters on the device.
+      PCC_CUDA(cudaMemcpyAsync(ub_pend_.p, gedges_.p, sizeof(unsigned long long) * B, cudaMemcpyDeviceToDevice,
+                               ctx_->stream));
+      PCC_RETURN_IF_ERROR(ub_flags_.FromHost(in_loop.data(), B));
+      PCC_CUDA(cudaMemsetAsync(ub_flags_.p + B, 0, B, ctx_->stream));  // moved
+      PCC_RETURN_IF_ERROR(ub_ev_.Zero());
+      PCC_RETURN_IF_ERROR(ub_rounds_.Zero());
+    }
     PCC_RETURN_IF_ERROR(gedges_.ToHost(h_gent_.data(), B));
     uint32_t front = 0;
     uint64_t fe = g.m, fs = g.n;
@@ -1425,6 +1488,32 @@ class Engine {
       fs = hc.frontier;
     } else {
       PCC_RETURN_IF_ERROR(Sync(ctx_));
+    }
+    if (device_loop) {
+      RoundState init{};
+      init.front_all = all ? 1 : 0;
+      init.front_val = front;
+      init.front_edges = fe;
+      init.front_size = fs;
+      init.visited = all ? L->bins->size : fs;
+      const UnionBook book{ub_flags_.p, ub_flags_.p + B, ub_pend_.p, ub_ev_.p, ub_rounds_.p};
+      bool fell_back = false, any_moved = false;
+      PCC_RETURN_IF_ERROR(IterateDevice(L, num_inner, &any_moved, &init, &book, &fell_back));
+      if (!fell_back) {
+        std::vector<uint8_t> flags(2 * size_t(B));
+        std::vector<unsigned long long> ev(B);
+        std::vector<uint32_t> rounds(B);
+        PCC_RETURN_IF_ERROR(ub_flags_.ToHost(flags.data(), 2 * size_t(B)));
+        PCC_RETURN_IF_ERROR(ub_ev_.ToHost(ev.data(), B));
+        PCC_RETURN_IF_ERROR(ub_rounds_.ToHost(rounds.data(), B));
+        PCC_RETURN_IF_ERROR(Sync(ctx_));
+        for (uint32_t j = 0; j < B; ++j) {
+          gr[j].rounds += static_cast<int32_t>(rounds[j]);
+          gr[j].edge_visits += ev[j];
+          (*moved)[j] = flags[B + j];
+        }
+        return Status::Ok();
+      }
     }
     std::vector<unsigned long long> pend(h_gent_.begin(), h_gent_.begin() + B);
     bool local_moved = true;
@@ -1477,6 +1566,10 @@ class Engine {
     PCC_RETURN_IF_ERROR(gflags_.Zero());
     PCC_RETURN_IF_ERROR(gmask_.Alloc(ctx_, B));
     PCC_RETURN_IF_ERROR(gedges_.Alloc(ctx_, B));
+    PCC_RETURN_IF_ERROR(ub_flags_.Alloc(ctx_, 2 * uint64_t(B)));
+    PCC_RETURN_IF_ERROR(ub_pend_.Alloc(ctx_, B));
+    PCC_RETURN_IF_ERROR(ub_ev_.Alloc(ctx_, B));
+    PCC_RETURN_IF_ERROR(ub_rounds_.Alloc(ctx_, B));
     PCC_RETURN_IF_ERROR(zcount_.Alloc(ctx_, 1));
     h_gflags_.assign(B, 0);
     h_mask_.assign(B, 0);
@@ -1661,6 +1754,11 @@ class Engine {
   const UnionLayout* un_ = nullptr;
   DBuf<uint32_t> gflags_, gmask_, zcount_;
   DBuf<unsigned long long> gedges_;
+  // Device-side union loop: in_loop[B] | moved[B], per-graph frontier
+  // entries, edge visits and rounds.
+  DBuf<uint8_t> ub_flags_;
+  DBuf<unsigned long long> ub_pend_, ub_ev_;
+  DBuf<uint32_t> ub_rounds_;
   std::vector<uint32_t> h_gflags_, h_mask_;
   std::vector<unsigned long long> h_gedges_, h_gent_;
 };
