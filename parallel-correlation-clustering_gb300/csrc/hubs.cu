@@ -111,15 +111,18 @@ __device__ __forceinline__ V AtomicAddV(V* p, V x) {
   }
 }
 
-// Shared scratch of a hub CTA of BT threads besides its table.
+// Shared scratch of a hub CTA of BT threads besides its table.  The
+// reduction arrays hold one partial per warp; their last element carries a
+// result that warp 0 publishes (wide CTAs, HubChangeSmax).
 template <int BT>
 struct HubShared {
   static constexpr int kW = BT / 32;
-  long long red_ll[kW];
-  unsigned long long red_k[kW];
+  long long red_ll[kW + 1];
+  long long red_mx[kW + 1];
+  unsigned long long red_k[kW + 1];
   double red_d[kW];
-  float red_f[kW];
-  uint32_t red_i[kW];
+  float red_f[kW + 1];
+  uint32_t red_i[kW + 1];
   int stage_i[kW][32];
   double stage_d[kW][32];
   uint32_t cont_key[kMaxCont];
@@ -132,13 +135,30 @@ struct HubShared {
   float change32;
 };
 
-// Block reductions; every thread receives the result.
+// Block reductions; every thread receives the result.  In wide CTAs (512
+// threads and more) warp 0 combines the warps' partials and publishes the
+// result in red[BT / 32], so that the other threads read one value instead
+// of BT / 32; the combines here (max, integer sum, lexicographic and
+// (value, id) selections) give the same result in any order.
+template <int BT>
+constexpr bool kWideBlock = BT >= 512;
+
 template <int BT>
 __device__ __forceinline__ long long BlockMaxLL(long long x, long long* red) {
 #pragma unroll
   for (int o = 16; o; o >>= 1) x = max(x, __shfl_xor_sync(kFull, x, o));
   if (LaneId() == 0) red[threadIdx.x >> 5] = x;
   __syncthreads();
+  if constexpr (kWideBlock<BT>) {
+    if (threadIdx.x < 32) {
+      long long r = threadIdx.x < BT / 32 ? red[threadIdx.x] : LLONG_MIN;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) r = max(r, __shfl_xor_sync(kFull, r, o));
+      if (threadIdx.x == 0) red[BT / 32] = r;
+    }
+    __syncthreads();
+    return red[BT / 32];
+  }
   long long r = red[0];
 #pragma unroll
   for (int w = 1; w < BT / 32; ++w) r = max(r, red[w]);
@@ -152,6 +172,16 @@ __device__ __forceinline__ float BlockMaxF(float x, float* red) {
   for (int o = 16; o; o >>= 1) x = fmaxf(x, __shfl_xor_sync(kFull, x, o));
   if (LaneId() == 0) red[threadIdx.x >> 5] = x;
   __syncthreads();
+  if constexpr (kWideBlock<BT>) {
+    if (threadIdx.x < 32) {
+      float r = threadIdx.x < BT / 32 ? red[threadIdx.x] : -CUDART_INF_F;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) r = fmaxf(r, __shfl_xor_sync(kFull, r, o));
+      if (threadIdx.x == 0) red[BT / 32] = r;
+    }
+    __syncthreads();
+    return red[BT / 32];
+  }
   float r = red[0];
 #pragma unroll
   for (int w = 1; w < BT / 32; ++w) r = fmaxf(r, red[w]);
@@ -172,6 +202,16 @@ __device__ __forceinline__ T BlockSum(T x, T* red) {
   }
   if (LaneId() == 0) red[threadIdx.x >> 5] = x;
   __syncthreads();
+  if constexpr (kWideBlock<BT> && std::is_integral<T>::value) {
+    if (threadIdx.x < 32) {
+      T r = threadIdx.x < BT / 32 ? red[threadIdx.x] : T(0);
+#pragma unroll
+      for (int o = 16; o; o >>= 1) r += __shfl_xor_sync(kFull, r, o);
+      if (threadIdx.x == 0) red[BT / 32] = r;
+    }
+    __syncthreads();
+    return red[BT / 32];
+  }
   T r = red[0];
 #pragma unroll
   for (int w = 1; w < BT / 32; ++w) {
@@ -219,6 +259,27 @@ __device__ __forceinline__ void BlockArgmax(double& v, uint32_t& id, unsigned lo
     redi[threadIdx.x >> 5] = id;
   }
   __syncthreads();
+  if constexpr (kWideBlock<BT>) {
+    if (threadIdx.x < 32) {
+      const bool in = threadIdx.x < BT / 32;
+      unsigned long long wo = redv[in ? threadIdx.x : 0];
+      uint32_t wi = in ? redi[threadIdx.x] : kNone;
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        const unsigned long long oo = __shfl_xor_sync(kFull, wo, off);
+        const uint32_t oi = __shfl_xor_sync(kFull, wi, off);
+        KeepBits(wo, wi, oo, oi);
+      }
+      if (threadIdx.x == 0) {
+        redv[BT / 32] = wo;
+        redi[BT / 32] = wi;
+      }
+    }
+    __syncthreads();
+    v = BitsVal(redv[BT / 32]);
+    id = redi[BT / 32];
+    return;
+  }
   unsigned long long ro = redv[0];
   uint32_t ri = redi[0];
 #pragma unroll
@@ -237,6 +298,22 @@ __device__ __forceinline__ LexKeyT<I> BlockLex(LexKeyT<I> x, long long* rs, unsi
     ri[threadIdx.x >> 5] = x.id;
   }
   __syncthreads();
+  if constexpr (kWideBlock<BT>) {
+    if (threadIdx.x < 32) {
+      LexKeyT<I> w;
+      if (threadIdx.x < BT / 32) w.Keep(static_cast<I>(rs[threadIdx.x]), rk[threadIdx.x], ri[threadIdx.x]);
+      LexGroupReduce<32, I>(w);
+      if (threadIdx.x == 0) {
+        rs[BT / 32] = w.S;
+        rk[BT / 32] = w.K;
+        ri[BT / 32] = w.id;
+      }
+    }
+    __syncthreads();
+    LexKeyT<I> r;
+    r.Keep(static_cast<I>(rs[BT / 32]), rk[BT / 32], ri[BT / 32]);
+    return r;
+  }
   LexKeyT<I> r;
 #pragma unroll
   for (int w = 0; w < BT / 32; ++w) r.Keep(static_cast<I>(rs[w]), rk[w], ri[w]);
@@ -259,8 +336,23 @@ __device__ __forceinline__ bool BlockLexLeadInt(LexKeyT<int>& lead, const LexKey
   }
   __syncthreads();
   LexKeyT<int> r;
+  if constexpr (kWideBlock<BT>) {
+    if (threadIdx.x < 32) {
+      LexKeyT<int> w;
+      if (threadIdx.x < BT / 32) w.Keep(static_cast<int>(rs[threadIdx.x]), rk[threadIdx.x], ri[threadIdx.x]);
+      LexWarpLeaderInt(w);
+      if (threadIdx.x == 0) {
+        rs[BT / 32] = w.S;
+        rk[BT / 32] = w.K;
+        ri[BT / 32] = w.id;
+      }
+    }
+    __syncthreads();
+    r.Keep(static_cast<int>(rs[BT / 32]), rk[BT / 32], ri[BT / 32]);
+  } else {
 #pragma unroll
-  for (int w = 0; w < BT / 32; ++w) r.Keep(static_cast<int>(rs[w]), rk[w], ri[w]);
+    for (int w = 0; w < BT / 32; ++w) r.Keep(static_cast<int>(rs[w]), rk[w], ri[w]);
+  }
   lead = r;
   const bool diff = r.id != kNone && tail.id != kNone && (-tail.S != r.S || ~tail.K != r.K);
   return !__syncthreads_or(diff);  // also orders the reads of rs/rk/ri before their next use
@@ -344,6 +436,12 @@ __device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double
     const float c32 = sh.change32;
     const float r32 = Res32Of(a, x.v);
     float U = -CUDART_INF_F;
+    // The two largest upper ends (Y + e; +inf for a candidate outside the
+    // error model) among this thread's slots, and the slot of the largest:
+    // when the second is below the block's U, no other slot of the thread
+    // can be a contender and the second pass need not re-evaluate them.
+    float hi1 = -CUDART_INF_F, hi2 = -CUDART_INF_F;
+    uint32_t slot1 = kNone;
     for (uint32_t s0 = tid; s0 < cap; s0 += BT * kB) {
       uint32_t kk[kB];
       I ss[kB];
@@ -361,12 +459,46 @@ __device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double
         if (kk[j] == kNone) continue;
         const FilterVal f = FilterOf<I>(r32, k32, kf[j], ss[j], smax, c32);
         if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
+        const float hi = f.sane ? __fadd_rn(f.Y, f.e) : CUDART_INF_F;
+        if (hi > hi1) {
+          hi2 = hi1;
+          hi1 = hi;
+          slot1 = s0 + j * BT;
+        } else if (hi > hi2) {
+          hi2 = hi;
+        }
       }
     }
     if (tid == 0) sh.ncont = 0;
     U = BlockMaxF<BT>(U, sh.red_f);
     LexKeyT<I> lead, tail;
-    for (uint32_t s0 = tid; s0 < cap; s0 += BT * kB) {
+    // The contenders are the slots with hi >= U (every slot when U = -inf).
+    const bool rescan = !(hi2 < U);
+    if (!rescan) {
+      // At most slot1 is a contender; the thread's other slots are cleared.
+      if (slot1 != kNone && !(hi1 < U)) {
+        const uint32_t key = skeys[slot1];
+        const I S = static_cast<I>(svals[slot1]);
+        const double KD = a.K[key];
+        const unsigned long long ko = KOrder(KD);
+        lead.Keep(S, ko, key);
+        tail.Keep(-S, ~ko, key);
+        const uint32_t pos = atomicAdd(&sh.ncont, 1u);
+        if (pos < kMaxCont) {
+          sh.cont_key[pos] = key;
+          sh.cont_S[pos] = S;
+        } else {
+          KeepBest(lv, lid, ValOf(a, x, change, static_cast<double>(S), KD), key);  // list full: now
+        }
+      }
+      for (uint32_t s = tid; s < cap; s += BT) {
+        if (skeys[s] != kNone) {
+          skeys[s] = kNone;
+          svals[s] = V(0);
+        }
+      }
+    }
+    for (uint32_t s0 = rescan ? tid : cap; s0 < cap; s0 += BT * kB) {
       uint32_t kk[kB];
       I ss[kB];
       float kf[kB];
@@ -561,6 +693,53 @@ __device__ __forceinline__ double HubChange(const BMArgs& a, const VertexCtx& x,
   return sh.change;
 }
 
+// HubChange and, in INT mode, the block maximum of the running sums.  Wide
+// CTAs take both in one reduction: warp 0 combines the warps' (sum, max)
+// partials and its lane 0 computes the change, so that the table scan's end
+// costs two barriers.
+template <int BT, bool kInt>
+__device__ __forceinline__ double HubChangeSmax(const BMArgs& a, const VertexCtx& x, long long t_int, double t_dbl,
+                                                long long* smax, HubShared<BT>& sh) {
+  if constexpr (!kWideBlock<BT>) {
+    __syncthreads();
+    const double change = HubChange<BT, kInt>(a, x, t_int, t_dbl, sh);
+    if (kInt) *smax = BlockMaxLL<BT>(*smax, sh.red_ll);
+    return change;
+  } else if constexpr (!kInt) {
+    return HubChange<BT, kInt>(a, x, t_int, t_dbl, sh);
+  } else {
+    constexpr int kW = BT / 32;
+    long long t = t_int, m = *smax;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      t += __shfl_xor_sync(kFull, t, o);
+      m = max(m, __shfl_xor_sync(kFull, m, o));
+    }
+    if (LaneId() == 0) {
+      sh.red_ll[threadIdx.x >> 5] = t;
+      sh.red_mx[threadIdx.x >> 5] = m;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      long long wt = threadIdx.x < kW ? sh.red_ll[threadIdx.x] : 0;
+      long long wm = threadIdx.x < kW ? sh.red_mx[threadIdx.x] : LLONG_MIN;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        wt += __shfl_xor_sync(kFull, wt, o);
+        wm = max(wm, __shfl_xor_sync(kFull, wm, o));
+      }
+      if (threadIdx.x == 0) {
+        sh.change = ChangeOf(a, x, static_cast<double>(wt));
+        sh.change32 = static_cast<float>(sh.change);
+        sh.red_mx[kW] = wm;
+      }
+    }
+    __syncthreads();
+    *smax = sh.red_mx[kW];
+    return sh.change;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Small hubs: one CTA per hub, a table of 2 * degree slots (never full).
 // ---------------------------------------------------------------------------
@@ -595,9 +774,8 @@ __global__ void __launch_bounds__(kSmallThreads) HubSmallKernel(HubArgs h) {
     long long t_int = 0, smax = LLONG_MIN;
     double t_dbl = 0.0;
     ScanRow<BT, kInt, kAsync, V>(a, x, 1, 0, 1, 0, true, skeys, svals, cap, cap, sh, &t_int, &t_dbl, &smax);
-    __syncthreads();
-    const double change = HubChange<BT, kInt>(a, x, t_int, t_dbl, sh);
-    if (kInt) smax = BlockMaxLL<BT>(smax, sh.red_ll);
+    // Its barriers also complete the table and sh.overflow before they are read.
+    const double change = HubChangeSmax<BT, kInt>(a, x, t_int, t_dbl, &smax, sh);
     if (tid == 0) {
       if (sh.overflow) atomicExch(&a.ctr->error, kErrHashFull);  // cannot happen: 2d + 2 slots
       sh.nkeys = 0;
@@ -661,12 +839,14 @@ __global__ void __launch_bounds__(kBigThreads) HubBigKernel(HubArgs h) {
       double t_dbl = 0.0;
       ScanRow<BT, kInt, kAsync, V>(a, x, P, p, Q, q, !have_T, skeys, svals, cap, maxkeys, sh, &t_int, &t_dbl,
                                    &smax);
-      __syncthreads();
+      // The reductions' barriers also order the reads of sh.overflow.
       if (!have_T) {
-        change = HubChange<BT, kInt>(a, x, t_int, t_dbl, sh);
+        change = HubChangeSmax<BT, kInt>(a, x, t_int, t_dbl, &smax, sh);
         have_T = true;
+      } else {
+        __syncthreads();
+        if (kInt) smax = BlockMaxLL<BT>(smax, sh.red_ll);
       }
-      if (kInt) smax = BlockMaxLL<BT>(smax, sh.red_ll);  // also orders the reads of sh.overflow
       const bool overflow = sh.overflow != 0;
       __syncthreads();
       if (tid == 0) {

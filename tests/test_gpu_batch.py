@@ -5,6 +5,7 @@ HBM budget."""
 import numpy as np
 import pytest
 
+import oracle as O
 import pcc_gb300 as P
 import pcc_graphs as G
 
@@ -117,6 +118,23 @@ def test_union_mixed_resolutions_and_objectives(ctx, small_graphs, move):
     labels2, stats2, _ = P.cluster_batch(graphs, cfgs, objectives=objs)
     for a, b in zip(labels, labels2):
         np.testing.assert_array_equal(a, b)
+
+
+def test_union_matches_oracle_on_batch_distribution(ctx, small_graphs):
+    """Two graphs of the batched SBM distribution with 20k-50k vertices, in
+    one union with small graphs, at resolution 0.05 with refinement: labels
+    and statistics bit-identical to the oracle's sequential clustering."""
+    big = G.batch_sbm_graphs(2, seed=21, n_lo=20000, n_hi=50000)
+    assert all(20000 <= g.n <= 50000 for g in big)
+    graphs = [small_graphs[0], big[0], small_graphs[1], big[1]]
+    cfg = P.make_config(resolution=0.05, refine=True)
+    labels, stats, _ = P.cluster_union(ctx, graphs, cfg)
+    for i in (1, 3):
+        lab_o, st_o = O.correlation_cluster(O.OracleGraph(graphs[i]), cfg)
+        np.testing.assert_array_equal(labels[i], lab_o)
+        for key in ("num_clusters", "rounds", "levels", "edge_visits"):
+            assert stats[i][key] == st_o[key], key
+        assert stats[i]["objective"] == pytest.approx(st_o["objective"], rel=1e-12, abs=1e-9)
 
 
 def test_union_node_weights_and_real_weights(ctx, small_graphs):
