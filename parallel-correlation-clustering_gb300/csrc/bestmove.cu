@@ -628,6 +628,11 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     }
     const V smax = vmax;
     float U = -CUDART_INF_F;
+    // The two largest upper ends (Y + e; +inf outside the error model) of
+    // this lane's candidates and the index of the largest: when the second
+    // is below U, only that one can be a contender.
+    float hi1 = -CUDART_INF_F, hi2 = -CUDART_INF_F;
+    uint32_t i1 = kNone;
     FilterVal rf[kCertRegRounds];
 #pragma unroll
     for (int r = 0; r < kCertRegRounds; ++r) {
@@ -635,19 +640,41 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
       if (lane + 32 * r < nused) {
         rf[r] = FilterOf<V>(r32, k32, rKf[r], rS[r], smax, cabs);
         if (rf[r].sane) U = fmaxf(U, __fsub_rn(rf[r].Y, rf[r].e));
+        KeepTop2(hi1, hi2, i1, rf[r].sane ? __fadd_rn(rf[r].Y, rf[r].e) : CUDART_INF_F, lane + 32 * r);
       }
     }
     for (uint32_t i = lane + 32 * kCertRegRounds; i < nused; i += 32) {
       const uint32_t slot = used[i];
       const FilterVal f = FilterOf<V>(r32, k32, a.Kf[keys[slot]], vals[slot], smax, cabs);
       if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
+      KeepTop2(hi1, hi2, i1, f.sane ? __fadd_rn(f.Y, f.e) : CUDART_INF_F, i);
     }
     U = WarpMaxFinite(U);
     LexKeyT<V> lead, tail;
+    // The contenders are the candidates with Y + e >= U (all when U = -inf).
+    if (hi2 < U) {
+      // At most candidate i1 is a contender: the others are cleared and
+      // marked without evaluating them again.
+      for (uint32_t i = lane; i < nused; i += 32) {
+        const uint32_t slot = used[i];
+        if (i == i1 && !(hi1 < U)) {
+          const uint32_t key = keys[slot];
+          const V S = vals[slot];
+          const unsigned long long ko = KOrder(a.K[key]);
+          lead.Keep(S, ko, key);
+          tail.Keep(-S, ~ko, key);
+          continue;
+        }
+        keys[slot] = kNone;
+        vals[slot] = 0;
+        used[i] = 0xFFFFu;
+      }
+    }
+    const uint32_t rescan_end = hi2 < U ? 0u : nused;
 #pragma unroll
     for (int r = 0; r < kCertRegRounds; ++r) {
       const uint32_t i = lane + 32 * r;
-      if (i >= nused) continue;
+      if (i >= rescan_end) continue;
       const uint32_t slot = rslot[r];
       if (rf[r].sane && __fadd_rn(rf[r].Y, rf[r].e) < U) {
         keys[slot] = kNone;  // not a contender: cleared now, skipped later
@@ -660,7 +687,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
       lead.Keep(rS[r], ko, key);
       tail.Keep(-rS[r], ~ko, key);
     }
-    for (uint32_t i = lane + 32 * kCertRegRounds; i < nused; i += 32) {
+    for (uint32_t i = lane + 32 * kCertRegRounds; i < rescan_end; i += 32) {
       const uint32_t slot = used[i];
       const uint32_t key = keys[slot];
       const FilterVal f = FilterOf<V>(r32, k32, a.Kf[key], vals[slot], smax, cabs);
@@ -847,10 +874,13 @@ __global__ void __launch_bounds__(kCtaWarps * 32) CertCtaKernel(BMArgs a, const 
 #pragma unroll
     for (int w = 1; w < kCtaWarps; ++w) smax = max(smax, s_max[w]);
     float U = -CUDART_INF_F;
+    float hi1 = -CUDART_INF_F, hi2 = -CUDART_INF_F;  // KeepTop2 of this thread's candidates
+    uint32_t i1 = kNone;
     for (uint32_t i = tid; i < nused; i += BT) {
       const uint32_t slot = used[i];
       const FilterVal f = FilterOf<V>(Res32Of(a, x.v), k32, a.Kf[keys[slot]], vals[slot], smax, cabs);
       if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
+      KeepTop2(hi1, hi2, i1, f.sane ? __fadd_rn(f.Y, f.e) : CUDART_INF_F, i);
     }
     U = WarpMaxFinite(U);
     if (lane == 0) s_u[warp] = U;
@@ -859,7 +889,28 @@ __global__ void __launch_bounds__(kCtaWarps * 32) CertCtaKernel(BMArgs a, const 
 #pragma unroll
     for (int w = 1; w < kCtaWarps; ++w) U = fmaxf(U, s_u[w]);
     LexKeyT<V> lead, tail;
-    for (uint32_t i = tid; i < nused; i += BT) {
+    // The contenders are the candidates with Y + e >= U (all when U = -inf);
+    // when this thread's runner-up is below U, at most its candidate i1 is
+    // one, and the others are cleared and marked without a second
+    // evaluation.
+    const bool rescan = !(hi2 < U);
+    if (!rescan) {
+      for (uint32_t i = tid; i < nused; i += BT) {
+        const uint32_t slot = used[i];
+        if (i == i1 && !(hi1 < U)) {
+          const uint32_t key = keys[slot];
+          const V S = vals[slot];
+          const unsigned long long ko = KOrder(a.K[key]);
+          lead.Keep(S, ko, key);
+          tail.Keep(-S, ~ko, key);
+          continue;
+        }
+        keys[slot] = kNone;
+        vals[slot] = 0;
+        used[i] = 0xFFFFu;
+      }
+    }
+    for (uint32_t i = tid; i < (rescan ? nused : 0u); i += BT) {
       const uint32_t slot = used[i];
       const uint32_t key = keys[slot];
       const FilterVal f = FilterOf<V>(Res32Of(a, x.v), k32, a.Kf[key], vals[slot], smax, cabs);

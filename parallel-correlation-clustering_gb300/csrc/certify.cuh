@@ -172,6 +172,20 @@ __device__ __forceinline__ FilterVal FilterOf(float r32, float k32, float KfD, I
   return f;
 }
 
+// Running top two of the candidates' upper ends (Y + e), with the index of
+// the largest.  A pre-filter pass keeps them so that its second pass can
+// skip re-evaluating a thread's candidates when the runner-up is below the
+// pass's U: then at most the largest can be a contender.
+__device__ __forceinline__ void KeepTop2(float& hi1, float& hi2, uint32_t& i1, float hi, uint32_t i) {
+  if (hi > hi1) {
+    hi2 = hi1;
+    hi1 = hi;
+    i1 = i;
+  } else if (hi > hi2) {
+    hi2 = hi;
+  }
+}
+
 // Result of the certification: kUncertain = take the FP64 path.
 enum CertResult : int { kCertNoMove = 0, kCertMove = 1, kUncertain = 2 };
 

@@ -459,14 +459,7 @@ __device__ void EvalTable(const BMArgs& a, const VertexCtx& x, float k32, double
         if (kk[j] == kNone) continue;
         const FilterVal f = FilterOf<I>(r32, k32, kf[j], ss[j], smax, c32);
         if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
-        const float hi = f.sane ? __fadd_rn(f.Y, f.e) : CUDART_INF_F;
-        if (hi > hi1) {
-          hi2 = hi1;
-          hi1 = hi;
-          slot1 = s0 + j * BT;
-        } else if (hi > hi2) {
-          hi2 = hi;
-        }
+        KeepTop2(hi1, hi2, slot1, f.sane ? __fadd_rn(f.Y, f.e) : CUDART_INF_F, s0 + j * BT);
       }
     }
     if (tid == 0) sh.ncont = 0;
