@@ -95,6 +95,28 @@ def test_union_matches_single_every_control_path(ctx, move, refine):
                 assert stats[i][key] == rst[key], (i, key, iters)
 
 
+@pytest.mark.parametrize("move", [P.NBHR_CLUSTER_MOVE, P.NBHR_MOVE, P.ALL_MOVE])
+def test_union_device_loop_matches_host_loop(ctx, move):
+    """Union rounds run as the device-side loop (per-graph rounds, edge
+    visits and in-loop flags kept on the device) and, with detailed timing,
+    driven from the host: labels and every per-graph counter agree."""
+    graphs = _union_mix()
+    cfg = P.make_config(resolution=0.05, refine=True, move_method=move,
+                        louvain_num_iterations=4, louvain_num_inner_iterations=3)
+    lab_d, st_d, tot_d = P.cluster_union(ctx, graphs, cfg)
+    ctx.set_detailed_timing(True)
+    try:
+        lab_h, st_h, tot_h = P.cluster_union(ctx, graphs, cfg)
+    finally:
+        ctx.set_detailed_timing(False)
+    for i in range(len(graphs)):
+        np.testing.assert_array_equal(lab_d[i], lab_h[i], err_msg=f"graph {i}")
+        for key in UNION_STATS:
+            assert st_d[i][key] == st_h[i][key], (i, key)
+    for key in ("edge_visits", "vertex_visits", "moves", "rounds", "levels"):
+        assert tot_d[key] == tot_h[key], key
+
+
 @pytest.mark.parametrize("move", [P.NBHR_CLUSTER_MOVE, P.ALL_MOVE])
 def test_union_mixed_resolutions_and_objectives(ctx, small_graphs, move):
     """Graphs with their own resolutions and objectives in one union: every
