@@ -403,7 +403,10 @@ pcc_status pcc_cluster_batch(int device, uint32_t num_graphs, const pcc_batch_gr
  *   - its own resolution.
  * So its labels and objective equal those of a standalone call (bit for bit
  * with integer weights and node weights, else within FP64 summation order for
- * the objective; modularity within 1e-12 relative).
+ * the objective; modularity within 1e-12 relative).  The rounds of a level
+ * run as one device-side loop (a CUDA graph WHILE node) that keeps each
+ * graph's rounds, edge visits and in-loop flag on the device, with one host
+ * read per level; with detailed timing on, the host drives them.
  * configs: one for all graphs or one per graph, equal in every field but the
  * resolution; LOUVAIN, synchronous, NONE_SUBCLUSTERING.  objectives: NULL
  * (correlation) or one per graph (0 correlation, 1 modularity: node weights

@@ -79,9 +79,10 @@ struct Context {
   // family, host-driven rounds) is on, or graphs are unavailable.
   bool detailed_timing = false;
   bool graphs_failed = false;
-  // Levels with fewer entries run host-driven rounds.  Capturing and
-  // instantiating a level's loop takes driver locks that concurrent worker
-  // contexts contend for, so the serving pool raises this for small graphs.
+  // Levels (and union levels) with fewer entries run host-driven rounds.
+  // Capturing and instantiating a level's loop takes driver locks that
+  // concurrent worker contexts contend for, so the serving pool's workers set
+  // it above any graph size.
   uint64_t device_loop_min_entries = 0;
   std::atomic<uint64_t> in_use{0};
   std::atomic<uint64_t> peak{0};   // high-water mark of in_use
