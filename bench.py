@@ -27,7 +27,7 @@ Three more workloads ride on the same JSON line (rank 0, one GPU each):
   batched   4096 SBM graphs through the batch call (disjoint unions), in
             graphs/s end to end, beside one call per graph on a sample
   serving   the continuous-batching server under Poisson arrivals: closed-
-            loop capacity and p50/p99 latency at 0.5x and 0.9x of it
+            loop capacity and p50/p99 latency at 0.25x-1.1x of it
 
 Multi-GPU: the path does not shard (a Louvain round needs the whole graph's
 cluster state), so N GPUs run N independent replicas ("replicas only").
@@ -400,7 +400,8 @@ def serving_leg(args, P, G, ctx):
     {0.01, 0.1, 0.5}, modularity or correlation with equal probability,
     120 GB HBM budget, `--serve-slots` concurrent slots.  Capacity is the
     closed-loop rate (every request queued at once); then Poisson arrivals at
-    0.5x and 0.9x that rate give latency percentiles (submit to completion).
+    0.25x, 0.5x, 0.75x, 0.9x and 1.1x that rate give latency percentiles
+    (submit to completion).
     Sampled responses must equal standalone calls."""
     import numpy as np
     reqs = G.serving_requests(args.serve_requests, seed=11, rmat_scale=20, distinct_rmat=2)
@@ -422,7 +423,7 @@ def serving_leg(args, P, G, ctx):
         _, cap_sbm = closed_loop(sbm_idx)
         _, cap_rmat = closed_loop(rmat_idx) if rmat_idx else (None, None)
         loads = []
-        for frac in (0.5, 0.9):
+        for frac in (0.25, 0.5, 0.75, 0.9, 1.1):
             lam = frac * capacity
             arrivals = np.cumsum(np.random.default_rng(13).exponential(1.0 / lam, len(reqs)))
             start = time.perf_counter()
@@ -436,7 +437,8 @@ def serving_leg(args, P, G, ctx):
             total = time.perf_counter() - start
             lat = np.array([x[2] for x in res])
             q = np.array([x[3] for x in res])
-            loads.append({"offered_graphs_per_s": lam, "achieved_graphs_per_s": len(reqs) / total,
+            loads.append({"offered_fraction_of_capacity": frac, "offered_graphs_per_s": lam,
+                          "achieved_graphs_per_s": len(reqs) / total,
                           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                           "mean_queue_ms": float(q.mean())})
     finally:
