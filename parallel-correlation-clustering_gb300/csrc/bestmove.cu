@@ -630,7 +630,10 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
     float U = -CUDART_INF_F;
     // The two largest upper ends (Y + e; +inf outside the error model) of
     // this lane's candidates and the index of the largest: when the second
-    // is below U, only that one can be a contender.
+    // is below U, only that one can be a contender.  Kept for the bins of
+    // more than 128 entries, where lanes hold several candidates (in the
+    // 33-128 bin it costs about what it saves).
+    constexpr bool kTop2 = HC >= 512;
     float hi1 = -CUDART_INF_F, hi2 = -CUDART_INF_F;
     uint32_t i1 = kNone;
     FilterVal rf[kCertRegRounds];
@@ -640,19 +643,20 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
       if (lane + 32 * r < nused) {
         rf[r] = FilterOf<V>(r32, k32, rKf[r], rS[r], smax, cabs);
         if (rf[r].sane) U = fmaxf(U, __fsub_rn(rf[r].Y, rf[r].e));
-        KeepTop2(hi1, hi2, i1, rf[r].sane ? __fadd_rn(rf[r].Y, rf[r].e) : CUDART_INF_F, lane + 32 * r);
+        if (kTop2) KeepTop2(hi1, hi2, i1, rf[r].sane ? __fadd_rn(rf[r].Y, rf[r].e) : CUDART_INF_F, lane + 32 * r);
       }
     }
     for (uint32_t i = lane + 32 * kCertRegRounds; i < nused; i += 32) {
       const uint32_t slot = used[i];
       const FilterVal f = FilterOf<V>(r32, k32, a.Kf[keys[slot]], vals[slot], smax, cabs);
       if (f.sane) U = fmaxf(U, __fsub_rn(f.Y, f.e));
-      KeepTop2(hi1, hi2, i1, f.sane ? __fadd_rn(f.Y, f.e) : CUDART_INF_F, i);
+      if (kTop2) KeepTop2(hi1, hi2, i1, f.sane ? __fadd_rn(f.Y, f.e) : CUDART_INF_F, i);
     }
     U = WarpMaxFinite(U);
     LexKeyT<V> lead, tail;
     // The contenders are the candidates with Y + e >= U (all when U = -inf).
-    if (hi2 < U) {
+    const bool skip = kTop2 && hi2 < U;
+    if (skip) {
       // At most candidate i1 is a contender: the others are cleared and
       // marked without evaluating them again.
       for (uint32_t i = lane; i < nused; i += 32) {
@@ -670,7 +674,7 @@ __global__ void __launch_bounds__(kWarpKernelWarps * 32) CertWarpKernel(BMArgs a
         used[i] = 0xFFFFu;
       }
     }
-    const uint32_t rescan_end = hi2 < U ? 0u : nused;
+    const uint32_t rescan_end = skip ? 0u : nused;
 #pragma unroll
     for (int r = 0; r < kCertRegRounds; ++r) {
       const uint32_t i = lane + 32 * r;
