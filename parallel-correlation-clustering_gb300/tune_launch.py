@@ -65,6 +65,19 @@ def _run(dg, cfg, objective):
     return P.correlation_cluster(dg, cfg)
 
 
+def pick_best(per_workload):
+    """The class's launch shape: the smallest sum over its workloads of
+    time / default-shape time (so that the workloads weigh equally); ties
+    keep the default.  per_workload: {workload: {"g/c/w": median ms}}.
+    Returns (best key, {key: score})."""
+    score = {}
+    for gmax, cta, waves in itertools.product(GROUP_MAX, CTA_MIN, WAVES):
+        key = f"{gmax}/{cta}/{waves}"
+        score[key] = sum(r[key] / r[DEFAULT] for r in per_workload.values())
+    best = min(score, key=lambda k: (score[k], k != DEFAULT))
+    return best, score
+
+
 def tune(reps: int, quick: bool):
     ctx = P.Context()
     results = {}
@@ -91,13 +104,7 @@ def tune(reps: int, quick: bool):
             per_workload[name] = rows
             ctx.set_launch_tuning(0, 0, 0.0)
             dg.free()
-        # Score: sum over the class's workloads of time / default time, so
-        # that the workloads weigh equally; ties keep the default.
-        score = {}
-        for gmax, cta, waves in itertools.product(GROUP_MAX, CTA_MIN, WAVES):
-            key = f"{gmax}/{cta}/{waves}"
-            score[key] = sum(r[key] / r[DEFAULT] for r in per_workload.values())
-        best = min(score, key=lambda k: (score[k], k != DEFAULT))
+        best, score = pick_best(per_workload)
         gmax, cta, waves = best.split("/")
         table.append((cls, int(gmax), int(cta), float(waves)))
         results[str(cls)] = {"workloads": per_workload, "score": score, "best": best}
